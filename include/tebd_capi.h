@@ -1,0 +1,138 @@
+/*
+ * tebd_capi.h -- C ABI of the GB300 (sm_103a) Vidal two-site TEBD update.
+ *
+ * This is the drop-in boundary for the reference's hot path.  Every entry point
+ * replaces one routine of OpenTEBD-extended (paths relative to that tree) and is
+ * callable from Fortran through ISO_C_BINDING (plain pointers, ints, doubles):
+ *
+ *   tebd_two_site_op       TwoSiteOp_c    VidalCore_v_2.0/local_operations_module.f90:463-494
+ *   tebd_two_site_op_r     TwoSiteOp_r    local_operations_module.f90:430-461
+ *   tebd_two_site_op_nc    TwoSiteOpNC_c  local_operations_module.f90:1845-1964
+ *   tebd_two_site_op_nc_r  TwoSiteOpNC_r  local_operations_module.f90:1723-1843
+ *   tebd_trotter_step      TrotterStep / TrotterStepNC with BoundaryCond='O'
+ *                          VidalCore_v_2.0/propagation_module.f90:42-114,200-252,890-1018
+ *   tebd_create/destroy    AllocateGamLam + AllocateLabel + SVDInit/SVDFinish
+ *                          VidalCore_v_2.0/TEBDtools_module.f90:486-521,589-620;
+ *                          local_operations_module.f90:84-151
+ *   tebd_set/get_gamma, tebd_set/get_lambda, tebd_set/get_labels
+ *                          the Gammas(:)%t / Lambdas(:)%v / LabelLeft,LabelRight(:)%vi
+ *                          arrays the reference passes by pointer
+ *                          (TEBDtools_module.f90:31-57)
+ *
+ * Layouts are exactly the Fortran ones, so a Fortran host passes C_LOC of its
+ * arrays without any transpose:
+ *   Gamma(site)   COMPLEX(8) (chi, d, chi), column-major, interleaved (re, im)
+ *                 doubles: element (alpha,i,beta) at 2*(alpha + chi*(i + d*beta))
+ *   Lambda(link)  REAL(8) (chi)
+ *   Labels(link)  INTEGER(4) (chi); 10000 marks an unused Schmidt index
+ *   Op2           (d*d, d*d) column-major; row index (i-1)*d + j (1-based): the
+ *                 right site's index runs fastest.  Complex Op2 interleaved.
+ * Sites are numbered 1..L and links 1..L+1, as in the reference; bond `link`
+ * couples sites link and link+1.
+ *
+ * Truncation parameters are the reference's: keep chi singular values, zero
+ * guard 1e-15 (dense, single-precision literal) and 1e-10 (number conserving).
+ *
+ * Threading: one handle per host thread; calls on one handle are serialised
+ * on the handle's own CUDA stream.  No call aborts the process: every entry
+ * point returns a status code and tebd_last_error() explains the last failure.
+ */
+#ifndef TEBD_CAPI_H
+#define TEBD_CAPI_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define TEBD_OK 0
+#define TEBD_ERR_ARG 1            /* invalid argument (size, index, mode)            */
+#define TEBD_ERR_CUDA 2           /* a CUDA runtime call failed                       */
+#define TEBD_ERR_OOM 3            /* device or host allocation failed                 */
+#define TEBD_ERR_SVD_NOCONV 4     /* Jacobi SVD hit its sweep cap before converging   */
+#define TEBD_ERR_NONFINITE 5      /* NaN/Inf met in Theta or in the singular values   */
+#define TEBD_ERR_STATE 6          /* call not valid in this handle's mode             */
+#define TEBD_ERR_NC_BLOCKS 7      /* a charge label fell outside the block range      */
+
+/* handle modes */
+#define TEBD_MODE_DENSE 0         /* TwoSiteOp: no symmetry                            */
+#define TEBD_MODE_NC 1            /* TwoSiteOpNC: U(1) number conservation             */
+
+/* SVD precision */
+#define TEBD_SVD_FP64 0           /* plain: FP64 one-sided Jacobi from the start        */
+#define TEBD_SVD_MIXED 1          /* FP32 Jacobi sweeps, then FP64 sweeps to converge   */
+
+#define TEBD_OPTS_VERSION 1
+
+typedef struct tebd_opts {
+  int version;        /* must be TEBD_OPTS_VERSION                                     */
+  int device;         /* CUDA device ordinal                                           */
+  int tot_num;        /* NC mode: total particle number (reference global totNum)      */
+  int max_filling;    /* NC mode: maximum occupation (reference global maxFilling)     */
+  int svd_mode;       /* TEBD_SVD_FP64 or TEBD_SVD_MIXED                               */
+  int max_sweeps;     /* Jacobi sweep cap; 0 selects the default (60)                  */
+  int max_batch;      /* bonds updated concurrently; 0 = all bonds of one parity       */
+  int reserved;
+  double jacobi_tol;  /* relative orthogonality tolerance; 0 = sqrt(n)*eps             */
+} tebd_opts;
+
+typedef struct tebd_handle tebd_handle;
+
+/* Fill *opts with defaults (dense-independent fields zero, version set). */
+void tebd_default_opts(tebd_opts *opts);
+
+/* Allocate the device-resident chain (L Gammas chi x d x chi, L+1 Lambdas, labels)
+ * and the per-bond SVD workspaces.  Gammas and Lambdas start at zero and labels
+ * at 10000, as AllocateGamLam/AllocateLabel leave them. */
+int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opts, tebd_handle **out);
+int tebd_destroy(tebd_handle *h);
+
+int tebd_set_gamma(tebd_handle *h, int site, const double *gamma);
+int tebd_get_gamma(tebd_handle *h, int site, double *gamma);
+int tebd_set_lambda(tebd_handle *h, int link, const double *lambda);
+int tebd_get_lambda(tebd_handle *h, int link, double *lambda);
+/* NC mode only: LabelLeft(link)%vi and LabelRight(link)%vi (either pointer may be NULL) */
+int tebd_set_labels(tebd_handle *h, int link, const int *label_left, const int *label_right);
+int tebd_get_labels(tebd_handle *h, int link, int *label_left, int *label_right);
+
+/* One bond update; replaces TwoSiteOp(link, Op2, Gammas, Lambdas, truncerr).
+ * op2 is complex (d^2 x d^2, interleaved) for tebd_two_site_op, real for _r. */
+int tebd_two_site_op(tebd_handle *h, int link, const double *op2, double *truncerr);
+int tebd_two_site_op_r(tebd_handle *h, int link, const double *op2, double *truncerr);
+
+/* Number-conserving bond update; replaces TwoSiteOpNC(link, Op2, Gammas, Lambdas,
+ * LabelLeft, LabelRight, truncerr) without the intDegFree argument. */
+int tebd_two_site_op_nc(tebd_handle *h, int link, const double *op2, double *truncerr);
+int tebd_two_site_op_nc_r(tebd_handle *h, int link, const double *op2, double *truncerr);
+
+/* Update several bonds that share no site (e.g. all odd links) in one batched
+ * launch sequence.  gates[k] is the complex Op2 for links[k]; truncerr[k] out.
+ * Dense or NC according to the handle's mode. */
+int tebd_apply_bonds(tebd_handle *h, int nbonds, const int *links, const double *const *gates,
+                     double *truncerr);
+
+/* One open-boundary Trotter step; replaces TrotterStep(Udt, Gammas, Lambdas,
+ * totalTruncerr) (dense mode) or TrotterStepNC(...) (NC mode).
+ * order 2: gates[link-1] = Udt(link), link = 1..L-1 (n_gates >= L-1).
+ * order 5 (Forest-Ruth): gates[g-1] = Udt(g), g = 1..2(L-1) (n_gates >= 2(L-2)+2).
+ * Same-parity bonds of each sweep are batched. */
+int tebd_trotter_step(tebd_handle *h, int order, int n_gates, const double *const *gates,
+                      double *total_truncerr);
+
+/* All d*chi singular values of the normalised Theta from the last update of
+ * `link` (descending; NC mode: the flattened block values in the reference's
+ * order).  *count receives how many were written (buffer holds d*chi). */
+int tebd_get_singular_values(tebd_handle *h, int link, double *sigma, int *count);
+
+/* Jacobi sweeps used by the last update of `link` (diagnostics). */
+int tebd_get_sweeps(tebd_handle *h, int link, int *sweeps);
+
+int tebd_sync(tebd_handle *h);
+const char *tebd_last_error(tebd_handle *h);
+/* Number of CUDA kernel launches issued by this handle since creation. */
+long long tebd_kernel_launches(tebd_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TEBD_CAPI_H */

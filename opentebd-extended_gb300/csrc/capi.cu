@@ -1,0 +1,517 @@
+// capi.cu -- the extern "C" boundary (include/tebd_capi.h) and its host orchestration.
+//
+// Host-side mirror of the reference's call structure:
+//   tebd_two_site_op(_r)     TwoSiteOp_c/_r   local_operations_module.f90:430-494
+//   tebd_two_site_op_nc(_r)  TwoSiteOpNC_c/_r local_operations_module.f90:1723-1964
+//   tebd_trotter_step        TrotterStep2ndOrder / TrotterStep5thOrder (OBC) and the NC twins
+//                            propagation_module.f90:82-114, 200-252, 956-1018
+// The reference applies the bonds of one sweep one after another; bonds of one
+// parity touch disjoint Gammas and Lambda(link+1) and only read the shared outer
+// Lambdas, so here each sweep is one batch (tebd_apply_bonds).  Truncation errors
+// are summed on the host in the reference's bond order.
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tebd_internal.cuh"
+
+using tebd::Slot;
+
+namespace tebd {
+
+int set_error(tebd_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int check_cuda(tebd_handle *h, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return TEBD_OK;
+  (void)cudaGetLastError();
+  return set_error(h, e == cudaErrorMemoryAllocation ? TEBD_ERR_OOM : TEBD_ERR_CUDA,
+                   std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// pinned staging layout
+constexpr size_t kPinFlags = 0;        // 64 bytes: pending count, status flags
+constexpr size_t kPinTrunc = 64;       // nslots doubles
+static size_t pin_gates_off(const tebd_handle *h) {
+  return (kPinTrunc + sizeof(double) * h->nslots + 255) & ~(size_t)255;
+}
+static size_t pin_links_off(const tebd_handle *h) {
+  return pin_gates_off(h) + sizeof(double2) * (size_t)h->nslots * h->d * h->d * h->d * h->d;
+}
+
+}  // namespace tebd
+
+using namespace tebd;
+
+static thread_local std::string g_noh_err;
+
+#define CK(expr, what)                                   \
+  do {                                                   \
+    int _rc = tebd::check_cuda(h, (expr), (what));       \
+    if (_rc) return _rc;                                 \
+  } while (0)
+
+extern "C" void tebd_default_opts(tebd_opts *o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->version = TEBD_OPTS_VERSION;
+}
+
+static void free_all(tebd_handle *h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->gam);
+  cudaFree(h->lam);
+  cudaFree(h->lab_l);
+  cudaFree(h->lab_r);
+  cudaFree(h->ws_base);
+  cudaFree(h->slots_d);
+  cudaFree(h->gates_d);
+  cudaFree(h->nrm_part);
+  cudaFree(h->nrm);
+  cudaFree(h->truncerr_d);
+  cudaFree(h->links_d);
+  cudaFree(h->js.rot);
+  cudaFree(h->js.done);
+  cudaFree(h->js.sweeps);
+  cudaFree(h->js.pending);
+  cudaFree(h->jprob_d);
+  cudaFree(h->jprobf_d);
+  cudaFree(h->status_d);
+  cudaFree(h->sig_link_d);
+  cudaFree(h->sig_count_d);
+  cudaFree(h->sweeps_link_d);
+  tebd::nc_free(h);
+  if (h->pinned) cudaFreeHost(h->pinned);
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+template <typename P>
+static int dalloc(tebd_handle *h, P **p, size_t bytes, const char *what) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  return tebd::check_cuda(h, cudaMalloc((void **)p, bytes), what);
+}
+
+extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opts,
+                           tebd_handle **out) {
+  if (!out) return TEBD_ERR_ARG;
+  *out = nullptr;
+  tebd_opts o;
+  tebd_default_opts(&o);
+  if (opts) {
+    if (opts->version != TEBD_OPTS_VERSION) {
+      g_noh_err = "tebd_create: opts.version mismatch";
+      return TEBD_ERR_ARG;
+    }
+    o = *opts;
+  }
+  if (L < 2 || d < 1 || d > 8 || chi < 1 || (mode != TEBD_MODE_DENSE && mode != TEBD_MODE_NC) ||
+      (o.svd_mode != TEBD_SVD_FP64 && o.svd_mode != TEBD_SVD_MIXED)) {
+    g_noh_err = "tebd_create: invalid L/d/chi/mode (need L>=2, 1<=d<=8, chi>=1)";
+    return TEBD_ERR_ARG;
+  }
+  if ((long long)d * chi > 8192) {
+    g_noh_err = "tebd_create: d*chi > 8192 is not supported";
+    return TEBD_ERR_ARG;
+  }
+  if (mode == TEBD_MODE_NC && (o.tot_num < 0 || o.max_filling < 0)) {
+    g_noh_err = "tebd_create: NC mode needs tot_num >= 0 and max_filling >= 0";
+    return TEBD_ERR_ARG;
+  }
+  tebd_handle *h = new (std::nothrow) tebd_handle();
+  if (!h) return TEBD_ERR_OOM;
+  h->L = L;
+  h->d = d;
+  h->chi = chi;
+  h->mode = mode;
+  h->n = d * chi;
+  h->opts = o;
+  h->device = o.device;
+  h->launches = 0;
+  int rc;
+#define FAIL(code)                 \
+  do {                             \
+    g_noh_err = h->err;            \
+    free_all(h);                   \
+    delete h;                      \
+    return (code);                 \
+  } while (0)
+  if ((rc = check_cuda(h, cudaSetDevice(o.device), "cudaSetDevice"))) FAIL(rc);
+  cudaDeviceProp prop;
+  if ((rc = check_cuda(h, cudaGetDeviceProperties(&prop, o.device), "cudaGetDeviceProperties")))
+    FAIL(rc);
+  if (prop.major * 10 + prop.minor != 103) {
+    set_error(h, TEBD_ERR_CUDA,
+              "this library is built for sm_103a (GB300); device is sm_" +
+                  std::to_string(prop.major * 10 + prop.minor));
+    FAIL(TEBD_ERR_CUDA);
+  }
+  if ((rc = check_cuda(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking),
+                       "cudaStreamCreate")))
+    FAIL(rc);
+  const int n = h->n;
+  const size_t csz = (size_t)chi * d * chi;
+  // slots: at most one per bond of one parity
+  int maxpar = L / 2;
+  if (maxpar < 1) maxpar = 1;
+  h->nslots = (o.max_batch > 0 && o.max_batch < maxpar) ? o.max_batch : maxpar;
+  const int ns = h->nslots;
+  if ((rc = dalloc(h, &h->gam, sizeof(double2) * csz * L, "alloc Gammas"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->lam, sizeof(double) * (size_t)chi * (L + 1), "alloc Lambdas"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->lab_l, sizeof(int) * (size_t)chi * (L + 1), "alloc labels"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->lab_r, sizeof(int) * (size_t)chi * (L + 1), "alloc labels"))) FAIL(rc);
+  // workspace carve
+  const bool mixed = o.svd_mode == TEBD_SVD_MIXED;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t nn = (size_t)n * n;
+  size_t per = al(sizeof(double2) * nn) * 2 + al(sizeof(double) * n) + al(sizeof(int) * n) +
+               al(sizeof(double2) * (size_t)d * d * d * d);
+  if (mixed) per += al(sizeof(float2) * nn) * 2 + al(sizeof(double2) * nn);
+  h->ws_bytes = per * ns;
+  if ((rc = dalloc(h, (char **)&h->ws_base, h->ws_bytes, "alloc SVD workspaces"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->gates_d, sizeof(double2) * (size_t)ns * d * d * d * d, "alloc gates")))
+    FAIL(rc);
+  h->slots.resize(ns);
+  {
+    char *p = (char *)h->ws_base;
+    for (int s = 0; s < ns; ++s) {
+      Slot &S = h->slots[s];
+      memset(&S, 0, sizeof(S));
+      S.X = (double2 *)p;
+      p += al(sizeof(double2) * nn);
+      S.V = (double2 *)p;
+      p += al(sizeof(double2) * nn);
+      S.S = (double *)p;
+      p += al(sizeof(double) * n);
+      S.perm = (int *)p;
+      p += al(sizeof(int) * n);
+      p += al(sizeof(double2) * (size_t)d * d * d * d);  // unused: gates live in gates_d
+      if (mixed) {
+        S.Xf = (float2 *)p;
+        p += al(sizeof(float2) * nn);
+        S.Vf = (float2 *)p;
+        p += al(sizeof(float2) * nn);
+        S.theta0 = (double2 *)p;
+        p += al(sizeof(double2) * nn);
+      }
+      S.gate = h->gates_d + (size_t)s * d * d * d * d;
+    }
+  }
+  if ((rc = dalloc(h, &h->slots_d, sizeof(Slot) * ns, "alloc slot table"))) FAIL(rc);
+  if ((rc = check_cuda(h, cudaMemcpy(h->slots_d, h->slots.data(), sizeof(Slot) * ns,
+                                     cudaMemcpyHostToDevice),
+                       "upload slot table")))
+    FAIL(rc);
+  {
+    std::vector<JacobiProblem<double>> jp(ns);
+    for (int s = 0; s < ns; ++s) jp[s] = {h->slots[s].X, h->slots[s].V, n, n, n, n};
+    if ((rc = dalloc(h, (char **)&h->jprob_d, sizeof(JacobiProblem<double>) * ns, "alloc jprob")))
+      FAIL(rc);
+    if ((rc = check_cuda(h, cudaMemcpy(h->jprob_d, jp.data(), sizeof(JacobiProblem<double>) * ns,
+                                       cudaMemcpyHostToDevice),
+                         "upload jprob")))
+      FAIL(rc);
+    if (mixed) {
+      std::vector<JacobiProblem<float>> jf(ns);
+      for (int s = 0; s < ns; ++s) jf[s] = {h->slots[s].Xf, h->slots[s].Vf, n, n, n, n};
+      if ((rc = dalloc(h, (char **)&h->jprobf_d, sizeof(JacobiProblem<float>) * ns, "alloc jprobf")))
+        FAIL(rc);
+      if ((rc = check_cuda(h, cudaMemcpy(h->jprobf_d, jf.data(), sizeof(JacobiProblem<float>) * ns,
+                                         cudaMemcpyHostToDevice),
+                           "upload jprobf")))
+        FAIL(rc);
+    }
+  }
+  if ((rc = dalloc(h, &h->nrm_part, sizeof(double) * ns * kNormParts, "alloc norm"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->nrm, sizeof(double) * ns, "alloc norm"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->truncerr_d, sizeof(double) * ns, "alloc truncerr"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->links_d, sizeof(int) * ns, "alloc links"))) FAIL(rc);
+  h->js_cap = ns * (mode == TEBD_MODE_NC ? (o.tot_num + 2 > 64 ? o.tot_num + 2 : 64) : 1);
+  if ((rc = dalloc(h, &h->js.rot, sizeof(int) * h->js_cap, "alloc jacobi state"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->js.done, sizeof(int) * h->js_cap, "alloc jacobi state"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->js.sweeps, sizeof(int) * h->js_cap, "alloc jacobi state"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->js.pending, sizeof(int) * 4, "alloc jacobi state"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->status_d, sizeof(int) * 4, "alloc status"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->sig_link_d, sizeof(double) * (size_t)(L - 1) * n, "alloc spectra")))
+    FAIL(rc);
+  if ((rc = dalloc(h, &h->sig_count_d, sizeof(int) * (L - 1), "alloc spectra"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->sweeps_link_d, sizeof(int) * (L - 1), "alloc spectra"))) FAIL(rc);
+  h->pinned_bytes = pin_links_off(h) + sizeof(int) * ns + 256;
+  if ((rc = check_cuda(h, cudaMallocHost((void **)&h->pinned, h->pinned_bytes), "alloc pinned")))
+    FAIL(rc);
+  // initial state as AllocateGamLam / AllocateLabel leave it: zeros and label 10000
+  if ((rc = check_cuda(h, cudaMemset(h->gam, 0, sizeof(double2) * csz * L), "memset"))) FAIL(rc);
+  if ((rc = check_cuda(h, cudaMemset(h->lam, 0, sizeof(double) * (size_t)chi * (L + 1)), "memset")))
+    FAIL(rc);
+  if ((rc = check_cuda(h, cudaMemset(h->status_d, 0, sizeof(int) * 4), "memset"))) FAIL(rc);
+  if ((rc = check_cuda(h, cudaMemset(h->sig_count_d, 0, sizeof(int) * (L - 1)), "memset"))) FAIL(rc);
+  if ((rc = check_cuda(h, cudaMemset(h->sweeps_link_d, 0, sizeof(int) * (L - 1)), "memset")))
+    FAIL(rc);
+  {
+    std::vector<int> lab((size_t)chi * (L + 1), kLabelUnused);
+    if ((rc = check_cuda(h, cudaMemcpy(h->lab_l, lab.data(), sizeof(int) * lab.size(),
+                                       cudaMemcpyHostToDevice), "init labels")))
+      FAIL(rc);
+    if ((rc = check_cuda(h, cudaMemcpy(h->lab_r, lab.data(), sizeof(int) * lab.size(),
+                                       cudaMemcpyHostToDevice), "init labels")))
+      FAIL(rc);
+  }
+  if (mode == TEBD_MODE_NC) {
+    if ((rc = tebd::nc_alloc(h))) FAIL(rc);
+  }
+#undef FAIL
+  *out = h;
+  return TEBD_OK;
+}
+
+extern "C" int tebd_destroy(tebd_handle *h) {
+  if (!h) return TEBD_ERR_ARG;
+  free_all(h);
+  delete h;
+  return TEBD_OK;
+}
+
+extern "C" const char *tebd_last_error(tebd_handle *h) {
+  return h ? h->err.c_str() : g_noh_err.c_str();
+}
+
+extern "C" long long tebd_kernel_launches(tebd_handle *h) { return h ? h->launches : -1; }
+
+extern "C" int tebd_sync(tebd_handle *h) {
+  if (!h) return TEBD_ERR_ARG;
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  CK(cudaStreamSynchronize(h->stream), "tebd_sync");
+  return TEBD_OK;
+}
+
+static int xfer(tebd_handle *h, void *dst, const void *src, size_t bytes, cudaMemcpyKind k,
+                const char *what) {
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  CK(cudaMemcpyAsync(dst, src, bytes, k, h->stream), what);
+  CK(cudaStreamSynchronize(h->stream), what);
+  return TEBD_OK;
+}
+
+extern "C" int tebd_set_gamma(tebd_handle *h, int site, const double *g) {
+  if (!h || !g) return TEBD_ERR_ARG;
+  if (site < 1 || site > h->L) return set_error(h, TEBD_ERR_ARG, "tebd_set_gamma: site out of range");
+  const size_t csz = (size_t)h->chi * h->d * h->chi;
+  return xfer(h, h->gam + (site - 1) * csz, g, sizeof(double2) * csz, cudaMemcpyHostToDevice,
+              "tebd_set_gamma");
+}
+
+extern "C" int tebd_get_gamma(tebd_handle *h, int site, double *g) {
+  if (!h || !g) return TEBD_ERR_ARG;
+  if (site < 1 || site > h->L) return set_error(h, TEBD_ERR_ARG, "tebd_get_gamma: site out of range");
+  const size_t csz = (size_t)h->chi * h->d * h->chi;
+  return xfer(h, g, h->gam + (site - 1) * csz, sizeof(double2) * csz, cudaMemcpyDeviceToHost,
+              "tebd_get_gamma");
+}
+
+extern "C" int tebd_set_lambda(tebd_handle *h, int link, const double *l) {
+  if (!h || !l) return TEBD_ERR_ARG;
+  if (link < 1 || link > h->L + 1)
+    return set_error(h, TEBD_ERR_ARG, "tebd_set_lambda: link out of range");
+  return xfer(h, h->lam + (size_t)(link - 1) * h->chi, l, sizeof(double) * h->chi,
+              cudaMemcpyHostToDevice, "tebd_set_lambda");
+}
+
+extern "C" int tebd_get_lambda(tebd_handle *h, int link, double *l) {
+  if (!h || !l) return TEBD_ERR_ARG;
+  if (link < 1 || link > h->L + 1)
+    return set_error(h, TEBD_ERR_ARG, "tebd_get_lambda: link out of range");
+  return xfer(h, l, h->lam + (size_t)(link - 1) * h->chi, sizeof(double) * h->chi,
+              cudaMemcpyDeviceToHost, "tebd_get_lambda");
+}
+
+extern "C" int tebd_set_labels(tebd_handle *h, int link, const int *ll, const int *lr) {
+  if (!h) return TEBD_ERR_ARG;
+  if (h->mode != TEBD_MODE_NC) return set_error(h, TEBD_ERR_STATE, "labels need TEBD_MODE_NC");
+  if (link < 1 || link > h->L + 1)
+    return set_error(h, TEBD_ERR_ARG, "tebd_set_labels: link out of range");
+  int rc;
+  if (ll && (rc = xfer(h, h->lab_l + (size_t)(link - 1) * h->chi, ll, sizeof(int) * h->chi,
+                       cudaMemcpyHostToDevice, "tebd_set_labels")))
+    return rc;
+  if (lr && (rc = xfer(h, h->lab_r + (size_t)(link - 1) * h->chi, lr, sizeof(int) * h->chi,
+                       cudaMemcpyHostToDevice, "tebd_set_labels")))
+    return rc;
+  return TEBD_OK;
+}
+
+extern "C" int tebd_get_labels(tebd_handle *h, int link, int *ll, int *lr) {
+  if (!h) return TEBD_ERR_ARG;
+  if (h->mode != TEBD_MODE_NC) return set_error(h, TEBD_ERR_STATE, "labels need TEBD_MODE_NC");
+  if (link < 1 || link > h->L + 1)
+    return set_error(h, TEBD_ERR_ARG, "tebd_get_labels: link out of range");
+  int rc;
+  if (ll && (rc = xfer(h, ll, h->lab_l + (size_t)(link - 1) * h->chi, sizeof(int) * h->chi,
+                       cudaMemcpyDeviceToHost, "tebd_get_labels")))
+    return rc;
+  if (lr && (rc = xfer(h, lr, h->lab_r + (size_t)(link - 1) * h->chi, sizeof(int) * h->chi,
+                       cudaMemcpyDeviceToHost, "tebd_get_labels")))
+    return rc;
+  return TEBD_OK;
+}
+
+extern "C" int tebd_get_singular_values(tebd_handle *h, int link, double *sigma, int *count) {
+  if (!h || !sigma || !count) return TEBD_ERR_ARG;
+  if (link < 1 || link > h->L - 1)
+    return set_error(h, TEBD_ERR_ARG, "tebd_get_singular_values: link out of range");
+  int rc;
+  if ((rc = xfer(h, count, h->sig_count_d + (link - 1), sizeof(int), cudaMemcpyDeviceToHost,
+                 "get spectrum count")))
+    return rc;
+  if (*count > 0)
+    return xfer(h, sigma, h->sig_link_d + (size_t)(link - 1) * h->n, sizeof(double) * *count,
+                cudaMemcpyDeviceToHost, "get spectrum");
+  return TEBD_OK;
+}
+
+extern "C" int tebd_get_sweeps(tebd_handle *h, int link, int *sweeps) {
+  if (!h || !sweeps) return TEBD_ERR_ARG;
+  if (link < 1 || link > h->L - 1)
+    return set_error(h, TEBD_ERR_ARG, "tebd_get_sweeps: link out of range");
+  return xfer(h, sweeps, h->sweeps_link_d + (link - 1), sizeof(int), cudaMemcpyDeviceToHost,
+              "get sweeps");
+}
+
+// One batch of at most nslots non-overlapping bonds (complex gates).
+static int run_batch(tebd_handle *h, int nb, const int *links, const double *const *gates,
+                     double *truncerr) {
+  const int d4 = h->d * h->d * h->d * h->d;
+  char *pin = (char *)h->pinned;
+  double2 *g_pin = (double2 *)(pin + pin_gates_off(h));
+  int *l_pin = (int *)(pin + pin_links_off(h));
+  for (int s = 0; s < nb; ++s) {
+    memcpy(g_pin + (size_t)s * d4, gates[s], sizeof(double2) * d4);
+    l_pin[s] = links[s];
+  }
+  CK(cudaMemcpyAsync(h->gates_d, g_pin, sizeof(double2) * (size_t)nb * d4, cudaMemcpyHostToDevice,
+                     h->stream),
+     "upload gates");
+  CK(cudaMemcpyAsync(h->links_d, l_pin, sizeof(int) * nb, cudaMemcpyHostToDevice, h->stream),
+     "upload links");
+  CK(cudaMemsetAsync(h->status_d, 0, sizeof(int) * 4, h->stream), "reset status");
+  int rc;
+  if (h->mode == TEBD_MODE_DENSE) {
+    if ((rc = launch_dense_prepare(h, nb, false))) return rc;
+    if ((rc = launch_eye(h, nb))) return rc;
+    if ((rc = run_jacobi(h, nb, h->opts.svd_mode))) return rc;
+    if ((rc = launch_dense_finish(h, nb))) return rc;
+  } else {
+    if ((rc = run_nc_batch(h, nb, links, nullptr))) return rc;
+  }
+  double *t_pin = (double *)(pin + kPinTrunc);
+  int *f_pin = (int *)(pin + kPinFlags);
+  CK(cudaMemcpyAsync(t_pin, h->truncerr_d, sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream),
+     "read truncerr");
+  CK(cudaMemcpyAsync(f_pin + 4, h->status_d, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->stream),
+     "read status");
+  CK(cudaStreamSynchronize(h->stream), "bond batch");
+  for (int s = 0; s < nb; ++s) truncerr[s] = t_pin[s];
+  if (f_pin[4] & 1) return set_error(h, TEBD_ERR_NONFINITE, "non-finite value in Theta or sigma");
+  if (f_pin[5]) return set_error(h, TEBD_ERR_NC_BLOCKS, "charge label outside the block range");
+  return TEBD_OK;
+}
+
+static int apply_bonds_impl(tebd_handle *h, int nbonds, const int *links,
+                            const double *const *gates, double *truncerr) {
+  if (nbonds < 0 || (nbonds > 0 && (!links || !gates || !truncerr))) return TEBD_ERR_ARG;
+  for (int k = 0; k < nbonds; ++k) {
+    if (links[k] < 1 || links[k] > h->L - 1)
+      return set_error(h, TEBD_ERR_ARG, "bond link out of range 1..L-1");
+    if (!gates[k]) return set_error(h, TEBD_ERR_ARG, "null gate");
+    for (int q = 0; q < k; ++q)
+      if (abs(links[k] - links[q]) < 2)
+        return set_error(h, TEBD_ERR_ARG, "batched bonds must not share a site");
+  }
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  for (int c = 0; c < nbonds; c += h->nslots) {
+    const int nb = std::min(h->nslots, nbonds - c);
+    const int rc = run_batch(h, nb, links + c, gates + c, truncerr + c);
+    if (rc) return rc;
+  }
+  return TEBD_OK;
+}
+
+extern "C" int tebd_apply_bonds(tebd_handle *h, int nbonds, const int *links,
+                                const double *const *gates, double *truncerr) {
+  if (!h) return TEBD_ERR_ARG;
+  return apply_bonds_impl(h, nbonds, links, gates, truncerr);
+}
+
+static int one_bond(tebd_handle *h, int link, const double *op2, bool real, double *truncerr,
+                    int want_mode) {
+  if (!h || !op2 || !truncerr) return TEBD_ERR_ARG;
+  if (h->mode != want_mode)
+    return set_error(h, TEBD_ERR_STATE,
+                     want_mode == TEBD_MODE_NC ? "TwoSiteOpNC needs a TEBD_MODE_NC handle"
+                                               : "TwoSiteOp needs a TEBD_MODE_DENSE handle");
+  const int d2 = h->d * h->d;
+  std::vector<double> tmp;
+  const double *g = op2;
+  if (real) {  // ThetaOperation_r: the real gate enters as (op, 0)
+    tmp.assign((size_t)2 * d2 * d2, 0.0);
+    for (int e = 0; e < d2 * d2; ++e) tmp[2 * e] = op2[e];
+    g = tmp.data();
+  }
+  return apply_bonds_impl(h, 1, &link, &g, truncerr);
+}
+
+extern "C" int tebd_two_site_op(tebd_handle *h, int link, const double *op2, double *truncerr) {
+  return one_bond(h, link, op2, false, truncerr, TEBD_MODE_DENSE);
+}
+extern "C" int tebd_two_site_op_r(tebd_handle *h, int link, const double *op2, double *truncerr) {
+  return one_bond(h, link, op2, true, truncerr, TEBD_MODE_DENSE);
+}
+extern "C" int tebd_two_site_op_nc(tebd_handle *h, int link, const double *op2, double *truncerr) {
+  return one_bond(h, link, op2, false, truncerr, TEBD_MODE_NC);
+}
+extern "C" int tebd_two_site_op_nc_r(tebd_handle *h, int link, const double *op2,
+                                     double *truncerr) {
+  return one_bond(h, link, op2, true, truncerr, TEBD_MODE_NC);
+}
+
+// Sweep structure of TrotterStep2ndOrder (:82-114) and TrotterStep5thOrder (:200-252):
+// 2nd order: odd, even, odd links with gate Udt(link);
+// Forest-Ruth: odd,even,odd,even,odd,even,odd with gate Udt(2(link-1)+pick).
+extern "C" int tebd_trotter_step(tebd_handle *h, int order, int n_gates, const double *const *gates,
+                                 double *total_truncerr) {
+  if (!h || !gates || !total_truncerr) return TEBD_ERR_ARG;
+  if (order != 2 && order != 5)
+    return set_error(h, TEBD_ERR_ARG, "trotter order must be 2 or 5 (Forest-Ruth)");
+  const int L = h->L;
+  const int need = order == 2 ? L - 1 : 2 * (L - 2) + 2;
+  if (n_gates < need) return set_error(h, TEBD_ERR_ARG, "too few gates for this Trotter order");
+  static const int pick5[7] = {1, 1, 2, 2, 2, 1, 1};
+  const int nsweeps = order == 2 ? 3 : 7;
+  std::vector<int> links;
+  std::vector<const double *> gp;
+  std::vector<double> te;
+  double total = 0.0;
+  for (int s = 0; s < nsweeps; ++s) {
+    links.clear();
+    gp.clear();
+    for (int link = (s % 2 == 0) ? 1 : 2; link <= L - 1; link += 2) {
+      links.push_back(link);
+      const int gi = order == 2 ? link : 2 * (link - 1) + pick5[s];
+      gp.push_back(gates[gi - 1]);
+    }
+    te.assign(links.size(), 0.0);
+    const int rc = apply_bonds_impl(h, (int)links.size(), links.data(), gp.data(), te.data());
+    if (rc) return rc;
+    for (double v : te) total = total + v;
+  }
+  *total_truncerr = total;
+  return TEBD_OK;
+}

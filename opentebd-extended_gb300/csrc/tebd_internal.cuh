@@ -1,0 +1,141 @@
+// tebd_internal.cuh -- shared definitions of the sm_103a TEBD library.
+//
+// Device layout of one handle (all allocations made once in tebd_create):
+//   gam     L Gammas, each chi x d x chi complex, Fortran column-major, site-major
+//           (site s at offset s*chi*d*chi): the exact array a Fortran host holds.
+//   lam     L+1 Lambdas of length chi (link-major).
+//   lab_l/r L+1 label vectors of length chi (NC mode).
+//   slots   one SVD workspace per concurrently updated bond: the reshaped Theta X
+//           (n x n, n = d*chi, column-major, ld = n), the right factor V (n x n),
+//           FP32 shadows of both for the mixed-precision SVD, sorted singular
+//           values and their column permutation.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "tebd_capi.h"
+
+namespace tebd {
+
+// Fortran default-REAL literals used as guards by the reference:
+// `1E-15` (local_operations_module.f90:362,373,396,421) and `10.0**(-10)`
+// (:1591,1643,1679,1711) are single precision, widened to double at comparison.
+constexpr double kGuardDense = (double)1e-15f;
+constexpr double kGuardNC = (double)1e-10f;
+constexpr int kLabelUnused = 10000;
+
+// ---------------------------------------------------------------------------
+// complex helpers (interleaved re/im, same storage as COMPLEX(8))
+// ---------------------------------------------------------------------------
+template <typename T>
+struct cplx;
+template <>
+struct cplx<double> {
+  using type = double2;
+};
+template <>
+struct cplx<float> {
+  using type = float2;
+};
+
+__host__ __device__ inline double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ inline double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ inline double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__host__ __device__ inline double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+
+// ---------------------------------------------------------------------------
+// batched one-sided Jacobi SVD problem descriptor
+// ---------------------------------------------------------------------------
+// Each problem is an m x n column-major matrix X (ld = ldx) whose columns are
+// orthogonalised in place, with the right rotations accumulated into V
+// (n x n, ld = ldv).  After convergence X = U*Sigma (column k = sigma_k u_k).
+template <typename T>
+struct JacobiProblem {
+  typename cplx<T>::type *X;
+  typename cplx<T>::type *V;
+  int m, n, ldx, ldv;
+};
+
+struct JacobiState {
+  int *rot;      // rotations applied in the current sweep, per problem
+  int *done;     // 1 once a sweep applied no rotation
+  int *sweeps;   // sweeps executed, per problem
+  int *pending;  // [0] number of problems not yet converged (host reads it)
+};
+
+// ---------------------------------------------------------------------------
+// per-handle state
+// ---------------------------------------------------------------------------
+struct Slot {
+  double2 *X, *V;    // n x n FP64 Theta / right factor
+  float2 *Xf, *Vf;   // FP32 shadows (mixed SVD)
+  double2 *theta0;   // n x n copy of the gated, unnormalised Theta (mixed SVD)
+  double *S;         // n sorted singular values of the normalised Theta
+  int *perm;         // n column permutation (descending sigma)
+  double2 *gate;     // d^2 x d^2 gate for this slot
+};
+
+}  // namespace tebd
+
+struct tebd_handle {
+  int L, d, chi, mode, n;
+  tebd_opts opts;
+  int device;
+  cudaStream_t stream;
+  // chain
+  double2 *gam;
+  double *lam;
+  int *lab_l, *lab_r;
+  // workspaces
+  int nslots;
+  std::vector<tebd::Slot> slots;  // host copy of the slot table
+  tebd::Slot *slots_d;            // device copy of the slot table
+  void *ws_base;                  // single allocation carved into slots
+  size_t ws_bytes;
+  double2 *gates_d;               // nslots * d^4 gates of the current batch
+  double *nrm_part;       // nslots * kNormParts partial sums of |Theta|^2
+  double *nrm;            // nslots Frobenius norms
+  double *truncerr_d;     // nslots
+  int *links_d;           // nslots link numbers of the current batch
+  tebd::JacobiState js;
+  void *jprob_d;          // device array of JacobiProblem<double>
+  void *jprobf_d;         // device array of JacobiProblem<float>
+  int *status_d;          // [0] non-finite flag, [1] NC block error flag
+  // NC workspaces (allocated in NC mode)
+  void *nc_ws;
+  size_t nc_ws_bytes;
+  // last spectrum per link (tebd_get_singular_values / tebd_get_sweeps)
+  double *sig_link_d;            // (L-1) * n
+  int *sig_count_d;              // L-1
+  int *sweeps_link_d;            // L-1
+  int js_cap;                    // capacity of the JacobiState arrays (problems)
+  double *pinned;                // pinned staging buffer (gates, truncation errors, flags)
+  size_t pinned_bytes;
+  std::string err;
+  long long launches;
+};
+
+namespace tebd {
+
+int set_error(tebd_handle *h, int code, const std::string &msg);
+int check_cuda(tebd_handle *h, cudaError_t e, const char *what);
+
+// kernels launched from capi.cu (defined in the .cu files)
+int launch_dense_prepare(tebd_handle *h, int nb, bool real_gate);
+int run_jacobi(tebd_handle *h, int nb, int svd_mode);
+int launch_dense_finish(tebd_handle *h, int nb);
+int launch_eye(tebd_handle *h, int nb);
+int run_nc_batch(tebd_handle *h, int nb, const int *links_host, double *truncerr_host);
+int nc_alloc(tebd_handle *h);
+void nc_free(tebd_handle *h);
+
+constexpr int kNormParts = 64;
+
+}  // namespace tebd
+
+#define TEBD_LAUNCHED(h) ((h)->launches++)

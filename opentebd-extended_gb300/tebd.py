@@ -1,0 +1,307 @@
+"""Host-side mirror of the reference's TEBD interface over the sm_103a C ABI.
+
+The Fortran reference exposes (paths relative to the OpenTEBD-extended tree):
+
+* ``TwoSiteOp(link, Op2, Gammas, Lambdas, truncerr)``
+  (VidalCore_v_2.0/local_operations_module.f90:46-48, 430-494)
+* ``TwoSiteOpNC(link, Op2, Gammas, Lambdas, LabelLeft, LabelRight, truncerr)``
+  (local_operations_module.f90:54-56, 1723-1964)
+* ``TrotterStep(Udt, Gammas, Lambdas, totalTruncerr)`` and ``TrotterStepNC``
+  (VidalCore_v_2.0/propagation_module.f90:42-114, 200-252, 890-1018)
+
+Here the chain lives in device memory owned by a :class:`Chain` (the handle of
+``include/tebd_capi.h``); Gammas/Lambdas/labels move only on ``set_*``/``get_*``.
+The module-level functions :func:`TwoSiteOp`, :func:`TwoSiteOpNC` and
+:func:`TrotterStep` keep the reference's argument meaning (1-based links, gates
+as (d^2, d^2) matrices with the right site's index fastest) and return the
+truncation error the Fortran routines write to ``truncerr``.
+
+There is no CPU fallback: if ``lib/libtebd_gb300.so`` is missing or no sm_103
+device is present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libtebd_gb300.so")
+
+TEBD_OK = 0
+TEBD_ERR_ARG = 1
+TEBD_ERR_CUDA = 2
+TEBD_ERR_OOM = 3
+TEBD_ERR_SVD_NOCONV = 4
+TEBD_ERR_NONFINITE = 5
+TEBD_ERR_STATE = 6
+TEBD_ERR_NC_BLOCKS = 7
+MODE_DENSE = 0
+MODE_NC = 1
+SVD_FP64 = 0
+SVD_MIXED = 1
+OPTS_VERSION = 1
+
+ERROR_NAMES = {
+    TEBD_ERR_ARG: "TEBD_ERR_ARG",
+    TEBD_ERR_CUDA: "TEBD_ERR_CUDA",
+    TEBD_ERR_OOM: "TEBD_ERR_OOM",
+    TEBD_ERR_SVD_NOCONV: "TEBD_ERR_SVD_NOCONV",
+    TEBD_ERR_NONFINITE: "TEBD_ERR_NONFINITE",
+    TEBD_ERR_STATE: "TEBD_ERR_STATE",
+    TEBD_ERR_NC_BLOCKS: "TEBD_ERR_NC_BLOCKS",
+}
+
+# every symbol include/tebd_capi.h declares
+EXPORTED_SYMBOLS = (
+    "tebd_default_opts", "tebd_create", "tebd_destroy", "tebd_set_gamma", "tebd_get_gamma",
+    "tebd_set_lambda", "tebd_get_lambda", "tebd_set_labels", "tebd_get_labels",
+    "tebd_two_site_op", "tebd_two_site_op_r", "tebd_two_site_op_nc", "tebd_two_site_op_nc_r",
+    "tebd_apply_bonds", "tebd_trotter_step", "tebd_get_singular_values", "tebd_get_sweeps",
+    "tebd_sync", "tebd_last_error", "tebd_kernel_launches",
+)
+
+
+class TebdError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERROR_NAMES.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [
+        ("version", ctypes.c_int),
+        ("device", ctypes.c_int),
+        ("tot_num", ctypes.c_int),
+        ("max_filling", ctypes.c_int),
+        ("svd_mode", ctypes.c_int),
+        ("max_sweeps", ctypes.c_int),
+        ("max_batch", ctypes.c_int),
+        ("reserved", ctypes.c_int),
+        ("jacobi_tol", ctypes.c_double),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            "libtebd_gb300.so not found at %s: build it with "
+            "`python opentebd-extended_gb300/build.py` (there is no CPU fallback)" % path)
+    L = ctypes.CDLL(path)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    vp = ctypes.c_void_p
+    L.tebd_default_opts.argtypes = [ctypes.POINTER(Opts)]
+    L.tebd_default_opts.restype = None
+    L.tebd_create.argtypes = [ctypes.c_int] * 4 + [ctypes.POINTER(Opts), ctypes.POINTER(vp)]
+    L.tebd_destroy.argtypes = [vp]
+    for nm in ("tebd_set_gamma", "tebd_get_gamma", "tebd_set_lambda", "tebd_get_lambda"):
+        getattr(L, nm).argtypes = [vp, ctypes.c_int, dp]
+    L.tebd_set_labels.argtypes = [vp, ctypes.c_int, ip, ip]
+    L.tebd_get_labels.argtypes = [vp, ctypes.c_int, ip, ip]
+    for nm in ("tebd_two_site_op", "tebd_two_site_op_r", "tebd_two_site_op_nc", "tebd_two_site_op_nc_r"):
+        getattr(L, nm).argtypes = [vp, ctypes.c_int, dp, dp]
+    L.tebd_apply_bonds.argtypes = [vp, ctypes.c_int, ip, ctypes.POINTER(dp), dp]
+    L.tebd_trotter_step.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(dp), dp]
+    L.tebd_get_singular_values.argtypes = [vp, ctypes.c_int, dp, ip]
+    L.tebd_get_sweeps.argtypes = [vp, ctypes.c_int, ip]
+    L.tebd_sync.argtypes = [vp]
+    L.tebd_last_error.argtypes = [vp]
+    L.tebd_last_error.restype = ctypes.c_char_p
+    L.tebd_kernel_launches.argtypes = [vp]
+    L.tebd_kernel_launches.restype = ctypes.c_longlong
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _as_gate(op2, d):
+    """(d^2, d^2) gate -> Fortran-ordered complex128 array (the C ABI's layout)."""
+    g = np.asfortranarray(np.asarray(op2, dtype=np.complex128))
+    if g.shape != (d * d, d * d):
+        raise ValueError("gate must be (d^2, d^2) = (%d, %d), got %s" % (d * d, d * d, g.shape))
+    return g
+
+
+class Chain:
+    """Device-resident Vidal chain: L Gammas (chi, d, chi), L+1 Lambdas (chi,),
+    and in number-conserving mode LabelLeft/LabelRight (L+1, chi)."""
+
+    def __init__(self, L, d, chi, mode=MODE_DENSE, tot_num=0, max_filling=None,
+                 svd_mode=SVD_FP64, max_sweeps=0, max_batch=0, jacobi_tol=0.0, device=0):
+        self._lib = load_library()
+        o = Opts()
+        self._lib.tebd_default_opts(ctypes.byref(o))
+        o.device = device
+        o.tot_num = tot_num
+        o.max_filling = (d - 1) if max_filling is None else max_filling
+        o.svd_mode = svd_mode
+        o.max_sweeps = max_sweeps
+        o.max_batch = max_batch
+        o.jacobi_tol = jacobi_tol
+        h = ctypes.c_void_p()
+        rc = self._lib.tebd_create(L, d, chi, mode, ctypes.byref(o), ctypes.byref(h))
+        if rc != TEBD_OK:
+            raise TebdError(rc, self._lib.tebd_last_error(None).decode())
+        self.h = h
+        self.L, self.d, self.chi, self.mode = L, d, chi, mode
+        self.tot_num, self.max_filling = o.tot_num, o.max_filling
+
+    # -- lifetime -------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.tebd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc != TEBD_OK:
+            raise TebdError(rc, self._lib.tebd_last_error(self.h).decode())
+
+    # -- state transfer -------------------------------------------------------
+    def set_gamma(self, site, gamma):
+        g = np.asfortranarray(np.asarray(gamma, dtype=np.complex128))
+        assert g.shape == (self.chi, self.d, self.chi), g.shape
+        self._check(self._lib.tebd_set_gamma(self.h, site, _dp(g)))
+
+    def get_gamma(self, site):
+        g = np.zeros((self.chi, self.d, self.chi), dtype=np.complex128, order="F")
+        self._check(self._lib.tebd_get_gamma(self.h, site, _dp(g)))
+        return g
+
+    def set_lambda(self, link, lam):
+        v = np.ascontiguousarray(lam, dtype=np.float64)
+        assert v.shape == (self.chi,)
+        self._check(self._lib.tebd_set_lambda(self.h, link, _dp(v)))
+
+    def get_lambda(self, link):
+        v = np.zeros(self.chi)
+        self._check(self._lib.tebd_get_lambda(self.h, link, _dp(v)))
+        return v
+
+    def set_labels(self, link, left=None, right=None):
+        a = None if left is None else np.ascontiguousarray(left, dtype=np.int32)
+        b = None if right is None else np.ascontiguousarray(right, dtype=np.int32)
+        self._check(self._lib.tebd_set_labels(self.h, link, None if a is None else _ip(a),
+                                              None if b is None else _ip(b)))
+
+    def get_labels(self, link):
+        a = np.zeros(self.chi, dtype=np.int32)
+        b = np.zeros(self.chi, dtype=np.int32)
+        self._check(self._lib.tebd_get_labels(self.h, link, _ip(a), _ip(b)))
+        return a, b
+
+    def set_state(self, gammas, lambdas, label_left=None, label_right=None):
+        for s, g in enumerate(gammas, start=1):
+            self.set_gamma(s, g)
+        for l, v in enumerate(lambdas, start=1):
+            self.set_lambda(l, v)
+        if label_left is not None:
+            for l in range(1, self.L + 2):
+                self.set_labels(l, label_left[l - 1], label_right[l - 1])
+
+    def get_state(self):
+        gam = [self.get_gamma(s) for s in range(1, self.L + 1)]
+        lam = [self.get_lambda(l) for l in range(1, self.L + 2)]
+        if self.mode == MODE_NC:
+            ll, lr = zip(*[self.get_labels(l) for l in range(1, self.L + 2)])
+            return gam, lam, list(ll), list(lr)
+        return gam, lam
+
+    # -- the hot path -----------------------------------------------------------
+    def two_site_op(self, link, op2):
+        """TwoSiteOp / TwoSiteOpNC on bond `link` (1-based); returns truncerr."""
+        op2 = np.asarray(op2)
+        te = np.zeros(1)
+        if np.iscomplexobj(op2):
+            g = _as_gate(op2, self.d)
+            fn = self._lib.tebd_two_site_op_nc if self.mode == MODE_NC else self._lib.tebd_two_site_op
+        else:
+            g = np.asfortranarray(op2, dtype=np.float64)
+            if g.shape != (self.d ** 2, self.d ** 2):
+                raise ValueError("gate must be (d^2, d^2)")
+            fn = self._lib.tebd_two_site_op_nc_r if self.mode == MODE_NC else self._lib.tebd_two_site_op_r
+        self._check(fn(self.h, link, _dp(g), _dp(te)))
+        return float(te[0])
+
+    def apply_bonds(self, links, gates):
+        """Batched update of non-overlapping bonds; returns the truncation errors."""
+        gs = [_as_gate(g, self.d) for g in gates]
+        arr = (ctypes.POINTER(ctypes.c_double) * len(gs))(*[_dp(g) for g in gs])
+        lk = np.ascontiguousarray(links, dtype=np.int32)
+        te = np.zeros(len(gs))
+        self._check(self._lib.tebd_apply_bonds(self.h, len(gs), _ip(lk), arr, _dp(te)))
+        return te
+
+    def trotter_step(self, Udt, order=2):
+        """TrotterStep(Udt, ...) with open boundaries; Udt[g-1] is the reference's Udt(g)."""
+        gs = [_as_gate(g, self.d) for g in Udt]
+        arr = (ctypes.POINTER(ctypes.c_double) * len(gs))(*[_dp(g) for g in gs])
+        te = np.zeros(1)
+        self._check(self._lib.tebd_trotter_step(self.h, order, len(gs), arr, _dp(te)))
+        return float(te[0])
+
+    def singular_values(self, link):
+        s = np.zeros(self.d * self.chi)
+        c = np.zeros(1, dtype=np.int32)
+        self._check(self._lib.tebd_get_singular_values(self.h, link, _dp(s), _ip(c)))
+        return s[: int(c[0])].copy()
+
+    def sweeps(self, link):
+        c = np.zeros(1, dtype=np.int32)
+        self._check(self._lib.tebd_get_sweeps(self.h, link, _ip(c)))
+        return int(c[0])
+
+    def sync(self):
+        self._check(self._lib.tebd_sync(self.h))
+
+    def kernel_launches(self):
+        return int(self._lib.tebd_kernel_launches(self.h))
+
+
+# -- reference-named entry points ---------------------------------------------
+def TwoSiteOp(link, Op2, chain: Chain) -> float:
+    """local_operations_module.f90 TwoSiteOp(link, Op2, Gammas, Lambdas, truncerr)."""
+    if chain.mode != MODE_DENSE:
+        raise TebdError(TEBD_ERR_STATE, "TwoSiteOp needs a dense chain")
+    return chain.two_site_op(link, Op2)
+
+
+def TwoSiteOpNC(link, Op2, chain: Chain) -> float:
+    """local_operations_module.f90 TwoSiteOpNC(link, Op2, Gammas, Lambdas, LabelLeft, LabelRight, truncerr)."""
+    if chain.mode != MODE_NC:
+        raise TebdError(TEBD_ERR_STATE, "TwoSiteOpNC needs a number-conserving chain")
+    return chain.two_site_op(link, Op2)
+
+
+def TrotterStep(Udt, chain: Chain, order=2) -> float:
+    """propagation_module.f90 TrotterStep / TrotterStepNC (BoundaryCond='O')."""
+    return chain.trotter_step(Udt, order)

@@ -1,0 +1,64 @@
+"""CPU tests of the boundary: the C-ABI library loads, exports every symbol
+include/tebd_capi.h declares, and rejects bad arguments without a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT, gpu_present
+
+
+def _header_symbols():
+    txt = open(os.path.join(ROOT, "include", "tebd_capi.h")).read()
+    return sorted(set(re.findall(r"\b(tebd_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    lib = pkg.load_library()
+    declared = _header_symbols()
+    assert declared, "no declarations parsed"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert sorted(pkg.EXPORTED_SYMBOLS) == declared
+
+
+def test_library_is_built_for_sm103a(pkg):
+    from opentebd_extended_gb300 import tebd as T
+
+    assert os.path.exists(T.LIB_PATH)
+    blob = open(T.LIB_PATH, "rb").read()
+    assert b"sm_103a" in blob or b"sm_103" in blob
+
+
+def test_invalid_arguments_rejected_before_cuda(pkg):
+    lib = pkg.load_library()
+    from opentebd_extended_gb300.tebd import Opts, TEBD_ERR_ARG
+
+    o = Opts()
+    lib.tebd_default_opts(ctypes.byref(o))
+    h = ctypes.c_void_p()
+    assert lib.tebd_create(1, 2, 4, 0, ctypes.byref(o), ctypes.byref(h)) == TEBD_ERR_ARG
+    assert lib.tebd_create(4, 0, 4, 0, ctypes.byref(o), ctypes.byref(h)) == TEBD_ERR_ARG
+    assert lib.tebd_create(4, 2, 4, 7, ctypes.byref(o), ctypes.byref(h)) == TEBD_ERR_ARG
+    o.version = 99
+    assert lib.tebd_create(4, 2, 4, 0, ctypes.byref(o), ctypes.byref(h)) == TEBD_ERR_ARG
+    assert b"version" in lib.tebd_last_error(None)
+    # null handles are rejected, never dereferenced
+    assert lib.tebd_destroy(None) == TEBD_ERR_ARG
+    assert lib.tebd_sync(None) == TEBD_ERR_ARG
+    assert lib.tebd_kernel_launches(None) == -1
+
+
+@pytest.mark.skipif(gpu_present(), reason="checks the no-GPU error path")
+def test_create_without_gpu_fails_cleanly(pkg):
+    with pytest.raises(pkg.TebdError) as e:
+        pkg.Chain(4, 2, 4)
+    assert e.value.code == 2  # TEBD_ERR_CUDA
+
+
+def test_fortran_binding_mentions_every_entry_point():
+    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    for name in ("tebd_two_site_op", "tebd_two_site_op_nc", "tebd_trotter_step", "tebd_create",
+                 "tebd_set_gamma", "tebd_get_lambda", "tebd_set_labels"):
+        assert name in txt, name
