@@ -132,6 +132,31 @@ const char *tebd_last_error(tebd_handle *h);
 /* Number of CUDA kernel launches issued by this handle since creation. */
 long long tebd_kernel_launches(tebd_handle *h);
 
+/* Diagnostics (no counterpart in the reference, which only prints CPU_TIME):
+ * work and device-time counters of the hot path, for roofline reporting. */
+typedef struct tebd_stats {
+  long long updates;           /* bond updates completed                                */
+  long long kernel_launches;   /* all kernels launched by this handle                   */
+  long long jacobi_launches;   /* Jacobi round kernels launched                         */
+  long long jacobi_sweeps;     /* sweeps summed over problems                           */
+  long long jacobi_pairs;      /* column pairs visited (each: one 3-term dot product)   */
+  long long jacobi_rotations;  /* column pairs rotated                                  */
+  double jacobi_flops;         /* algorithmic FP64 flops of the Jacobi rounds           */
+  double jacobi_bytes;         /* algorithmic bytes moved by the Jacobi rounds          */
+  double jacobi_ms;            /* device time of the Jacobi rounds (profiling on)       */
+  double batch_ms;             /* device time of whole bond batches (profiling on)      */
+  long long compact_rows;      /* sum over updates of the SVD's row count (d * kept chi) */
+  long long compact_cols;      /* sum over updates of the SVD's column count            */
+} tebd_stats;
+int tebd_set_profiling(tebd_handle *h, int on);
+int tebd_get_stats(tebd_handle *h, tebd_stats *stats);
+int tebd_reset_stats(tebd_handle *h);
+/* Measured FP64 FMA throughput of the device (TFLOP/s), by a short DFMA loop. */
+int tebd_measure_fp64_peak(int device, double *tflops);
+/* The handle's CUDA stream (a cudaStream_t), for callers that time or order
+ * their own work against the library's. */
+void *tebd_get_stream(tebd_handle *h);
+
 #ifdef __cplusplus
 }
 #endif

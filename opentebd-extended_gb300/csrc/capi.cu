@@ -83,6 +83,9 @@ static void free_all(tebd_handle *h) {
   cudaFree(h->js.done);
   cudaFree(h->js.sweeps);
   cudaFree(h->js.pending);
+  cudaFree(h->js.counters);
+  for (int e = 0; e < 4; ++e)
+    if (h->ev[e]) cudaEventDestroy(h->ev[e]);
   cudaFree(h->jprob_d);
   cudaFree(h->jprobf_d);
   cudaFree(h->status_d);
@@ -180,6 +183,8 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
   if ((rc = dalloc(h, (char **)&h->ws_base, h->ws_bytes, "alloc SVD workspaces"))) FAIL(rc);
   if ((rc = dalloc(h, &h->gates_d, sizeof(double2) * (size_t)ns * d * d * d * d, "alloc gates")))
     FAIL(rc);
+  if ((rc = dalloc(h, &h->cp_d, sizeof(Compact) * ns, "alloc compaction records"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->idx_d, sizeof(int) * (size_t)ns * 5 * chi, "alloc index maps"))) FAIL(rc);
   h->slots.resize(ns);
   {
     char *p = (char *)h->ws_base;
@@ -204,6 +209,13 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
         p += al(sizeof(double2) * nn);
       }
       S.gate = h->gates_d + (size_t)s * d * d * d * d;
+      int *ix = h->idx_d + (size_t)s * 5 * chi;
+      S.idx0 = ix;
+      S.idx1 = ix + chi;
+      S.idx2 = ix + 2 * chi;
+      S.inv0 = ix + 3 * chi;
+      S.inv2 = ix + 4 * chi;
+      S.cp = h->cp_d + s;
     }
   }
   if ((rc = dalloc(h, &h->slots_d, sizeof(Slot) * ns, "alloc slot table"))) FAIL(rc);
@@ -213,7 +225,7 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
     FAIL(rc);
   {
     std::vector<JacobiProblem<double>> jp(ns);
-    for (int s = 0; s < ns; ++s) jp[s] = {h->slots[s].X, h->slots[s].V, n, n, n, n};
+    for (int s = 0; s < ns; ++s) jp[s] = {h->slots[s].X, h->slots[s].V, n, n, n, n, 0.0};
     if ((rc = dalloc(h, (char **)&h->jprob_d, sizeof(JacobiProblem<double>) * ns, "alloc jprob")))
       FAIL(rc);
     if ((rc = check_cuda(h, cudaMemcpy(h->jprob_d, jp.data(), sizeof(JacobiProblem<double>) * ns,
@@ -222,7 +234,7 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
       FAIL(rc);
     if (mixed) {
       std::vector<JacobiProblem<float>> jf(ns);
-      for (int s = 0; s < ns; ++s) jf[s] = {h->slots[s].Xf, h->slots[s].Vf, n, n, n, n};
+      for (int s = 0; s < ns; ++s) jf[s] = {h->slots[s].Xf, h->slots[s].Vf, n, n, n, n, 0.0};
       if ((rc = dalloc(h, (char **)&h->jprobf_d, sizeof(JacobiProblem<float>) * ns, "alloc jprobf")))
         FAIL(rc);
       if ((rc = check_cuda(h, cudaMemcpy(h->jprobf_d, jf.data(), sizeof(JacobiProblem<float>) * ns,
@@ -240,6 +252,11 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
   if ((rc = dalloc(h, &h->js.done, sizeof(int) * h->js_cap, "alloc jacobi state"))) FAIL(rc);
   if ((rc = dalloc(h, &h->js.sweeps, sizeof(int) * h->js_cap, "alloc jacobi state"))) FAIL(rc);
   if ((rc = dalloc(h, &h->js.pending, sizeof(int) * 4, "alloc jacobi state"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->js.counters, sizeof(unsigned long long) * 4, "alloc counters"))) FAIL(rc);
+  if ((rc = check_cuda(h, cudaMemset(h->js.counters, 0, sizeof(unsigned long long) * 4), "memset")))
+    FAIL(rc);
+  for (int e = 0; e < 4; ++e)
+    if ((rc = check_cuda(h, cudaEventCreate(&h->ev[e]), "cudaEventCreate"))) FAIL(rc);
   if ((rc = dalloc(h, &h->status_d, sizeof(int) * 4, "alloc status"))) FAIL(rc);
   if ((rc = dalloc(h, &h->sig_link_d, sizeof(double) * (size_t)(L - 1) * n, "alloc spectra")))
     FAIL(rc);
@@ -402,11 +419,14 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
   CK(cudaMemcpyAsync(h->links_d, l_pin, sizeof(int) * nb, cudaMemcpyHostToDevice, h->stream),
      "upload links");
   CK(cudaMemsetAsync(h->status_d, 0, sizeof(int) * 4, h->stream), "reset status");
+  if (h->profiling) cudaEventRecord(h->ev[2], h->stream);
   int rc;
   if (h->mode == TEBD_MODE_DENSE) {
     if ((rc = launch_dense_prepare(h, nb, false))) return rc;
     if ((rc = launch_eye(h, nb))) return rc;
-    if ((rc = run_jacobi(h, nb, h->opts.svd_mode))) return rc;
+    int nmax = 0;
+    if ((rc = dense_compact_sizes(h, nb, &nmax))) return rc;
+    if ((rc = run_jacobi(h, nb, h->opts.svd_mode, nmax))) return rc;
     if ((rc = launch_dense_finish(h, nb))) return rc;
   } else {
     if ((rc = run_nc_batch(h, nb, links, nullptr))) return rc;
@@ -417,8 +437,15 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
      "read truncerr");
   CK(cudaMemcpyAsync(f_pin + 4, h->status_d, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->stream),
      "read status");
+  if (h->profiling) cudaEventRecord(h->ev[3], h->stream);
   CK(cudaStreamSynchronize(h->stream), "bond batch");
   for (int s = 0; s < nb; ++s) truncerr[s] = t_pin[s];
+  if (h->profiling) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]) == cudaSuccess) h->stats.batch_ms += ms;
+  }
+  h->stats.updates += nb;
+  if ((rc = jacobi_collect(h))) return rc;
   if (f_pin[4] & 1) return set_error(h, TEBD_ERR_NONFINITE, "non-finite value in Theta or sigma");
   if (f_pin[5]) return set_error(h, TEBD_ERR_NC_BLOCKS, "charge label outside the block range");
   return TEBD_OK;
@@ -515,3 +542,29 @@ extern "C" int tebd_trotter_step(tebd_handle *h, int order, int n_gates, const d
   *total_truncerr = total;
   return TEBD_OK;
 }
+
+extern "C" int tebd_set_profiling(tebd_handle *h, int on) {
+  if (!h) return TEBD_ERR_ARG;
+  h->profiling = on ? 1 : 0;
+  return TEBD_OK;
+}
+
+extern "C" int tebd_get_stats(tebd_handle *h, tebd_stats *st) {
+  if (!h || !st) return TEBD_ERR_ARG;
+  *st = h->stats;
+  st->kernel_launches = h->launches;
+  return TEBD_OK;
+}
+
+extern "C" int tebd_reset_stats(tebd_handle *h) {
+  if (!h) return TEBD_ERR_ARG;
+  memset(&h->stats, 0, sizeof(h->stats));
+  return TEBD_OK;
+}
+
+extern "C" int tebd_measure_fp64_peak(int device, double *tflops) {
+  if (!tflops) return TEBD_ERR_ARG;
+  return tebd::measure_fp64_peak(device, tflops);
+}
+
+extern "C" void *tebd_get_stream(tebd_handle *h) { return h ? (void *)h->stream : nullptr; }

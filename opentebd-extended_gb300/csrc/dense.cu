@@ -1,6 +1,6 @@
 // dense.cu -- HBM/L2 passes and the Theta contraction of the dense two-site update.
 //
-// Replaces, for a batch of same-parity bonds at once (one grid z/y index per bond):
+// Replaces, for a batch of same-parity bonds at once (one grid y/z index per bond):
 //   FormTheta      local_operations_module.f90:184-211   -> k_theta_form
 //   ThetaOperation local_operations_module.f90:213-280   -> k_gate_apply
 //   ReshapeTheta   local_operations_module.f90:283-320   -> k_theta_form's permuted store
@@ -9,10 +9,13 @@
 //   FormGamma1     local_operations_module.f90:381-404   -> k_restore_gamma1
 //   FormGamma2     local_operations_module.f90:406-428   -> k_restore_gamma2
 //
-// Theta is built directly in the reshaped (d chi) x (d chi) layout of ReshapeTheta:
-// row (i-1)chi+alpha, column (j-1)chi+beta (1-based), column-major, ld = n = d*chi.
+// Theta is built directly in ReshapeTheta's matrix layout (row (i-1)chi+alpha,
+// column (j-1)chi+beta), restricted to the kept indices of the Compact record:
+// row i*r0 + a', column j*r2 + b', column-major with ld = m = d*r0.  Rows and
+// columns of exact-zero Lambdas are identically zero in the reference's Theta,
+// so the singular values are the same; the dropped ones are exact zeros.
 // The 1/||Theta|| scaling of ReshapeTheta is not applied to the matrix: the SVD
-// factors do not depend on it, and the singular values are divided by the norm.
+// factors do not depend on it and the singular values are divided by the norm.
 #include <math.h>
 
 #include "tebd_internal.cuh"
@@ -20,10 +23,51 @@
 namespace tebd {
 
 // ---------------------------------------------------------------------------
-// Theta = diag(l0) G1 diag(l1) G2 diag(l2) as a complex FP64 GEMM.
-// A[r, g] = l0[r%chi] G1[r + n g]          (n x chi, the Gamma1 array as-is)
-// B[g, c] = l1[g] G2[g + chi c] l2[c/d]    (chi x n, the Gamma2 array as-is)
-// C[r, c] is stored at X[r + n*((c%d)*chi + c/d)] (ReshapeTheta's column order).
+// Compaction record and index maps (one CTA per slot, warp-ballot prefix scans).
+// Also fills the slot's FP64 Jacobi problem (m, n, ld).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(96) k_compact(const double *__restrict__ lam, const int *links,
+                                                Slot *slots, JacobiProblem<double> *jp, int chi,
+                                                int d) {
+  const int s = blockIdx.x;
+  const int link = links[s];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double *l = lam + (size_t)(link - 1 + w) * chi;  // w=0: Lambda0, 1: Lambda1, 2: Lambda2
+  int *idx = w == 0 ? slots[s].idx0 : (w == 1 ? slots[s].idx1 : slots[s].idx2);
+  int *inv = w == 0 ? slots[s].inv0 : (w == 2 ? slots[s].inv2 : nullptr);
+  int count = 0;
+  for (int base = 0; base < chi; base += 32) {
+    const int a = base + lane;
+    const bool keep = a < chi && l[a] != 0.0;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const int pos = count + __popc(m & ((1u << lane) - 1u));
+    if (keep) idx[pos] = a;
+    if (inv && a < chi) inv[a] = keep ? pos : -1;
+    count += __popc(m);
+  }
+  __shared__ int cnt[3];
+  if (lane == 0) cnt[w] = count;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Compact c;
+    c.r0 = cnt[0];
+    c.r1 = cnt[1];
+    c.r2 = cnt[2];
+    c.m = d * cnt[0];
+    c.n = d * cnt[2];
+    *slots[s].cp = c;
+    jp[s].m = c.m;
+    jp[s].n = c.n;
+    jp[s].ldx = c.m > 0 ? c.m : 1;
+    jp[s].ldv = c.n > 0 ? c.n : 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Theta = diag(l0) G1 diag(l1) G2 diag(l2) on the kept indices, complex FP64 GEMM.
+// A[r', g'] = l0[a] G1[a + chi*i + chi*d*g]   r' = i*r0 + a', a = idx0[a'], g = idx1[g']
+// B[g', c'] = l1[g] G2[g + chi*l + chi*d*b] l2[b]   c' = l + d*b', b = idx2[b']
+// C[r', c'] is stored at X[r' + m*(l*r2 + b')].
 // Tile 64x64 outputs, k-step 8, 256 threads, 4x4 complex outputs per thread.
 // ---------------------------------------------------------------------------
 constexpr int TT_M = 64, TT_N = 64, TT_K = 8;
@@ -32,43 +76,50 @@ __global__ void __launch_bounds__(256) k_theta_form(const double2 *__restrict__ 
                                                     const double *__restrict__ lam,
                                                     const int *__restrict__ links, Slot *slots,
                                                     int chi, int d) {
-  const int n = chi * d;
   const int s = blockIdx.z;
-  const int link = links[s];  // 1-based
+  const Compact cp = *slots[s].cp;
+  const int r0b = blockIdx.x * TT_M, c0b = blockIdx.y * TT_N;
+  if (r0b >= cp.m || c0b >= cp.n) return;  // uniform per CTA
+  const int link = links[s];
   const size_t csz = (size_t)chi * d * chi;
   const double2 *G1 = gam + (size_t)(link - 1) * csz;
   const double2 *G2 = gam + (size_t)link * csz;
   const double *l0 = lam + (size_t)(link - 1) * chi;
   const double *l1 = lam + (size_t)link * chi;
   const double *l2 = lam + (size_t)(link + 1) * chi;
+  const int *idx0 = slots[s].idx0, *idx1 = slots[s].idx1, *idx2 = slots[s].idx2;
   double2 *X = slots[s].X;
+  const int m = cp.m, n = cp.n, r0 = cp.r0, r1 = cp.r1, r2 = cp.r2;
 
   __shared__ double2 As[TT_K][TT_M + 1];
   __shared__ double2 Bs[TT_K][TT_N + 1];
   const int tid = threadIdx.x;
-  const int tr = tid % 16, tc = tid / 16;  // 16 x 16 thread grid, 4x4 outputs each
-  const int r0 = blockIdx.x * TT_M, c0 = blockIdx.y * TT_N;
+  const int tr = tid % 16, tc = tid / 16;
   double2 acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b) acc[a][b] = make_double2(0.0, 0.0);
 
-  for (int k0 = 0; k0 < chi; k0 += TT_K) {
-    // A tile: 64 rows x 8 k  (512 elements, 2 per thread), coalesced along rows
+  for (int k0 = 0; k0 < r1; k0 += TT_K) {
     for (int e = tid; e < TT_M * TT_K; e += 256) {
       const int rr = e % TT_M, kk = e / TT_M;
-      const int r = r0 + rr, g = k0 + kk;
+      const int r = r0b + rr, gk = k0 + kk;
       double2 v = make_double2(0.0, 0.0);
-      if (r < n && g < chi) v = cscale(G1[r + (size_t)n * g], l0[r % chi]);
+      if (r < m && gk < r1) {
+        const int i = r / r0, a = idx0[r - i * r0], g = idx1[gk];
+        v = cscale(G1[a + (size_t)chi * i + csz / chi * g], l0[a]);
+      }
       As[kk][rr] = v;
     }
-    // B tile: 8 k x 64 cols, coalesced along k (the Gamma2 leading dimension)
     for (int e = tid; e < TT_K * TT_N; e += 256) {
       const int kk = e % TT_K, cc = e / TT_K;
-      const int g = k0 + kk, c = c0 + cc;
+      const int gk = k0 + kk, c = c0b + cc;
       double2 v = make_double2(0.0, 0.0);
-      if (g < chi && c < n) v = cscale(G2[g + (size_t)chi * c], l1[g] * l2[c / d]);
+      if (gk < r1 && c < n) {
+        const int lphys = c % d, b = idx2[c / d], g = idx1[gk];
+        v = cscale(G2[g + (size_t)chi * lphys + (size_t)chi * d * b], l1[g] * l2[b]);
+      }
       Bs[kk][cc] = v;
     }
     __syncthreads();
@@ -94,20 +145,20 @@ __global__ void __launch_bounds__(256) k_theta_form(const double2 *__restrict__ 
   }
 #pragma unroll
   for (int p = 0; p < 4; ++p) {
-    const int r = r0 + tr + 16 * p;
-    if (r >= n) continue;
+    const int r = r0b + tr + 16 * p;
+    if (r >= m) continue;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const int c = c0 + tc + 16 * q;
+      const int c = c0b + tc + 16 * q;
       if (c >= n) continue;
-      const int lphys = c % d, beta = c / d;
-      X[r + (size_t)n * ((size_t)lphys * chi + beta)] = acc[p][q];
+      const int lphys = c % d, bp = c / d;
+      X[r + (size_t)m * ((size_t)lphys * r2 + bp)] = acc[p][q];
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// ThetaOperation: for every (alpha, beta) the d^2-vector Theta(alpha,:,:,beta)
+// ThetaOperation: for every kept (alpha, beta) the d^2-vector Theta(alpha,:,:,beta)
 // is multiplied by Op2 (row (i-1)d+j, column (k-1)d+l).  In place.
 // ---------------------------------------------------------------------------
 constexpr int kMaxD = 8;
@@ -115,18 +166,19 @@ constexpr int kMaxD = 8;
 __global__ void __launch_bounds__(128) k_gate_apply(Slot *slots, int chi, int d) {
   extern __shared__ double2 gsm[];  // d^4
   const int s = blockIdx.y;
-  const int n = chi * d, d2 = d * d;
+  const Compact cp = *slots[s].cp;
+  const int d2 = d * d;
   const double2 *G = slots[s].gate;
   for (int e = threadIdx.x; e < d2 * d2; e += blockDim.x) gsm[e] = G[e];
   __syncthreads();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= chi * chi) return;
-  const int alpha = t % chi, beta = t / chi;
+  if (t >= cp.r0 * cp.r2) return;
+  const int a = t % cp.r0, b = t / cp.r0;
+  const int m = cp.m, r0 = cp.r0, r2 = cp.r2;
   double2 *X = slots[s].X;
   double2 v[kMaxD * kMaxD];
   for (int k = 0; k < d; ++k)
-    for (int l = 0; l < d; ++l)
-      v[k * d + l] = X[(size_t)(k * chi + alpha) + (size_t)n * (l * chi + beta)];
+    for (int l = 0; l < d; ++l) v[k * d + l] = X[(size_t)(k * r0 + a) + (size_t)m * (l * r2 + b)];
   for (int i = 0; i < d; ++i)
     for (int j = 0; j < d; ++j) {
       const int row = i * d + j;
@@ -138,16 +190,17 @@ __global__ void __launch_bounds__(128) k_gate_apply(Slot *slots, int chi, int d)
         acc.y = fma(g.x, v[kl].y, acc.y);
         acc.y = fma(g.y, v[kl].x, acc.y);
       }
-      X[(size_t)(i * chi + alpha) + (size_t)n * (j * chi + beta)] = acc;
+      X[(size_t)(i * r0 + a) + (size_t)m * (j * r2 + b)] = acc;
     }
 }
 
 // ---------------------------------------------------------------------------
 // Frobenius norm of Theta, deterministic two-level reduction (fixed order).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_norm_partial(Slot *slots, int n, double *part) {
+__global__ void __launch_bounds__(256) k_norm_partial(Slot *slots, double *part) {
   const int s = blockIdx.y;
-  const size_t total = (size_t)n * n;
+  const Compact cp = *slots[s].cp;
+  const size_t total = (size_t)cp.m * cp.n;
   const size_t chunk = (total + kNormParts - 1) / kNormParts;
   const size_t beg = blockIdx.x * chunk;
   const size_t end = beg + chunk < total ? beg + chunk : total;
@@ -167,19 +220,23 @@ __global__ void __launch_bounds__(256) k_norm_partial(Slot *slots, int n, double
   if (threadIdx.x == 0) part[s * kNormParts + blockIdx.x] = red[0];
 }
 
-__global__ void k_norm_final(const double *part, double *nrm, int nb, int *status) {
+__global__ void k_norm_final(const double *part, double *nrm, JacobiProblem<double> *jp, int nb,
+                             int *status) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nb) return;
   double acc = 0.0;
   for (int j = 0; j < kNormParts; ++j) acc += part[s * kNormParts + j];
   const double v = sqrt(acc);
   nrm[s] = v;
-  if (!isfinite(v)) atomicOr(&status[0], 1);
+  const double f = kNegligibleColumn * v;
+  jp[s].floor = f * f;
+  if (!isfinite(v) || v == 0.0) atomicOr(&status[0], 1);
 }
 
-// V = identity (n x n) for every slot
-__global__ void k_eye(Slot *slots, int n) {
+// V = identity (n x n, ld n) for every slot
+__global__ void k_eye(Slot *slots) {
   const int s = blockIdx.y;
+  const int n = slots[s].cp->n;
   double2 *V = slots[s].V;
   const size_t total = (size_t)n * n;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
@@ -190,20 +247,22 @@ __global__ void k_eye(Slot *slots, int n) {
 }
 
 // ---------------------------------------------------------------------------
-// After the SVD: column norms of X = U Sigma, descending order (rank sort,
-// ties broken by column index), normalised singular values S = sigma/||Theta||.
-// One CTA per slot, one warp per column for the norms.
+// After the SVD: column norms of X = U Sigma, descending order (rank sort, ties
+// broken by column index), normalised singular values S = sigma/||Theta||; the
+// n_full - n dropped values are exact zeros.  One CTA per slot.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) k_sigma_sort(Slot *slots, const double *nrm, int n,
+__global__ void __launch_bounds__(1024) k_sigma_sort(Slot *slots, const double *nrm, int n_full,
                                                      int *status) {
   extern __shared__ double sig[];  // n
   const int s = blockIdx.x;
+  const Compact cp = *slots[s].cp;
+  const int m = cp.m, n = cp.n;
   const double2 *X = slots[s].X;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int c = warp; c < n; c += nw) {
     double acc = 0.0;
-    for (int r = lane; r < n; r += 32) {
-      const double2 v = X[r + (size_t)n * c];
+    for (int r = lane; r < m; r += 32) {
+      const double2 v = X[r + (size_t)m * c];
       acc = fma(v.x, v.x, fma(v.y, v.y, acc));
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -215,12 +274,16 @@ __global__ void __launch_bounds__(1024) k_sigma_sort(Slot *slots, const double *
     const double v = sig[k];
     if (!isfinite(v)) atomicOr(&status[0], 1);
     int rank = 0;
-    for (int m = 0; m < n; ++m) {
-      const double w = sig[m];
-      rank += (w > v) || (w == v && m < k);
+    for (int q = 0; q < n; ++q) {
+      const double w = sig[q];
+      rank += (w > v) || (w == v && q < k);
     }
     slots[s].perm[rank] = k;
     slots[s].S[rank] = v * inv;
+  }
+  for (int k = n + threadIdx.x; k < n_full; k += blockDim.x) {
+    slots[s].perm[k] = -1;
+    slots[s].S[k] = 0.0;
   }
 }
 
@@ -253,45 +316,54 @@ __global__ void k_store_spectrum(Slot *slots, const int *links, const int *sweep
 }
 
 // FormGamma1 (:381-404): Gamma1(alpha,i,beta) = U((i-1)chi+alpha, beta) / Lambda0(alpha)
-// with U(:,beta) = X(:,perm(beta)) / sigma(perm(beta)).  Same linear index on both sides.
+// with U(:,beta) = X(:,perm(beta)) / sigma(perm(beta)); zero where the guard fails,
+// where alpha was compacted away, and for columns beyond the rank.
 __global__ void k_restore_gamma1(double2 *gam, const double *lam, const int *links, Slot *slots,
                                  const double *nrm, int chi, int d) {
   const int s = blockIdx.y;
-  const int n = chi * d;
+  const int nf = chi * d;
   const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= (size_t)n * chi) return;
+  if (t >= (size_t)nf * chi) return;
+  const Compact cp = *slots[s].cp;
   const int link = links[s];
-  const int r = (int)(t % n), beta = (int)(t / n);
-  const int alpha = r % chi;
+  const int r = (int)(t % nf), beta = (int)(t / nf);
+  const int i = r / chi, alpha = r % chi;
   const double *l0 = lam + (size_t)(link - 1) * chi;
-  const int col = slots[s].perm[beta];
-  const double sigma = slots[s].S[beta] * nrm[s];
   double2 out = make_double2(0.0, 0.0);
-  if (fabs(l0[alpha]) > kGuardDense && sigma > 0.0) {
-    const double2 x = slots[s].X[r + (size_t)n * col];
-    const double sc = 1.0 / (sigma * l0[alpha]);
-    out = make_double2(x.x * sc, x.y * sc);
+  const int ap = slots[s].inv0[alpha];
+  if (beta < cp.n && ap >= 0 && fabs(l0[alpha]) > kGuardDense) {
+    const double sigma = slots[s].S[beta] * nrm[s];
+    if (sigma > 0.0) {
+      const int col = slots[s].perm[beta];
+      const double2 x = slots[s].X[(size_t)(i * cp.r0 + ap) + (size_t)cp.m * col];
+      const double sc = 1.0 / (sigma * l0[alpha]);
+      out = make_double2(x.x * sc, x.y * sc);
+    }
   }
   gam[(size_t)(link - 1) * chi * d * chi + t] = out;
 }
 
 // FormGamma2 (:406-428): Gamma2(alpha,i,beta) = VT(alpha,(i-1)chi+beta) / Lambda2(beta),
-// VT = V^H, i.e. conj(V((i-1)chi+beta, perm(alpha))).  32x32 tile transpose through smem.
+// VT = V^H, i.e. conj(V(i*r2 + b', perm(alpha))).  32x32 tile transpose through smem.
 __global__ void __launch_bounds__(256) k_restore_gamma2(double2 *gam, const double *lam,
                                                         const int *links, Slot *slots, int chi,
                                                         int d) {
   __shared__ double2 tile[32][33];
   const int s = blockIdx.z;
-  const int n = chi * d;
+  const int nf = chi * d;
+  const Compact cp = *slots[s].cp;
   const int link = links[s];
   const int a0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
   const double2 *V = slots[s].V;
-  const int *perm = slots[s].perm;
+  const int *perm = slots[s].perm, *inv2 = slots[s].inv2;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   for (int yy = ty; yy < 32; yy += 8) {
     const int alpha = a0 + yy, c = c0 + tx;
     double2 v = make_double2(0.0, 0.0);
-    if (alpha < chi && c < n) v = V[c + (size_t)n * perm[alpha]];
+    if (alpha < chi && alpha < cp.n && c < nf) {
+      const int bp = inv2[c % chi];
+      if (bp >= 0) v = V[(size_t)((c / chi) * cp.r2 + bp) + (size_t)cp.n * perm[alpha]];
+    }
     tile[yy][tx] = v;
   }
   __syncthreads();
@@ -299,7 +371,7 @@ __global__ void __launch_bounds__(256) k_restore_gamma2(double2 *gam, const doub
   double2 *G2 = gam + (size_t)link * chi * d * chi;
   for (int yy = ty; yy < 32; yy += 8) {
     const int c = c0 + yy, alpha = a0 + tx;
-    if (alpha >= chi || c >= n) continue;
+    if (alpha >= chi || c >= nf) continue;
     const int i = c / chi, beta = c % chi;
     const double2 v = tile[tx][yy];
     double2 out = make_double2(0.0, 0.0);
@@ -307,7 +379,7 @@ __global__ void __launch_bounds__(256) k_restore_gamma2(double2 *gam, const doub
       const double inv = 1.0 / l2[beta];
       out = make_double2(v.x * inv, -v.y * inv);
     }
-    G2[alpha + (size_t)chi * i + (size_t)n * beta] = out;
+    G2[alpha + (size_t)chi * i + (size_t)nf * beta] = out;
   }
 }
 
@@ -319,15 +391,18 @@ static inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) 
 int launch_dense_prepare(tebd_handle *h, int nb, bool /*real_gate: converted on the host*/) {
   const int chi = h->chi, d = h->d, n = h->n;
   cudaStream_t st = h->stream;
+  JacobiProblem<double> *jp = reinterpret_cast<JacobiProblem<double> *>(h->jprob_d);
+  k_compact<<<nb, 96, 0, st>>>(h->lam, h->links_d, h->slots_d, jp, chi, d);
+  TEBD_LAUNCHED(h);
   k_theta_form<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
                                                                        h->slots_d, chi, d);
   TEBD_LAUNCHED(h);
   const size_t gsm = sizeof(double2) * (size_t)d * d * d * d;
   k_gate_apply<<<dim3(cdiv((size_t)chi * chi, 128), nb), 128, gsm, st>>>(h->slots_d, chi, d);
   TEBD_LAUNCHED(h);
-  k_norm_partial<<<dim3(kNormParts, nb), 256, 0, st>>>(h->slots_d, n, h->nrm_part);
+  k_norm_partial<<<dim3(kNormParts, nb), 256, 0, st>>>(h->slots_d, h->nrm_part);
   TEBD_LAUNCHED(h);
-  k_norm_final<<<cdiv(nb, 128), 128, 0, st>>>(h->nrm_part, h->nrm, nb, h->status_d);
+  k_norm_final<<<cdiv(nb, 128), 128, 0, st>>>(h->nrm_part, h->nrm, jp, nb, h->status_d);
   TEBD_LAUNCHED(h);
   return check_cuda(h, cudaGetLastError(), "dense prepare launch");
 }
@@ -336,7 +411,7 @@ int launch_eye(tebd_handle *h, int nb) {
   const size_t total = (size_t)h->n * h->n;
   unsigned gx = cdiv(total, 256);
   if (gx > 1024) gx = 1024;
-  k_eye<<<dim3(gx, nb), 256, 0, h->stream>>>(h->slots_d, h->n);
+  k_eye<<<dim3(gx, nb), 256, 0, h->stream>>>(h->slots_d);
   TEBD_LAUNCHED(h);
   return check_cuda(h, cudaGetLastError(), "eye launch");
 }
@@ -358,6 +433,29 @@ int launch_dense_finish(tebd_handle *h, int nb) {
                                                                         h->slots_d, chi, d);
   TEBD_LAUNCHED(h);
   return check_cuda(h, cudaGetLastError(), "dense finish launch");
+}
+
+}  // namespace tebd
+
+namespace tebd {
+
+// Largest compacted column count of the batch (sizes the Jacobi rounds).
+int dense_compact_sizes(tebd_handle *h, int nb, int *nmax) {
+  std::vector<Compact> cp(nb);
+  int rc = check_cuda(h, cudaMemcpyAsync(cp.data(), h->cp_d, sizeof(Compact) * nb,
+                                         cudaMemcpyDeviceToHost, h->stream),
+                      "read compaction");
+  if (rc) return rc;
+  rc = check_cuda(h, cudaStreamSynchronize(h->stream), "read compaction");
+  if (rc) return rc;
+  int mx = 0;
+  for (int s = 0; s < nb; ++s) {
+    if (cp[s].n > mx) mx = cp[s].n;
+    h->stats.compact_rows += cp[s].m;
+    h->stats.compact_cols += cp[s].n;
+  }
+  *nmax = mx;
+  return TEBD_OK;
 }
 
 }  // namespace tebd

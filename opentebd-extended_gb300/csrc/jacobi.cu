@@ -54,7 +54,7 @@ __device__ __forceinline__ bool jacobi_pair(typename cplx<T>::type *__restrict__
                                             typename cplx<T>::type *__restrict__ B,
                                             typename cplx<T>::type *__restrict__ VA,
                                             typename cplx<T>::type *__restrict__ VB, int m,
-                                            int nv, int lane, T tol) {
+                                            int nv, int lane, T tol, double floor) {
   using C2 = typename cplx<T>::type;
   T al = 0, be = 0, gr = 0, gi = 0;
   for (int r = lane; r < m; r += 32) {
@@ -69,7 +69,7 @@ __device__ __forceinline__ bool jacobi_pair(typename cplx<T>::type *__restrict__
   gr = warp_sum(gr);
   gi = warp_sum(gi);
   const T g = sqrt(gr * gr + gi * gi);
-  if (!(g > tol * sqrt(al) * sqrt(be))) return false;
+  if (!(g > tol * sqrt(al) * sqrt(be)) || (double)al <= floor || (double)be <= floor) return false;
   const T zeta = (be - al) / (T(2) * g);
   T t;
   if (fabs(zeta) > JacobiBig<T>::v())
@@ -109,32 +109,35 @@ __global__ void __launch_bounds__(kJacobiWarps * 32)
     k_jacobi_round(const JacobiProblem<T> *__restrict__ probs, const int *__restrict__ done,
                    int *__restrict__ rot, int round, T tol) {
   const int p = blockIdx.y;
-  if (done[p]) return;
+  if (done[p]) return;  // uniform per CTA
   const JacobiProblem<T> P = probs[p];
   const int npad = P.n + (P.n & 1);
   const int R = npad - 1;
-  if (round >= R) return;
+  if (round >= R) return;  // uniform per CTA
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * kJacobiWarps + warp;
-  if (k >= npad / 2) return;
-  int i, j;
-  if (k == 0) {
-    i = R;
-    j = round;
-  } else {
-    i = (round + k) % R;
-    j = (round - k + R) % R;
+  int i = -1, j = -1;
+  if (k < npad / 2) {
+    if (k == 0) {
+      i = R;
+      j = round;
+    } else {
+      i = (round + k) % R;
+      j = (round - k + R) % R;
+    }
+    if (i > j) {
+      const int t = i;
+      i = j;
+      j = t;
+    }
   }
-  if (i >= P.n || j >= P.n) return;  // the phantom column of an odd n
-  if (i > j) {
-    const int t = i;
-    i = j;
-    j = t;
-  }
-  const bool r = jacobi_pair<T>(P.X + (size_t)P.ldx * i, P.X + (size_t)P.ldx * j,
-                                P.V + (size_t)P.ldv * i, P.V + (size_t)P.ldv * j, P.m, P.n, lane,
-                                tol);
-  if (r && lane == 0) rot[p] = 1;
+  bool rotated = false;
+  if (i >= 0 && j < P.n)  // j == P.n is the phantom column of an odd n
+    rotated = jacobi_pair<T>(P.X + (size_t)P.ldx * i, P.X + (size_t)P.ldx * j,
+                             P.V + (size_t)P.ldv * i, P.V + (size_t)P.ldv * j, P.m, P.n, lane, tol,
+                             P.floor);
+  const int c = __syncthreads_count(rotated && lane == 0);
+  if (threadIdx.x == 0 && c) atomicAdd(&rot[p], c);
 }
 
 __global__ void k_jacobi_init(int nprob, int *rot, int *done, int *sweeps) {
@@ -145,17 +148,33 @@ __global__ void k_jacobi_init(int nprob, int *rot, int *done, int *sweeps) {
   }
 }
 
-__global__ void k_jacobi_sweep_end(int nprob, int *rot, int *done, int *sweeps, int *pending) {
+// End of a sweep: converge problems without rotations, accumulate the work
+// counters (pairs visited, rows streamed) used for roofline reporting.
+template <typename T>
+__global__ void k_jacobi_sweep_end(const JacobiProblem<T> *__restrict__ probs, int nprob, int *rot,
+                                   int *done, int *sweeps, int *pending,
+                                   unsigned long long *counters) {
   if (threadIdx.x != 0) return;
   int cnt = 0;
+  unsigned long long nrot = 0, npairs = 0, rows = 0, rrows = 0;
   for (int p = 0; p < nprob; ++p) {
     if (!done[p]) {
+      const unsigned long long n = (unsigned long long)probs[p].n;
+      const unsigned long long pairs = n * (n - 1) / 2;
       sweeps[p] += 1;
+      npairs += pairs;
+      rows += pairs * (unsigned long long)probs[p].m;
+      nrot += (unsigned long long)rot[p];
+      rrows += (unsigned long long)rot[p] * (unsigned long long)(probs[p].m + probs[p].n);
       if (rot[p] == 0) done[p] = 1;
       rot[p] = 0;
     }
     cnt += !done[p];
   }
+  counters[0] += nrot;
+  counters[1] += npairs;
+  counters[2] += rows;
+  counters[3] += rrows;
   pending[0] = cnt;
 }
 
@@ -168,13 +187,16 @@ static int jacobi_sweeps(tebd_handle *h, const JacobiProblem<T> *probs_d, int np
   const unsigned gx = (unsigned)((npad / 2 + kJacobiWarps - 1) / kJacobiWarps);
   int *pending_h = reinterpret_cast<int *>(h->pinned);
   for (int sw = 0; sw < max_sweeps; ++sw) {
+    if (h->profiling) cudaEventRecord(h->ev[0], st);
     for (int r = 0; r < rounds; ++r) {
       k_jacobi_round<T><<<dim3(gx, nprob), kJacobiWarps * 32, 0, st>>>(probs_d, h->js.done,
                                                                        h->js.rot, r, tol);
       TEBD_LAUNCHED(h);
     }
-    k_jacobi_sweep_end<<<1, 32, 0, st>>>(nprob, h->js.rot, h->js.done, h->js.sweeps,
-                                          h->js.pending);
+    h->stats.jacobi_launches += rounds;
+    if (h->profiling) cudaEventRecord(h->ev[1], st);
+    k_jacobi_sweep_end<T><<<1, 32, 0, st>>>(probs_d, nprob, h->js.rot, h->js.done, h->js.sweeps,
+                                             h->js.pending, h->js.counters);
     TEBD_LAUNCHED(h);
     int rc = check_cuda(h, cudaMemcpyAsync(pending_h, h->js.pending, sizeof(int),
                                            cudaMemcpyDeviceToHost, st),
@@ -182,17 +204,24 @@ static int jacobi_sweeps(tebd_handle *h, const JacobiProblem<T> *probs_d, int np
     if (rc) return rc;
     rc = check_cuda(h, cudaStreamSynchronize(st), "jacobi sweep");
     if (rc) return rc;
+    if (h->profiling) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]) == cudaSuccess) h->stats.jacobi_ms += ms;
+    }
     *sweeps_used = sw + 1;
     if (*pending_h == 0) return TEBD_OK;
   }
   return set_error(h, TEBD_ERR_SVD_NOCONV, "Jacobi SVD did not converge within the sweep cap");
 }
 
-int run_jacobi(tebd_handle *h, int nb, int /*svd_mode*/) {
-  const int n = h->n;
+// Dense batch: nmax = largest compacted column count of the batch (the rounds
+// of smaller problems past their own n-1 return at once).
+int run_jacobi(tebd_handle *h, int nb, int /*svd_mode*/, int nmax) {
+  const int n = nmax;
   k_jacobi_init<<<1, 64, 0, h->stream>>>(nb, h->js.rot, h->js.done, h->js.sweeps);
   TEBD_LAUNCHED(h);
-  const double tol = h->opts.jacobi_tol > 0 ? h->opts.jacobi_tol : (double)n * 2.220446049250313e-16;
+  const double tol =
+      h->opts.jacobi_tol > 0 ? h->opts.jacobi_tol : (double)(n > 16 ? n : 16) * 2.220446049250313e-16;
   const int cap = h->opts.max_sweeps > 0 ? h->opts.max_sweeps : 60;
   int used = 0;
   return jacobi_sweeps<double>(h, reinterpret_cast<const JacobiProblem<double> *>(h->jprob_d), nb, n,
@@ -208,6 +237,73 @@ int run_jacobi_problems(tebd_handle *h, const JacobiProblem<double> *probs_d, in
   const int cap = h->opts.max_sweeps > 0 ? h->opts.max_sweeps : 60;
   int used = 0;
   return jacobi_sweeps<double>(h, probs_d, nprob, nmax, tol, cap, &used);
+}
+
+// Read the device work counters into the handle's stats (called after a batch).
+int jacobi_collect(tebd_handle *h) {
+  unsigned long long c[4];
+  int rc = check_cuda(h, cudaMemcpyAsync(c, h->js.counters, sizeof(c), cudaMemcpyDeviceToHost,
+                                         h->stream), "read jacobi counters");
+  if (rc) return rc;
+  rc = check_cuda(h, cudaMemsetAsync(h->js.counters, 0, sizeof(c), h->stream), "reset counters");
+  if (rc) return rc;
+  rc = check_cuda(h, cudaStreamSynchronize(h->stream), "read jacobi counters");
+  if (rc) return rc;
+  h->stats.jacobi_rotations += (long long)c[0];
+  h->stats.jacobi_pairs += (long long)c[1];
+  // FP64 flops: 16 per row for the three dot products of every visited pair,
+  // 20 per row of X and of V for every rotated pair (2 columns x 2 components x 5).
+  h->stats.jacobi_flops += 16.0 * (double)c[2] + 20.0 * (double)c[3];
+  // bytes: dot pass reads 2 columns; a rotation re-reads and writes the 2 columns
+  // of X and of V (16 B per complex element).
+  h->stats.jacobi_bytes += 32.0 * (double)c[2] + 64.0 * (double)c[3];
+  return TEBD_OK;
+}
+
+// FP64 FMA throughput probe: independent fma chains, no memory traffic.
+__global__ void k_fp64_peak(double *out, double a, double b, int iters) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
+         x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b);
+    x1 = fma(x1, a, b);
+    x2 = fma(x2, a, b);
+    x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b);
+    x5 = fma(x5, a, b);
+    x6 = fma(x6, a, b);
+    x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+int measure_fp64_peak(int device, double *tflops) {
+  if (cudaSetDevice(device) != cudaSuccess) return TEBD_ERR_CUDA;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return TEBD_ERR_CUDA;
+  const int blocks = prop.multiProcessorCount * 8, threads = 256, iters = 4096;
+  double *buf = nullptr;
+  if (cudaMalloc(&buf, sizeof(double) * blocks * threads) != cudaSuccess) return TEBD_ERR_OOM;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(a);
+    k_fp64_peak<<<blocks, threads>>>(buf, 0.999, 1e-3, iters);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best) best = ms;
+  }
+  const cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(buf);
+  if (e != cudaSuccess) return TEBD_ERR_CUDA;
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return TEBD_OK;
 }
 
 }  // namespace tebd

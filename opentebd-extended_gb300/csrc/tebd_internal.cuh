@@ -59,25 +59,49 @@ struct JacobiProblem {
   typename cplx<T>::type *X;
   typename cplx<T>::type *V;
   int m, n, ldx, ldv;
+  double floor;  // columns with squared norm <= floor are treated as zero (not rotated)
 };
 
+// Relative size below which a column of Theta is numerically zero for the SVD:
+// |x| <= 2^-60 ||Theta||_F (~8.7e-19, three decades under the reference's 1e-15
+// Lambda guard).  Such columns are not rotated; this only removes sweeps spent
+// reorthogonalising rounding noise.
+constexpr double kNegligibleColumn = 8.673617379884035e-19;
+
 struct JacobiState {
-  int *rot;      // rotations applied in the current sweep, per problem
-  int *done;     // 1 once a sweep applied no rotation
-  int *sweeps;   // sweeps executed, per problem
-  int *pending;  // [0] number of problems not yet converged (host reads it)
+  int *rot;                       // rotations applied in the current sweep, per problem
+  int *done;                      // 1 once a sweep applied no rotation
+  int *sweeps;                    // sweeps executed, per problem
+  int *pending;                   // [0] problems not yet converged (host reads it)
+  unsigned long long *counters;   // [0] rotations, [1] pairs visited, [2] pair-rows, [3] rotated
+                                  // pair-rows (rows of X plus rows of V), summed over problems
 };
 
 // ---------------------------------------------------------------------------
 // per-handle state
 // ---------------------------------------------------------------------------
+// Exact compaction of Theta.  Rows (i,alpha) with Lambda0(alpha) == 0 and columns
+// (j,beta) with Lambda2(beta) == 0 are identically zero, and Lambda1(gamma) == 0
+// removes gamma from the contraction; FormLambda1 leaves exact zeros below its
+// guard, so most of a fixed-chi allocation is zero until the chain saturates.
+// Theta is formed and decomposed as the (d r0) x (d r2) matrix of the kept
+// indices: row i*r0 + a', column j*r2 + b'.  Its singular values are those of the
+// full matrix; the dropped ones are exact zeros.
+struct Compact {
+  int r0, r1, r2;  // kept counts of Lambda0, Lambda1, Lambda2
+  int m, n;        // d*r0 rows, d*r2 columns
+};
+
 struct Slot {
-  double2 *X, *V;    // n x n FP64 Theta / right factor
+  double2 *X, *V;    // FP64 Theta (m x n, ld m) / right factor (n x n, ld n)
   float2 *Xf, *Vf;   // FP32 shadows (mixed SVD)
-  double2 *theta0;   // n x n copy of the gated, unnormalised Theta (mixed SVD)
+  double2 *theta0;   // copy of the gated, unnormalised Theta (mixed SVD)
   double *S;         // n sorted singular values of the normalised Theta
   int *perm;         // n column permutation (descending sigma)
   double2 *gate;     // d^2 x d^2 gate for this slot
+  int *idx0, *idx1, *idx2;  // kept alpha / gamma / beta (chi each)
+  int *inv0, *inv2;         // alpha -> a' and beta -> b' (-1 if dropped)
+  Compact *cp;              // device compaction record
 };
 
 }  // namespace tebd
@@ -98,6 +122,8 @@ struct tebd_handle {
   void *ws_base;                  // single allocation carved into slots
   size_t ws_bytes;
   double2 *gates_d;               // nslots * d^4 gates of the current batch
+  tebd::Compact *cp_d;            // nslots compaction records
+  int *idx_d;                     // nslots * 5 * chi index maps
   double *nrm_part;       // nslots * kNormParts partial sums of |Theta|^2
   double *nrm;            // nslots Frobenius norms
   double *truncerr_d;     // nslots
@@ -118,6 +144,10 @@ struct tebd_handle {
   size_t pinned_bytes;
   std::string err;
   long long launches;
+  // diagnostics
+  tebd_stats stats;
+  int profiling;
+  cudaEvent_t ev[4];
 };
 
 namespace tebd {
@@ -127,9 +157,13 @@ int check_cuda(tebd_handle *h, cudaError_t e, const char *what);
 
 // kernels launched from capi.cu (defined in the .cu files)
 int launch_dense_prepare(tebd_handle *h, int nb, bool real_gate);
-int run_jacobi(tebd_handle *h, int nb, int svd_mode);
+int run_jacobi(tebd_handle *h, int nb, int svd_mode, int nmax);
+int dense_compact_sizes(tebd_handle *h, int nb, int *nmax);
 int launch_dense_finish(tebd_handle *h, int nb);
 int launch_eye(tebd_handle *h, int nb);
+int run_jacobi_problems(tebd_handle *h, const JacobiProblem<double> *probs_d, int nprob, int nmax);
+int jacobi_collect(tebd_handle *h);
+int measure_fp64_peak(int device, double *tflops);
 int run_nc_batch(tebd_handle *h, int nb, const int *links_host, double *truncerr_host);
 int nc_alloc(tebd_handle *h);
 void nc_free(tebd_handle *h);

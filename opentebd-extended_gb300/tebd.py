@@ -59,7 +59,8 @@ EXPORTED_SYMBOLS = (
     "tebd_set_lambda", "tebd_get_lambda", "tebd_set_labels", "tebd_get_labels",
     "tebd_two_site_op", "tebd_two_site_op_r", "tebd_two_site_op_nc", "tebd_two_site_op_nc_r",
     "tebd_apply_bonds", "tebd_trotter_step", "tebd_get_singular_values", "tebd_get_sweeps",
-    "tebd_sync", "tebd_last_error", "tebd_kernel_launches",
+    "tebd_sync", "tebd_last_error", "tebd_kernel_launches", "tebd_set_profiling", "tebd_get_stats",
+    "tebd_reset_stats", "tebd_measure_fp64_peak", "tebd_get_stream",
 )
 
 
@@ -83,6 +84,26 @@ class Opts(ctypes.Structure):
         ("reserved", ctypes.c_int),
         ("jacobi_tol", ctypes.c_double),
     ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("updates", ctypes.c_longlong),
+        ("kernel_launches", ctypes.c_longlong),
+        ("jacobi_launches", ctypes.c_longlong),
+        ("jacobi_sweeps", ctypes.c_longlong),
+        ("jacobi_pairs", ctypes.c_longlong),
+        ("jacobi_rotations", ctypes.c_longlong),
+        ("jacobi_flops", ctypes.c_double),
+        ("jacobi_bytes", ctypes.c_double),
+        ("jacobi_ms", ctypes.c_double),
+        ("batch_ms", ctypes.c_double),
+        ("compact_rows", ctypes.c_longlong),
+        ("compact_cols", ctypes.c_longlong),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _lib = None
@@ -120,6 +141,12 @@ def load_library(path: str = LIB_PATH):
     L.tebd_last_error.restype = ctypes.c_char_p
     L.tebd_kernel_launches.argtypes = [vp]
     L.tebd_kernel_launches.restype = ctypes.c_longlong
+    L.tebd_set_profiling.argtypes = [vp, ctypes.c_int]
+    L.tebd_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.tebd_reset_stats.argtypes = [vp]
+    L.tebd_measure_fp64_peak.argtypes = [ctypes.c_int, dp]
+    L.tebd_get_stream.argtypes = [vp]
+    L.tebd_get_stream.restype = ctypes.c_void_p
     _lib = L
     return L
 
@@ -196,6 +223,15 @@ class Chain:
         g = np.zeros((self.chi, self.d, self.chi), dtype=np.complex128, order="F")
         self._check(self._lib.tebd_get_gamma(self.h, site, _dp(g)))
         return g
+
+    def get_gamma_into(self, site, out):
+        """Download Gamma(site) into a caller-owned Fortran-ordered complex128 array."""
+        assert out.dtype == np.complex128 and out.flags.f_contiguous and out.shape == (self.chi, self.d, self.chi)
+        self._check(self._lib.tebd_get_gamma(self.h, site, _dp(out)))
+
+    def get_lambda_into(self, link, out):
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.shape == (self.chi,)
+        self._check(self._lib.tebd_get_lambda(self.h, link, _dp(out)))
 
     def set_lambda(self, link, lam):
         v = np.ascontiguousarray(lam, dtype=np.float64)
@@ -285,6 +321,31 @@ class Chain:
 
     def kernel_launches(self):
         return int(self._lib.tebd_kernel_launches(self.h))
+
+    def set_profiling(self, on=True):
+        self._check(self._lib.tebd_set_profiling(self.h, 1 if on else 0))
+
+    def stats(self):
+        st = Stats()
+        self._check(self._lib.tebd_get_stats(self.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def reset_stats(self):
+        self._check(self._lib.tebd_reset_stats(self.h))
+
+    def stream(self):
+        """The handle's cudaStream_t as an integer."""
+        return int(self._lib.tebd_get_stream(self.h) or 0)
+
+
+def measure_fp64_peak(device=0):
+    """FP64 FMA throughput of the device in TFLOP/s (DFMA loop in the library)."""
+    lib = load_library()
+    v = np.zeros(1)
+    rc = lib.tebd_measure_fp64_peak(device, _dp(v))
+    if rc != TEBD_OK:
+        raise TebdError(rc, "tebd_measure_fp64_peak failed")
+    return float(v[0])
 
 
 # -- reference-named entry points ---------------------------------------------

@@ -95,6 +95,36 @@ def test_rank_deficient_product_state(pkg, oracle):
         assert np.allclose(c.get_lambda(3), np.eye(chi)[0], atol=1e-14)
 
 
+@pytest.mark.parametrize("chi,d", [(9, 3), (40, 2)])
+def test_exact_zero_lambdas_anywhere(pkg, oracle, chi, d):
+    """Rows/columns of exactly-zero Lambdas are dropped from the SVD; zeros at
+    interior positions and differing counts on the three links must give the
+    reference's Lambdas and Gammas' physics."""
+    gam, lam = random_bond(chi, d, 31 + chi)
+    rng = np.random.default_rng(chi)
+    for l, frac in zip(lam[1:4], (0.5, 0.3, 0.7)):
+        l[rng.random(chi) < frac] = 0.0
+        l[0] = max(l[0], 0.1)
+        l /= np.linalg.norm(l)
+    U = random_unitary(d * d, rng)
+    with pkg.Chain(4, d, chi) as c:
+        c.set_state(gam, lam)
+        te = c.two_site_op(2, U)
+        s = c.singular_values(2)
+        g1, g2, l1 = c.get_gamma(2), c.get_gamma(3), c.get_lambda(3)
+    rg1, rg2, rl1, rte, rs = oracle.two_site_op(gam[1], gam[2], lam[1], lam[2], lam[3], U)
+    ok, worst = sigma_ok(s, rs)
+    assert ok, worst
+    assert np.allclose(l1, rl1, atol=1e-11)
+    assert abs(te - rte) < 1e-11
+    rho = obs.two_site_rho(lam[1], g1, l1, g2, lam[3])
+    rrho = obs.two_site_rho(lam[1], rg1, rl1, rg2, lam[3])
+    assert np.allclose(rho, rrho, atol=1e-11)
+    # dropped rows of Gamma1 / columns of Gamma2 are zero, as FormGamma1/2's guard makes them
+    assert np.all(g1[lam[1] == 0] == 0)
+    assert np.all(g2[:, :, lam[3] == 0] == 0)
+
+
 def test_golden_reference_propagators(pkg):
     """The reference's own d=4 gate fixtures (Extensible_Wrapper/Propagator_*.nml),
     against the oracle outputs recorded in tests/golden/propagators_d4.npz."""
