@@ -157,6 +157,25 @@ int tebd_measure_fp64_peak(int device, double *tflops);
  * their own work against the library's. */
 void *tebd_get_stream(tebd_handle *h);
 
+/* Allocation-free dense update of bond `link` of a chain the caller already
+ * holds in device memory.  No counterpart in the reference: it exists for
+ * callers that must not allocate (a region under CUDA-graph capture, a device
+ * memory pool that may not grow after start-up, a host that keeps its own
+ * device-resident chain and no handle).  It calls no cudaMalloc/cudaFree and no
+ * allocating library routine; every temporary lives in one static device array
+ * of about 2.1 MB that each GPU loading this library holds until exit.
+ *   gammas   device, L Gammas back to back, each chi x d x chi complex (Fortran order)
+ *   lambdas  device, L+1 Lambdas back to back, each chi doubles
+ *   op2      device, complex (d^2 x d^2) gate, layout as for tebd_two_site_op
+ *   truncerr host, receives the truncation error
+ *   stream   cudaStream_t to run on (NULL: the legacy default stream)
+ * Limit: d*chi <= 256 (and chi <= 256); larger sizes return TEBD_ERR_ARG.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised. */
+int tebd_two_site_op_noalloc(int L, int d, int chi, int link, double *gammas, double *lambdas,
+                             const double *op2, double *truncerr, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

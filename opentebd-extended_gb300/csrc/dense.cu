@@ -459,3 +459,39 @@ int dense_compact_sizes(tebd_handle *h, int nb, int *nmax) {
 }
 
 }  // namespace tebd
+
+namespace tebd {
+
+// Handle-free launch sequences for one bond (slot 0), used by the
+// allocation-free entry point in noalloc.cu.  Same kernels, same order as
+// launch_dense_prepare / launch_eye / launch_dense_finish.
+void raw_dense_prepare(cudaStream_t st, double2 *gam, const double *lam, const int *links_d,
+                       Slot *slots_d, JacobiProblem<double> *jp, double *nrm_part, double *nrm,
+                       int *status, int chi, int d) {
+  const int n = chi * d;
+  k_compact<<<1, 96, 0, st>>>(lam, links_d, slots_d, jp, chi, d);
+  k_theta_form<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), 1), 256, 0, st>>>(gam, lam, links_d, slots_d,
+                                                                      chi, d);
+  const size_t gsm = sizeof(double2) * (size_t)d * d * d * d;
+  k_gate_apply<<<dim3(cdiv((size_t)chi * chi, 128), 1), 128, gsm, st>>>(slots_d, chi, d);
+  k_norm_partial<<<dim3(kNormParts, 1), 256, 0, st>>>(slots_d, nrm_part);
+  k_norm_final<<<1, 32, 0, st>>>(nrm_part, nrm, jp, 1, status);
+  const size_t total = (size_t)n * n;
+  unsigned gx = cdiv(total, 256);
+  if (gx > 1024) gx = 1024;
+  k_eye<<<dim3(gx, 1), 256, 0, st>>>(slots_d);
+}
+
+void raw_dense_finish(cudaStream_t st, double2 *gam, double *lam, const int *links_d,
+                      Slot *slots_d, const double *nrm, double *truncerr, int *status, int chi,
+                      int d) {
+  const int n = chi * d;
+  k_sigma_sort<<<1, 1024, sizeof(double) * n, st>>>(slots_d, nrm, n, status);
+  k_lambda<<<1, 32, 0, st>>>(slots_d, links_d, lam, truncerr, chi, 1);
+  k_restore_gamma1<<<dim3(cdiv((size_t)n * chi, 256), 1), 256, 0, st>>>(gam, lam, links_d, slots_d,
+                                                                       nrm, chi, d);
+  k_restore_gamma2<<<dim3(cdiv(chi, 32), cdiv(n, 32), 1), 256, 0, st>>>(gam, lam, links_d, slots_d,
+                                                                       chi, d);
+}
+
+}  // namespace tebd

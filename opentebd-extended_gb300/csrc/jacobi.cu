@@ -307,3 +307,22 @@ int measure_fp64_peak(int device, double *tflops) {
 }
 
 }  // namespace tebd
+
+namespace tebd {
+
+// Handle-free Jacobi launches for the allocation-free entry point (noalloc.cu).
+void raw_jacobi_init(cudaStream_t st, int *rot, int *done, int *sweeps) {
+  k_jacobi_init<<<1, 64, 0, st>>>(1, rot, done, sweeps);
+}
+
+void raw_jacobi_sweep(cudaStream_t st, const JacobiProblem<double> *probs_d, int *rot, int *done,
+                      int *sweeps, int *pending, unsigned long long *counters, int nmax,
+                      double tol) {
+  const int npad = nmax + (nmax & 1);
+  const unsigned gx = (unsigned)((npad / 2 + kJacobiWarps - 1) / kJacobiWarps);
+  for (int r = 0; r < npad - 1; ++r)
+    k_jacobi_round<double><<<dim3(gx, 1), kJacobiWarps * 32, 0, st>>>(probs_d, done, rot, r, tol);
+  k_jacobi_sweep_end<double><<<1, 32, 0, st>>>(probs_d, 1, rot, done, sweeps, pending, counters);
+}
+
+}  // namespace tebd

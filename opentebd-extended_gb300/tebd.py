@@ -60,7 +60,7 @@ EXPORTED_SYMBOLS = (
     "tebd_two_site_op", "tebd_two_site_op_r", "tebd_two_site_op_nc", "tebd_two_site_op_nc_r",
     "tebd_apply_bonds", "tebd_trotter_step", "tebd_get_singular_values", "tebd_get_sweeps",
     "tebd_sync", "tebd_last_error", "tebd_kernel_launches", "tebd_set_profiling", "tebd_get_stats",
-    "tebd_reset_stats", "tebd_measure_fp64_peak", "tebd_get_stream",
+    "tebd_reset_stats", "tebd_measure_fp64_peak", "tebd_get_stream", "tebd_two_site_op_noalloc",
 )
 
 
@@ -147,6 +147,7 @@ def load_library(path: str = LIB_PATH):
     L.tebd_measure_fp64_peak.argtypes = [ctypes.c_int, dp]
     L.tebd_get_stream.argtypes = [vp]
     L.tebd_get_stream.restype = ctypes.c_void_p
+    L.tebd_two_site_op_noalloc.argtypes = [ctypes.c_int] * 4 + [vp, vp, vp, dp, vp]
     _lib = L
     return L
 
