@@ -58,9 +58,10 @@ extern "C" {
 #define TEBD_MODE_DENSE 0         /* TwoSiteOp: no symmetry                            */
 #define TEBD_MODE_NC 1            /* TwoSiteOpNC: U(1) number conservation             */
 
-/* SVD precision */
-#define TEBD_SVD_FP64 0           /* plain: FP64 one-sided Jacobi from the start        */
-#define TEBD_SVD_MIXED 1          /* FP32 Jacobi sweeps, then FP64 sweeps to converge   */
+/* SVD algorithm (all FP64) */
+#define TEBD_SVD_FP64 0           /* default: column-pivoted QR to the numerical rank,
+                                     then one-sided Jacobi on R^H                      */
+#define TEBD_SVD_JACOBI 2         /* one-sided Jacobi on the whole (compacted) Theta    */
 
 #define TEBD_OPTS_VERSION 1
 
@@ -69,7 +70,7 @@ typedef struct tebd_opts {
   int device;         /* CUDA device ordinal                                           */
   int tot_num;        /* NC mode: total particle number (reference global totNum)      */
   int max_filling;    /* NC mode: maximum occupation (reference global maxFilling)     */
-  int svd_mode;       /* TEBD_SVD_FP64 or TEBD_SVD_MIXED                               */
+  int svd_mode;       /* TEBD_SVD_FP64 or TEBD_SVD_JACOBI                              */
   int max_sweeps;     /* Jacobi sweep cap; 0 selects the default (60)                  */
   int max_batch;      /* bonds updated concurrently; 0 = all bonds of one parity       */
   int reserved;
@@ -147,6 +148,9 @@ typedef struct tebd_stats {
   double batch_ms;             /* device time of whole bond batches (profiling on)      */
   long long compact_rows;      /* sum over updates of the SVD's row count (d * kept chi) */
   long long compact_cols;      /* sum over updates of the SVD's column count            */
+  double qr_flops;             /* algorithmic FP64 flops of the pivoted QR and of U = QZ */
+  double qr_ms;                /* device time of the pivoted-QR kernel (profiling on)   */
+  long long rank_sum;          /* sum over updates of the numerical rank k              */
 } tebd_stats;
 int tebd_set_profiling(tebd_handle *h, int on);
 int tebd_get_stats(tebd_handle *h, tebd_stats *stats);

@@ -75,6 +75,8 @@ static void free_all(tebd_handle *h) {
   cudaFree(h->ws_base);
   cudaFree(h->slots_d);
   cudaFree(h->gates_d);
+  cudaFree(h->cp_d);
+  cudaFree(h->idx_d);
   cudaFree(h->nrm_part);
   cudaFree(h->nrm);
   cudaFree(h->truncerr_d);
@@ -118,7 +120,7 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
     o = *opts;
   }
   if (L < 2 || d < 1 || d > 8 || chi < 1 || (mode != TEBD_MODE_DENSE && mode != TEBD_MODE_NC) ||
-      (o.svd_mode != TEBD_SVD_FP64 && o.svd_mode != TEBD_SVD_MIXED)) {
+      (o.svd_mode != TEBD_SVD_FP64 && o.svd_mode != TEBD_SVD_JACOBI)) {
     g_noh_err = "tebd_create: invalid L/d/chi/mode (need L>=2, 1<=d<=8, chi>=1)";
     return TEBD_ERR_ARG;
   }
@@ -126,8 +128,9 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
     g_noh_err = "tebd_create: d*chi > 8192 is not supported";
     return TEBD_ERR_ARG;
   }
-  if (mode == TEBD_MODE_NC && (o.tot_num < 0 || o.max_filling < 0)) {
-    g_noh_err = "tebd_create: NC mode needs tot_num >= 0 and max_filling >= 0";
+  if (mode == TEBD_MODE_NC && (o.tot_num < 0 || o.tot_num >= 1000 || o.max_filling < 0)) {
+    // labels >= 1000 mean "unused" in the reference, so particle numbers stay below 1000
+    g_noh_err = "tebd_create: NC mode needs 0 <= tot_num < 1000 and max_filling >= 0";
     return TEBD_ERR_ARG;
   }
   tebd_handle *h = new (std::nothrow) tebd_handle();
@@ -173,12 +176,12 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
   if ((rc = dalloc(h, &h->lab_l, sizeof(int) * (size_t)chi * (L + 1), "alloc labels"))) FAIL(rc);
   if ((rc = dalloc(h, &h->lab_r, sizeof(int) * (size_t)chi * (L + 1), "alloc labels"))) FAIL(rc);
   // workspace carve
-  const bool mixed = o.svd_mode == TEBD_SVD_MIXED;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t nn = (size_t)n * n;
+  // per slot: X, V (n^2 each), S, perm, QR buffers (jpvt, tau, 2n norms), aux (3 n^2)
   size_t per = al(sizeof(double2) * nn) * 2 + al(sizeof(double) * n) + al(sizeof(int) * n) +
-               al(sizeof(double2) * (size_t)d * d * d * d);
-  if (mixed) per += al(sizeof(float2) * nn) * 2 + al(sizeof(double2) * nn);
+               al(sizeof(int) * n) + al(sizeof(double2) * n) + al(sizeof(double) * 2 * n) +
+               al(sizeof(double2) * 3 * nn);
   h->ws_bytes = per * ns;
   if ((rc = dalloc(h, (char **)&h->ws_base, h->ws_bytes, "alloc SVD workspaces"))) FAIL(rc);
   if ((rc = dalloc(h, &h->gates_d, sizeof(double2) * (size_t)ns * d * d * d * d, "alloc gates")))
@@ -199,15 +202,14 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
       p += al(sizeof(double) * n);
       S.perm = (int *)p;
       p += al(sizeof(int) * n);
-      p += al(sizeof(double2) * (size_t)d * d * d * d);  // unused: gates live in gates_d
-      if (mixed) {
-        S.Xf = (float2 *)p;
-        p += al(sizeof(float2) * nn);
-        S.Vf = (float2 *)p;
-        p += al(sizeof(float2) * nn);
-        S.theta0 = (double2 *)p;
-        p += al(sizeof(double2) * nn);
-      }
+      S.jpvt = (int *)p;
+      p += al(sizeof(int) * n);
+      S.tau = (double2 *)p;
+      p += al(sizeof(double2) * n);
+      S.vn = (double *)p;
+      p += al(sizeof(double) * 2 * n);
+      S.aux = (double2 *)p;
+      p += al(sizeof(double2) * 3 * nn);
       S.gate = h->gates_d + (size_t)s * d * d * d * d;
       int *ix = h->idx_d + (size_t)s * 5 * chi;
       S.idx0 = ix;
@@ -232,23 +234,13 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
                                        cudaMemcpyHostToDevice),
                          "upload jprob")))
       FAIL(rc);
-    if (mixed) {
-      std::vector<JacobiProblem<float>> jf(ns);
-      for (int s = 0; s < ns; ++s) jf[s] = {h->slots[s].Xf, h->slots[s].Vf, n, n, n, n, 0.0};
-      if ((rc = dalloc(h, (char **)&h->jprobf_d, sizeof(JacobiProblem<float>) * ns, "alloc jprobf")))
-        FAIL(rc);
-      if ((rc = check_cuda(h, cudaMemcpy(h->jprobf_d, jf.data(), sizeof(JacobiProblem<float>) * ns,
-                                         cudaMemcpyHostToDevice),
-                           "upload jprobf")))
-        FAIL(rc);
-    }
   }
   if ((rc = dalloc(h, &h->nrm_part, sizeof(double) * ns * kNormParts, "alloc norm"))) FAIL(rc);
   if ((rc = dalloc(h, &h->nrm, sizeof(double) * ns, "alloc norm"))) FAIL(rc);
   if ((rc = dalloc(h, &h->truncerr_d, sizeof(double) * ns, "alloc truncerr"))) FAIL(rc);
   if ((rc = dalloc(h, &h->links_d, sizeof(int) * ns, "alloc links"))) FAIL(rc);
   h->js_cap = ns * (mode == TEBD_MODE_NC ? (o.tot_num + 2 > 64 ? o.tot_num + 2 : 64) : 1);
-  if ((rc = dalloc(h, &h->js.rot, sizeof(int) * h->js_cap, "alloc jacobi state"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->js.rot, sizeof(int) * 2 * h->js_cap, "alloc jacobi state"))) FAIL(rc);
   if ((rc = dalloc(h, &h->js.done, sizeof(int) * h->js_cap, "alloc jacobi state"))) FAIL(rc);
   if ((rc = dalloc(h, &h->js.sweeps, sizeof(int) * h->js_cap, "alloc jacobi state"))) FAIL(rc);
   if ((rc = dalloc(h, &h->js.pending, sizeof(int) * 4, "alloc jacobi state"))) FAIL(rc);
@@ -423,10 +415,14 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
   int rc;
   if (h->mode == TEBD_MODE_DENSE) {
     if ((rc = launch_dense_prepare(h, nb, false))) return rc;
-    if ((rc = launch_eye(h, nb))) return rc;
     int nmax = 0;
     if ((rc = dense_compact_sizes(h, nb, &nmax))) return rc;
-    if ((rc = run_jacobi(h, nb, h->opts.svd_mode, nmax))) return rc;
+    if (h->opts.svd_mode == TEBD_SVD_JACOBI) {
+      if ((rc = launch_eye(h, nb))) return rc;
+      if ((rc = run_jacobi(h, nb, h->opts.svd_mode, nmax))) return rc;
+    } else {
+      if ((rc = run_qrj(h, nb, nmax))) return rc;
+    }
     if ((rc = launch_dense_finish(h, nb))) return rc;
   } else {
     if ((rc = run_nc_batch(h, nb, links, nullptr))) return rc;

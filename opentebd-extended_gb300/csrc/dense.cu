@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(96) k_compact(const double *__restrict__ lam, 
     c.r2 = cnt[2];
     c.m = d * cnt[0];
     c.n = d * cnt[2];
+    c.k = c.n;
     *slots[s].cp = c;
     jp[s].m = c.m;
     jp[s].n = c.n;
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(1024) k_sigma_sort(Slot *slots, const double *
   extern __shared__ double sig[];  // n
   const int s = blockIdx.x;
   const Compact cp = *slots[s].cp;
-  const int m = cp.m, n = cp.n;
+  const int m = cp.m, n = cp.k;  // X holds k columns sigma_c u_c (k = n for plain Jacobi)
   const double2 *X = slots[s].X;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int c = warp; c < n; c += nw) {
@@ -331,7 +332,7 @@ __global__ void k_restore_gamma1(double2 *gam, const double *lam, const int *lin
   const double *l0 = lam + (size_t)(link - 1) * chi;
   double2 out = make_double2(0.0, 0.0);
   const int ap = slots[s].inv0[alpha];
-  if (beta < cp.n && ap >= 0 && fabs(l0[alpha]) > kGuardDense) {
+  if (beta < cp.k && ap >= 0 && fabs(l0[alpha]) > kGuardDense) {
     const double sigma = slots[s].S[beta] * nrm[s];
     if (sigma > 0.0) {
       const int col = slots[s].perm[beta];
@@ -360,7 +361,7 @@ __global__ void __launch_bounds__(256) k_restore_gamma2(double2 *gam, const doub
   for (int yy = ty; yy < 32; yy += 8) {
     const int alpha = a0 + yy, c = c0 + tx;
     double2 v = make_double2(0.0, 0.0);
-    if (alpha < chi && alpha < cp.n && c < nf) {
+    if (alpha < chi && alpha < cp.k && c < nf) {
       const int bp = inv2[c % chi];
       if (bp >= 0) v = V[(size_t)((c / chi) * cp.r2 + bp) + (size_t)cp.n * perm[alpha]];
     }

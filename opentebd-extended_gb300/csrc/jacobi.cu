@@ -20,7 +20,10 @@
 // rotation ends the problem.  A problem that exceeds the sweep cap reports
 // TEBD_ERR_SVD_NOCONV.  Every wait is a host-side loop over bounded launches:
 // no kernel spins.
+#include <cooperative_groups.h>
 #include <math.h>
+
+#include <vector>
 
 #include "tebd_internal.cuh"
 
@@ -58,7 +61,7 @@ __device__ __forceinline__ bool jacobi_pair(typename cplx<T>::type *__restrict__
   using C2 = typename cplx<T>::type;
   T al = 0, be = 0, gr = 0, gi = 0;
   for (int r = lane; r < m; r += 32) {
-    const C2 a = A[r], b = B[r];
+    const C2 a = __ldcg(A + r), b = __ldcg(B + r);
     al = fma(a.x, a.x, fma(a.y, a.y, al));
     be = fma(b.x, b.x, fma(b.y, b.y, be));
     gr = fma(a.x, b.x, fma(a.y, b.y, gr));
@@ -80,7 +83,7 @@ __device__ __forceinline__ bool jacobi_pair(typename cplx<T>::type *__restrict__
   const T s = c * t;
   const T sr = s * (gr / g), si = s * (gi / g);
   for (int r = lane; r < m; r += 32) {
-    const C2 a = A[r], b = B[r];
+    const C2 a = __ldcg(A + r), b = __ldcg(B + r);
     C2 na, nb;
     na.x = fma(c, a.x, fma(-sr, b.x, -si * b.y));
     na.y = fma(c, a.y, fma(-sr, b.y, si * b.x));
@@ -90,7 +93,7 @@ __device__ __forceinline__ bool jacobi_pair(typename cplx<T>::type *__restrict__
     B[r] = nb;
   }
   for (int r = lane; r < nv; r += 32) {
-    const C2 a = VA[r], b = VB[r];
+    const C2 a = __ldcg(VA + r), b = __ldcg(VB + r);
     C2 na, nb;
     na.x = fma(c, a.x, fma(-sr, b.x, -si * b.y));
     na.y = fma(c, a.y, fma(-sr, b.y, si * b.x));
@@ -178,6 +181,134 @@ __global__ void k_jacobi_sweep_end(const JacobiProblem<T> *__restrict__ probs, i
   pending[0] = cnt;
 }
 
+// ---------------------------------------------------------------------------
+// Persistent variant: one thread-block cluster per problem runs every round of
+// every sweep in a single launch.  The rounds of a sweep are separated by
+// cluster barriers (barrier.cluster arrive.release / wait.acquire), which order
+// the global-memory column updates between the CTAs of the cluster; no launch
+// per round.  The rotation count of a sweep is summed in a per-problem counter
+// (two, alternating by sweep parity) that every CTA reads after the sweep's
+// last barrier, so all CTAs of a cluster take the same exit decision.  The loop
+// is bounded by the sweep cap; nothing spins.
+// ---------------------------------------------------------------------------
+constexpr int kPW = 16;  // warps per CTA of the persistent kernel
+
+template <typename T>
+__global__ void __launch_bounds__(kPW * 32)
+    k_jacobi_persistent(const JacobiProblem<T> *__restrict__ probs, int *__restrict__ rotc,
+                        int *__restrict__ done, int *__restrict__ sweeps,
+                        unsigned long long *__restrict__ counters, T tol, int max_sweeps) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int p = blockIdx.y;
+  const int crank = (int)cluster.block_rank();
+  const int C = (int)cluster.num_blocks();
+  const JacobiProblem<T> P = probs[p];
+  const int npad = P.n + (P.n & 1), R = npad - 1, half = npad / 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gw = crank * kPW + warp, nw = C * kPW;
+  int sw = 0, converged = (P.n < 2);
+  unsigned long long nrot = 0, npairs = 0, rows = 0, rrows = 0;
+  for (; sw < max_sweeps && !converged; ++sw) {
+    int *cnt = rotc + 2 * p + (sw & 1);
+    int local = 0;
+    for (int r = 0; r < R; ++r) {
+      for (int k = gw; k < half; k += nw) {
+        int i, j;
+        if (k == 0) {
+          i = R;
+          j = r;
+        } else {
+          i = (r + k) % R;
+          j = (r - k + R) % R;
+        }
+        if (i > j) {
+          const int t = i;
+          i = j;
+          j = t;
+        }
+        if (j < P.n &&
+            jacobi_pair<T>(P.X + (size_t)P.ldx * i, P.X + (size_t)P.ldx * j, P.V + (size_t)P.ldv * i,
+                           P.V + (size_t)P.ldv * j, P.m, P.n, lane, tol, P.floor))
+          local += (lane == 0);
+      }
+      cluster.sync();
+      // the other parity's counter was last read before this sweep's first barrier
+      if (r == 0 && crank == 0 && threadIdx.x == 0) rotc[2 * p + ((sw + 1) & 1)] = 0;
+    }
+    if (local) atomicAdd(cnt, local);
+    cluster.sync();
+    const int total = __ldcg(cnt);
+    if (crank == 0 && threadIdx.x == 0) {
+      const unsigned long long pairs = (unsigned long long)P.n * (unsigned long long)(P.n - 1) / 2;
+      npairs += pairs;
+      rows += pairs * (unsigned long long)P.m;
+      nrot += (unsigned long long)total;
+      rrows += (unsigned long long)total * (unsigned long long)(P.m + P.n);
+    }
+    converged = (total == 0);
+  }
+  if (crank == 0 && threadIdx.x == 0) {
+    sweeps[p] = sw;
+    done[p] = converged;
+    atomicAdd(&counters[0], nrot);
+    atomicAdd(&counters[1], npairs);
+    atomicAdd(&counters[2], rows);
+    atomicAdd(&counters[3], rrows);
+  }
+}
+
+// Cluster size: enough warps for the pairs of one round, at most 8 CTAs.
+static int persistent_cluster_size(int nmax) {
+  const int half = (nmax + (nmax & 1)) / 2;
+  int c = (half + kPW - 1) / kPW;
+  return c < 1 ? 1 : (c > 8 ? 8 : c);
+}
+
+template <typename T>
+static int jacobi_persistent(tebd_handle *h, const JacobiProblem<T> *probs_d, int nprob, int nmax,
+                             T tol, int max_sweeps) {
+  cudaStream_t st = h->stream;
+  int rc = check_cuda(h, cudaMemsetAsync(h->js.rot, 0, sizeof(int) * 2 * nprob, st), "reset counters");
+  if (rc) return rc;
+  const int C = persistent_cluster_size(nmax);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C, nprob, 1);
+  cfg.blockDim = dim3(kPW * 32, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (h->profiling) cudaEventRecord(h->ev[0], st);
+  rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_jacobi_persistent<T>, probs_d, h->js.rot, h->js.done,
+                                        h->js.sweeps, h->js.counters, tol, max_sweeps),
+                  "jacobi persistent launch");
+  if (rc) return rc;
+  TEBD_LAUNCHED(h);
+  h->stats.jacobi_launches += 1;
+  if (h->profiling) cudaEventRecord(h->ev[1], st);
+  // convergence flags of the batch
+  std::vector<int> dn(nprob);
+  rc = check_cuda(h, cudaMemcpyAsync(dn.data(), h->js.done, sizeof(int) * nprob,
+                                     cudaMemcpyDeviceToHost, st), "read convergence");
+  if (rc) return rc;
+  rc = check_cuda(h, cudaStreamSynchronize(st), "jacobi persistent");
+  if (rc) return rc;
+  if (h->profiling) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]) == cudaSuccess) h->stats.jacobi_ms += ms;
+  }
+  for (int p = 0; p < nprob; ++p)
+    if (!dn[p])
+      return set_error(h, TEBD_ERR_SVD_NOCONV, "Jacobi SVD did not converge within the sweep cap");
+  return TEBD_OK;
+}
+
 template <typename T>
 static int jacobi_sweeps(tebd_handle *h, const JacobiProblem<T> *probs_d, int nprob, int nmax,
                          T tol, int max_sweeps, int *sweeps_used) {
@@ -223,9 +354,8 @@ int run_jacobi(tebd_handle *h, int nb, int /*svd_mode*/, int nmax) {
   const double tol =
       h->opts.jacobi_tol > 0 ? h->opts.jacobi_tol : (double)(n > 16 ? n : 16) * 2.220446049250313e-16;
   const int cap = h->opts.max_sweeps > 0 ? h->opts.max_sweeps : 60;
-  int used = 0;
-  return jacobi_sweeps<double>(h, reinterpret_cast<const JacobiProblem<double> *>(h->jprob_d), nb, n,
-                               tol, cap, &used);
+  return jacobi_persistent<double>(h, reinterpret_cast<const JacobiProblem<double> *>(h->jprob_d), nb,
+                                   n, tol, cap);
 }
 
 // Generic entry used by the NC path: caller-provided problem table.
@@ -235,8 +365,7 @@ int run_jacobi_problems(tebd_handle *h, const JacobiProblem<double> *probs_d, in
   const double tol =
       h->opts.jacobi_tol > 0 ? h->opts.jacobi_tol : (double)(nmax > 8 ? nmax : 8) * 2.220446049250313e-16;
   const int cap = h->opts.max_sweeps > 0 ? h->opts.max_sweeps : 60;
-  int used = 0;
-  return jacobi_sweeps<double>(h, probs_d, nprob, nmax, tol, cap, &used);
+  return jacobi_persistent<double>(h, probs_d, nprob, nmax, tol, cap);
 }
 
 // Read the device work counters into the handle's stats (called after a batch).
@@ -323,6 +452,16 @@ void raw_jacobi_sweep(cudaStream_t st, const JacobiProblem<double> *probs_d, int
   for (int r = 0; r < npad - 1; ++r)
     k_jacobi_round<double><<<dim3(gx, 1), kJacobiWarps * 32, 0, st>>>(probs_d, done, rot, r, tol);
   k_jacobi_sweep_end<double><<<1, 32, 0, st>>>(probs_d, 1, rot, done, sweeps, pending, counters);
+}
+
+}  // namespace tebd
+
+namespace tebd {
+
+// Non-template entry for the QR-preconditioned path (qrj.cu).
+int jacobi_persistent_double(tebd_handle *h, const JacobiProblem<double> *probs_d, int nprob,
+                             int nmax, double tol, int max_sweeps) {
+  return jacobi_persistent<double>(h, probs_d, nprob, nmax, tol, max_sweeps);
 }
 
 }  // namespace tebd

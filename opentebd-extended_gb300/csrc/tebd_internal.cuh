@@ -90,6 +90,7 @@ struct JacobiState {
 struct Compact {
   int r0, r1, r2;  // kept counts of Lambda0, Lambda1, Lambda2
   int m, n;        // d*r0 rows, d*r2 columns
+  int k;           // singular triplets computed (numerical rank for the QR path, else n)
 };
 
 struct Slot {
@@ -102,6 +103,11 @@ struct Slot {
   int *idx0, *idx1, *idx2;  // kept alpha / gamma / beta (chi each)
   int *inv0, *inv2;         // alpha -> a' and beta -> b' (-1 if dropped)
   Compact *cp;              // device compaction record
+  // QR-preconditioned SVD (qrj.cu)
+  int *jpvt;                // n column permutation of the pivoted QR
+  double2 *tau;             // n reflector scalars
+  double *vn;               // 2n partial column norms (later: the k singular values)
+  double2 *aux;             // 3 n^2: A = R^H (n x k), Z (k x k), Y = Q [Z; 0] (m x k)
 };
 
 }  // namespace tebd
@@ -135,6 +141,7 @@ struct tebd_handle {
   // NC workspaces (allocated in NC mode)
   void *nc_ws;
   size_t nc_ws_bytes;
+  void *nc_meta;  // host-side NC slot table (nc.cu)
   // last spectrum per link (tebd_get_singular_values / tebd_get_sweeps)
   double *sig_link_d;            // (L-1) * n
   int *sig_count_d;              // L-1
@@ -162,6 +169,9 @@ int dense_compact_sizes(tebd_handle *h, int nb, int *nmax);
 int launch_dense_finish(tebd_handle *h, int nb);
 int launch_eye(tebd_handle *h, int nb);
 int run_jacobi_problems(tebd_handle *h, const JacobiProblem<double> *probs_d, int nprob, int nmax);
+int jacobi_persistent_double(tebd_handle *h, const JacobiProblem<double> *probs_d, int nprob,
+                             int nmax, double tol, int max_sweeps);
+int run_qrj(tebd_handle *h, int nb, int nmax);
 int jacobi_collect(tebd_handle *h);
 int measure_fp64_peak(int device, double *tflops);
 int run_nc_batch(tebd_handle *h, int nb, const int *links_host, double *truncerr_host);

@@ -40,7 +40,7 @@ TEBD_ERR_NC_BLOCKS = 7
 MODE_DENSE = 0
 MODE_NC = 1
 SVD_FP64 = 0
-SVD_MIXED = 1
+SVD_JACOBI = 2
 OPTS_VERSION = 1
 
 ERROR_NAMES = {
@@ -100,6 +100,9 @@ class Stats(ctypes.Structure):
         ("batch_ms", ctypes.c_double),
         ("compact_rows", ctypes.c_longlong),
         ("compact_cols", ctypes.c_longlong),
+        ("qr_flops", ctypes.c_double),
+        ("qr_ms", ctypes.c_double),
+        ("rank_sum", ctypes.c_longlong),
     ]
 
     def as_dict(self):

@@ -40,11 +40,13 @@ def random_unitary(n, rng):
     return q * (np.diag(r) / np.abs(np.diag(r)))
 
 
+@pytest.mark.parametrize("svd_mode", [0, 2])
 @pytest.mark.parametrize("chi,d", [(1, 2), (8, 2), (16, 3), (12, 5), (32, 4)])
-def test_single_update_matches_oracle(pkg, oracle, chi, d):
+def test_single_update_matches_oracle(pkg, oracle, chi, d, svd_mode):
+    """Both SVD algorithms: pivoted QR + Jacobi on R^H (0, default) and plain Jacobi (2)."""
     gam, lam = random_bond(chi, d, 100 + chi + d)
     U = random_unitary(d * d, np.random.default_rng(chi * d))
-    with pkg.Chain(4, d, chi) as c:
+    with pkg.Chain(4, d, chi, svd_mode=svd_mode) as c:
         c.set_state(gam, lam)
         te = c.two_site_op(2, U)
         s = c.singular_values(2)
