@@ -179,9 +179,11 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t nn = (size_t)n * n;
   // per slot: X, V (n^2 each), S, perm, QR buffers (jpvt, tau, 2n norms), aux (3 n^2)
+  // (the QR buffers and aux serve the dense path only; NC blocks live in X and V)
+  const size_t aux_elems = mode == TEBD_MODE_DENSE ? 3 * nn : 0;
   size_t per = al(sizeof(double2) * nn) * 2 + al(sizeof(double) * n) + al(sizeof(int) * n) +
                al(sizeof(int) * n) + al(sizeof(double2) * n) + al(sizeof(double) * 2 * n) +
-               al(sizeof(double2) * 3 * nn);
+               al(sizeof(double2) * aux_elems);
   h->ws_bytes = per * ns;
   if ((rc = dalloc(h, (char **)&h->ws_base, h->ws_bytes, "alloc SVD workspaces"))) FAIL(rc);
   if ((rc = dalloc(h, &h->gates_d, sizeof(double2) * (size_t)ns * d * d * d * d, "alloc gates")))
@@ -208,8 +210,8 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
       p += al(sizeof(double2) * n);
       S.vn = (double *)p;
       p += al(sizeof(double) * 2 * n);
-      S.aux = (double2 *)p;
-      p += al(sizeof(double2) * 3 * nn);
+      S.aux = aux_elems ? (double2 *)p : nullptr;
+      p += al(sizeof(double2) * aux_elems);
       S.gate = h->gates_d + (size_t)s * d * d * d * d;
       int *ix = h->idx_d + (size_t)s * 5 * chi;
       S.idx0 = ix;
