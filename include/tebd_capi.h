@@ -59,9 +59,12 @@ extern "C" {
 #define TEBD_MODE_NC 1            /* TwoSiteOpNC: U(1) number conservation             */
 
 /* SVD algorithm (all FP64) */
-#define TEBD_SVD_FP64 0           /* default: column-pivoted QR to the numerical rank,
-                                     then one-sided Jacobi on R^H                      */
+#define TEBD_SVD_FP64 0           /* default: per bond, bidiagonalisation for a large
+                                     tall/square compacted Theta (>= 256 columns), else
+                                     column-pivoted QR + one-sided Jacobi on R^H        */
 #define TEBD_SVD_JACOBI 2         /* one-sided Jacobi on the whole (compacted) Theta    */
+#define TEBD_SVD_BIDIAG 3         /* bidiagonalisation for every tall/square Theta      */
+#define TEBD_SVD_QRJ 4            /* pivoted QR + Jacobi on R^H for every bond          */
 
 #define TEBD_OPTS_VERSION 1
 
@@ -70,7 +73,7 @@ typedef struct tebd_opts {
   int device;         /* CUDA device ordinal                                           */
   int tot_num;        /* NC mode: total particle number (reference global totNum)      */
   int max_filling;    /* NC mode: maximum occupation (reference global maxFilling)     */
-  int svd_mode;       /* TEBD_SVD_FP64 or TEBD_SVD_JACOBI                              */
+  int svd_mode;       /* TEBD_SVD_FP64 (default), _JACOBI, _BIDIAG or _QRJ             */
   int max_sweeps;     /* Jacobi sweep cap; 0 selects the default (60)                  */
   int max_batch;      /* bonds updated concurrently; 0 = all bonds of one parity       */
   int reserved;
@@ -151,6 +154,8 @@ typedef struct tebd_stats {
   double qr_flops;             /* algorithmic FP64 flops of the pivoted QR and of U = QZ */
   double qr_ms;                /* device time of the pivoted-QR kernel (profiling on)   */
   long long rank_sum;          /* sum over updates of the numerical rank k              */
+  double bidiag_ms;            /* device time of the bidiagonal route (profiling on)     */
+  long long bidiag_updates;    /* updates that took the bidiagonal route                */
 } tebd_stats;
 int tebd_set_profiling(tebd_handle *h, int on);
 int tebd_get_stats(tebd_handle *h, tebd_stats *stats);

@@ -76,6 +76,7 @@ static void free_all(tebd_handle *h) {
   cudaFree(h->slots_d);
   cudaFree(h->gates_d);
   cudaFree(h->cp_d);
+  cudaFree(h->path_d);
   cudaFree(h->idx_d);
   cudaFree(h->nrm_part);
   cudaFree(h->nrm);
@@ -120,7 +121,8 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
     o = *opts;
   }
   if (L < 2 || d < 1 || d > 8 || chi < 1 || (mode != TEBD_MODE_DENSE && mode != TEBD_MODE_NC) ||
-      (o.svd_mode != TEBD_SVD_FP64 && o.svd_mode != TEBD_SVD_JACOBI)) {
+      (o.svd_mode != TEBD_SVD_FP64 && o.svd_mode != TEBD_SVD_JACOBI &&
+       o.svd_mode != TEBD_SVD_BIDIAG && o.svd_mode != TEBD_SVD_QRJ)) {
     g_noh_err = "tebd_create: invalid L/d/chi/mode (need L>=2, 1<=d<=8, chi>=1)";
     return TEBD_ERR_ARG;
   }
@@ -181,14 +183,17 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
   // per slot: X, V (n^2 each), S, perm, QR buffers (jpvt, tau, 2n norms), aux (3 n^2)
   // (the QR buffers and aux serve the dense path only; NC blocks live in X and V)
   const size_t aux_elems = mode == TEBD_MODE_DENSE ? 3 * nn : 0;
+  const size_t bd_elems = mode == TEBD_MODE_DENSE ? bidiag_ws_doubles(n, chi) : 0;
   size_t per = al(sizeof(double2) * nn) * 2 + al(sizeof(double) * n) + al(sizeof(int) * n) +
-               al(sizeof(int) * n) + al(sizeof(double2) * n) + al(sizeof(double) * 2 * n) +
-               al(sizeof(double2) * aux_elems);
+               al(sizeof(int) * n) + al(sizeof(double2) * n) * 2 + al(sizeof(double) * 2 * n) +
+               al(sizeof(double2) * aux_elems) + al(sizeof(double) * bd_elems);
   h->ws_bytes = per * ns;
   if ((rc = dalloc(h, (char **)&h->ws_base, h->ws_bytes, "alloc SVD workspaces"))) FAIL(rc);
   if ((rc = dalloc(h, &h->gates_d, sizeof(double2) * (size_t)ns * d * d * d * d, "alloc gates")))
     FAIL(rc);
   if ((rc = dalloc(h, &h->cp_d, sizeof(Compact) * ns, "alloc compaction records"))) FAIL(rc);
+  if ((rc = dalloc(h, &h->path_d, sizeof(int) * ns, "alloc SVD routes"))) FAIL(rc);
+  h->path_h.assign(ns, kPathQRJ);
   if ((rc = dalloc(h, &h->idx_d, sizeof(int) * (size_t)ns * 5 * chi, "alloc index maps"))) FAIL(rc);
   h->slots.resize(ns);
   {
@@ -212,6 +217,10 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
       p += al(sizeof(double) * 2 * n);
       S.aux = aux_elems ? (double2 *)p : nullptr;
       p += al(sizeof(double2) * aux_elems);
+      S.taup = (double2 *)p;
+      p += al(sizeof(double2) * n);
+      S.bdws = bd_elems ? (double *)p : nullptr;
+      p += al(sizeof(double) * bd_elems);
       S.gate = h->gates_d + (size_t)s * d * d * d * d;
       int *ix = h->idx_d + (size_t)s * 5 * chi;
       S.idx0 = ix;
@@ -418,12 +427,34 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
   if (h->mode == TEBD_MODE_DENSE) {
     if ((rc = launch_dense_prepare(h, nb, false))) return rc;
     int nmax = 0;
-    if ((rc = dense_compact_sizes(h, nb, &nmax))) return rc;
+    std::vector<Compact> cps;
+    if ((rc = dense_compact_sizes(h, nb, &nmax, &cps))) return rc;
     if (h->opts.svd_mode == TEBD_SVD_JACOBI) {
+      CK(cudaMemsetAsync(h->path_d, 0, sizeof(int) * nb, h->stream), "reset SVD routes");
       if ((rc = launch_eye(h, nb))) return rc;
       if ((rc = run_jacobi(h, nb, h->opts.svd_mode, nmax))) return rc;
     } else {
-      if ((rc = run_qrj(h, nb, nmax))) return rc;
+      // route per bond: bidiagonalisation when the compacted Theta is large in both
+      // dimensions (default: min(m, n) >= kBidiagMinDim; a wide Theta is bidiagonalised
+      // as Theta^H), pivoted QR + Jacobi on R^H otherwise (low rank, cheap sweeps)
+      int nbd = 0, nbd_max = 0;
+      for (int s = 0; s < nb; ++s) {
+        const int mn = std::min(cps[s].m, cps[s].n), mx = std::max(cps[s].m, cps[s].n);
+        const bool bd = h->opts.svd_mode == TEBD_SVD_BIDIAG ? mn >= 2
+                        : h->opts.svd_mode == TEBD_SVD_QRJ  ? false
+                                                            : mn >= kBidiagMinDim;
+        h->path_h[s] = !bd ? kPathQRJ : (cps[s].m >= cps[s].n ? kPathBidiag : kPathBidiagT);
+        if (bd) {
+          ++nbd;
+          nbd_max = std::max(nbd_max, mx);
+        }
+      }
+      h->stats.bidiag_updates += nbd;
+      CK(cudaMemcpyAsync(h->path_d, h->path_h.data(), sizeof(int) * nb, cudaMemcpyHostToDevice,
+                         h->stream),
+         "upload SVD routes");
+      if (nbd < nb && (rc = run_qrj(h, nb, nmax))) return rc;
+      if (nbd > 0 && (rc = run_bidiag(h, nb, nbd_max))) return rc;
     }
     if ((rc = launch_dense_finish(h, nb))) return rc;
   } else {

@@ -305,13 +305,14 @@ __global__ void k_lambda(Slot *slots, const int *links, double *lam, double *tru
 
 // Keep the last spectrum and sweep count of every link for tebd_get_singular_values.
 __global__ void k_store_spectrum(Slot *slots, const int *links, const int *sweeps, double *sig_link,
-                                 int *sig_count, int *sweeps_link, int n) {
+                                 int *sig_count, int *sweeps_link, int n, const int *path) {
   const int s = blockIdx.x;
   const int link = links[s];
   for (int k = threadIdx.x; k < n; k += blockDim.x)
     sig_link[(size_t)(link - 1) * n + k] = slots[s].S[k];
   if (threadIdx.x == 0) {
-    sig_count[link - 1] = n;
+    // the bidiagonal route computes only the kept values; the Jacobi routes all of them
+    sig_count[link - 1] = path[s] != kPathQRJ ? slots[s].cp->k : n;
     sweeps_link[link - 1] = sweeps[s];
   }
 }
@@ -425,7 +426,7 @@ int launch_dense_finish(tebd_handle *h, int nb) {
   k_lambda<<<cdiv(nb, 64), 64, 0, st>>>(h->slots_d, h->links_d, h->lam, h->truncerr_d, chi, nb);
   TEBD_LAUNCHED(h);
   k_store_spectrum<<<nb, 256, 0, st>>>(h->slots_d, h->links_d, h->js.sweeps, h->sig_link_d,
-                                       h->sig_count_d, h->sweeps_link_d, n);
+                                       h->sig_count_d, h->sweeps_link_d, n, h->path_d);
   TEBD_LAUNCHED(h);
   k_restore_gamma1<<<dim3(cdiv((size_t)n * chi, 256), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
                                                                        h->slots_d, h->nrm, chi, d);
@@ -441,7 +442,7 @@ int launch_dense_finish(tebd_handle *h, int nb) {
 namespace tebd {
 
 // Largest compacted column count of the batch (sizes the Jacobi rounds).
-int dense_compact_sizes(tebd_handle *h, int nb, int *nmax) {
+int dense_compact_sizes(tebd_handle *h, int nb, int *nmax, std::vector<Compact> *out) {
   std::vector<Compact> cp(nb);
   int rc = check_cuda(h, cudaMemcpyAsync(cp.data(), h->cp_d, sizeof(Compact) * nb,
                                          cudaMemcpyDeviceToHost, h->stream),
@@ -456,6 +457,7 @@ int dense_compact_sizes(tebd_handle *h, int nb, int *nmax) {
     h->stats.compact_cols += cp[s].n;
   }
   *nmax = mx;
+  if (out) *out = cp;
   return TEBD_OK;
 }
 

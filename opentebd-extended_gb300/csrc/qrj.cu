@@ -48,10 +48,11 @@ inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 // ---------------------------------------------------------------------------
 // 1. column-pivoted Householder QR, in place on the slot's X (m x n, ld m)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kQW * 32) k_qrp(Slot *slots, const double *nrm) {
+__global__ void __launch_bounds__(kQW * 32) k_qrp(Slot *slots, const double *nrm, const int *path) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int s = blockIdx.y;
+  if (path[s] != kPathQRJ) return;  // uniform per cluster
   const Slot S = slots[s];
   const Compact cp = *S.cp;
   const int m = cp.m, n = cp.n, kmax = min(m, n);
@@ -213,8 +214,13 @@ __global__ void __launch_bounds__(kQW * 32) k_qrp(Slot *slots, const double *nrm
 // ---------------------------------------------------------------------------
 // 2. A = R^H (n x k, ld n) and Z = I (k x k, ld k); Jacobi problem of the slot
 // ---------------------------------------------------------------------------
-__global__ void k_qrj_build(Slot *slots, JacobiProblem<double> *jp, const double *nrm) {
+__global__ void k_qrj_build(Slot *slots, JacobiProblem<double> *jp, const double *nrm,
+                            const int *path) {
   const int s = blockIdx.y;
+  if (path[s] != kPathQRJ) {  // the bidiagonal route: no Jacobi problem for this slot
+    if (blockIdx.x == 0 && threadIdx.x == 0) jp[s].n = 0;
+    return;
+  }
   const Slot S = slots[s];
   const Compact cp = *S.cp;
   const int m = cp.m, n = cp.n, k = cp.k;
@@ -252,8 +258,9 @@ __global__ void k_qrj_build(Slot *slots, JacobiProblem<double> *jp, const double
 // ---------------------------------------------------------------------------
 // 3a. Y = Q [Z; 0] (m x k, ld m), one warp per column; sigma_i = |A(:,i)|
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_qrj_apply_q(Slot *slots) {
+__global__ void __launch_bounds__(256) k_qrj_apply_q(Slot *slots, const int *path) {
   const int s = blockIdx.y;
+  if (path[s] != kPathQRJ) return;
   const Slot S = slots[s];
   const Compact cp = *S.cp;
   const int m = cp.m, n = cp.n, k = cp.k;
@@ -297,8 +304,9 @@ __global__ void __launch_bounds__(256) k_qrj_apply_q(Slot *slots) {
 
 // 3b. X(:, i) = Y(:, i) sigma_i  (= U Sigma, what the sort/restore kernels read)
 //     V(jpvt(c), i) = A(c, i) / sigma_i (= P W)
-__global__ void k_qrj_store(Slot *slots) {
+__global__ void k_qrj_store(Slot *slots, const int *path) {
   const int s = blockIdx.y;
+  if (path[s] != kPathQRJ) return;
   const Slot S = slots[s];
   const Compact cp = *S.cp;
   const int m = cp.m, n = cp.n, k = cp.k;
@@ -348,7 +356,8 @@ int run_qrj(tebd_handle *h, int nb, int nmax) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     if (h->profiling) cudaEventRecord(h->ev[0], st);
-    rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_qrp, h->slots_d, (const double *)h->nrm), "QR launch");
+    rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_qrp, h->slots_d, (const double *)h->nrm,
+                                          (const int *)h->path_d), "QR launch");
     if (rc) return rc;
     TEBD_LAUNCHED(h);
     if (h->profiling) cudaEventRecord(h->ev[1], st);
@@ -367,6 +376,7 @@ int run_qrj(tebd_handle *h, int nb, int nmax) {
   int kmax = 0;
   size_t maxnk = 1, maxmk = 1;
   for (int s = 0; s < nb; ++s) {
+    if (h->path_h[s] != kPathQRJ) continue;
     const double m = cp[s].m, n = cp[s].n, k = cp[s].k;
     kmax = std::max(kmax, cp[s].k);
     maxnk = std::max(maxnk, (size_t)(n * k + k * k));
@@ -380,18 +390,18 @@ int run_qrj(tebd_handle *h, int nb, int nmax) {
   JacobiProblem<double> *jp = reinterpret_cast<JacobiProblem<double> *>(h->jprob_d);
   unsigned gx = cdiv(maxnk, 256);
   if (gx > 512) gx = 512;
-  k_qrj_build<<<dim3(gx, nb), 256, 0, st>>>(h->slots_d, jp, h->nrm);
+  k_qrj_build<<<dim3(gx, nb), 256, 0, st>>>(h->slots_d, jp, h->nrm, h->path_d);
   TEBD_LAUNCHED(h);
   const double tol = h->opts.jacobi_tol > 0 ? h->opts.jacobi_tol
                                             : (double)(kmax > 16 ? kmax : 16) * 2.220446049250313e-16;
   const int cap = h->opts.max_sweeps > 0 ? h->opts.max_sweeps : 60;
   if ((rc = jacobi_persistent_double(h, jp, nb, kmax, tol, cap))) return rc;
   // 3. U and V
-  k_qrj_apply_q<<<dim3(cdiv(kmax > 0 ? kmax : 1, 8), nb), 256, 0, st>>>(h->slots_d);
+  k_qrj_apply_q<<<dim3(cdiv(kmax > 0 ? kmax : 1, 8), nb), 256, 0, st>>>(h->slots_d, h->path_d);
   TEBD_LAUNCHED(h);
   gx = cdiv(maxmk, 256);
   if (gx > 512) gx = 512;
-  k_qrj_store<<<dim3(gx, nb), 256, 0, st>>>(h->slots_d);
+  k_qrj_store<<<dim3(gx, nb), 256, 0, st>>>(h->slots_d, h->path_d);
   TEBD_LAUNCHED(h);
   return check_cuda(h, cudaGetLastError(), "QRJ launch");
 }

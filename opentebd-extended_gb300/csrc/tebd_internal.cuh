@@ -107,8 +107,17 @@ struct Slot {
   int *jpvt;                // n column permutation of the pivoted QR
   double2 *tau;             // n reflector scalars
   double *vn;               // 2n partial column norms (later: the k singular values)
-  double2 *aux;             // 3 n^2: A = R^H (n x k), Z (k x k), Y = Q [Z; 0] (m x k)
+  double2 *aux;             // 3 n^2: A = R^H (n x k), Z (k x k), Y = Q [Z; 0] (m x k);
+                            // bidiagonal path: right reflectors (n x n), partial sums
+  double2 *taup;            // n right-reflector scalars (bidiagonal path)
+  double *bdws;             // bidiagonal path: d, e, sigma, inverse-iteration scratch, Z, U
 };
+
+// SVD route of one bond of a dense batch
+constexpr int kPathQRJ = 0;      // pivoted QR + one-sided Jacobi on R^H (qrj.cu)
+constexpr int kPathBidiag = 1;   // bidiagonalisation + bisection + inverse iteration (bidiag.cu)
+constexpr int kPathBidiagT = 2;  // the same on Theta^H, for a wide compacted Theta (m < n)
+constexpr int kBidiagMinDim = 256;  // default route switch: min(m, n) of the compacted Theta
 
 }  // namespace tebd
 
@@ -129,6 +138,8 @@ struct tebd_handle {
   size_t ws_bytes;
   double2 *gates_d;               // nslots * d^4 gates of the current batch
   tebd::Compact *cp_d;            // nslots compaction records
+  int *path_d;                    // nslots SVD route per slot (kPathQRJ / kPathBidiag)
+  std::vector<int> path_h;        // host copy of the current batch's routes
   int *idx_d;                     // nslots * 5 * chi index maps
   double *nrm_part;       // nslots * kNormParts partial sums of |Theta|^2
   double *nrm;            // nslots Frobenius norms
@@ -165,13 +176,15 @@ int check_cuda(tebd_handle *h, cudaError_t e, const char *what);
 // kernels launched from capi.cu (defined in the .cu files)
 int launch_dense_prepare(tebd_handle *h, int nb, bool real_gate);
 int run_jacobi(tebd_handle *h, int nb, int svd_mode, int nmax);
-int dense_compact_sizes(tebd_handle *h, int nb, int *nmax);
+int dense_compact_sizes(tebd_handle *h, int nb, int *nmax, std::vector<Compact> *out);
 int launch_dense_finish(tebd_handle *h, int nb);
 int launch_eye(tebd_handle *h, int nb);
 int run_jacobi_problems(tebd_handle *h, const JacobiProblem<double> *probs_d, int nprob, int nmax);
 int jacobi_persistent_double(tebd_handle *h, const JacobiProblem<double> *probs_d, int nprob,
                              int nmax, double tol, int max_sweeps);
 int run_qrj(tebd_handle *h, int nb, int nmax);
+int run_bidiag(tebd_handle *h, int nb, int nmax);
+size_t bidiag_ws_doubles(int n, int chi);
 int jacobi_collect(tebd_handle *h);
 int measure_fp64_peak(int device, double *tflops);
 int run_nc_batch(tebd_handle *h, int nb, const int *links_host, double *truncerr_host);

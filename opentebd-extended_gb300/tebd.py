@@ -41,6 +41,8 @@ MODE_DENSE = 0
 MODE_NC = 1
 SVD_FP64 = 0
 SVD_JACOBI = 2
+SVD_BIDIAG = 3
+SVD_QRJ = 4
 OPTS_VERSION = 1
 
 ERROR_NAMES = {
@@ -103,6 +105,8 @@ class Stats(ctypes.Structure):
         ("qr_flops", ctypes.c_double),
         ("qr_ms", ctypes.c_double),
         ("rank_sum", ctypes.c_longlong),
+        ("bidiag_ms", ctypes.c_double),
+        ("bidiag_updates", ctypes.c_longlong),
     ]
 
     def as_dict(self):

@@ -20,7 +20,11 @@ SIG_REL, SIG_ABS = 1e-12, 1e-13
 
 
 def sigma_ok(s_gpu, s_ref):
+    """The bidiagonal route reports only the chi values it keeps, the Jacobi routes
+    all d*chi: compare the leading len(s_gpu) values."""
     s_gpu, s_ref = np.asarray(s_gpu), np.asarray(s_ref)
+    assert 1 <= len(s_gpu) <= len(s_ref)
+    s_ref = s_ref[:len(s_gpu)]
     tol = SIG_REL * s_ref + SIG_ABS * max(s_ref[0], 1e-300)
     return np.all(np.abs(s_gpu - s_ref) <= tol), np.max(np.abs(s_gpu - s_ref) - tol)
 
@@ -40,10 +44,11 @@ def random_unitary(n, rng):
     return q * (np.diag(r) / np.abs(np.diag(r)))
 
 
-@pytest.mark.parametrize("svd_mode", [0, 2])
+@pytest.mark.parametrize("svd_mode", [0, 2, 3, 4])
 @pytest.mark.parametrize("chi,d", [(1, 2), (8, 2), (16, 3), (12, 5), (32, 4)])
 def test_single_update_matches_oracle(pkg, oracle, chi, d, svd_mode):
-    """Both SVD algorithms: pivoted QR + Jacobi on R^H (0, default) and plain Jacobi (2)."""
+    """Every SVD route: default per-bond choice (0), plain Jacobi (2), bidiagonalisation
+    with bisection and inverse iteration (3), pivoted QR + Jacobi on R^H (4)."""
     gam, lam = random_bond(chi, d, 100 + chi + d)
     U = random_unitary(d * d, np.random.default_rng(chi * d))
     with pkg.Chain(4, d, chi, svd_mode=svd_mode) as c:
@@ -79,7 +84,8 @@ def test_real_gate_and_edges(pkg, oracle):
             assert np.allclose(c.get_lambda(link + 1), rl1, atol=1e-11)
 
 
-def test_rank_deficient_product_state(pkg, oracle):
+@pytest.mark.parametrize("svd_mode", [0, 3])
+def test_rank_deficient_product_state(pkg, oracle, svd_mode):
     """Product state, product gate: one singular value 1, all others exactly 0."""
     H = pkg.hamiltonians
     rng = np.random.default_rng(2)
@@ -88,7 +94,7 @@ def test_rank_deficient_product_state(pkg, oracle):
     c0 /= np.linalg.norm(c0, axis=0)
     gam, lam = H.product_state(c0, chi)
     U = np.kron(random_unitary(d, rng), random_unitary(d, rng))
-    with pkg.Chain(L, d, chi) as c:
+    with pkg.Chain(L, d, chi, svd_mode=svd_mode) as c:
         c.set_state(gam, lam)
         te = c.two_site_op(2, U)
         s = c.singular_values(2)
@@ -97,19 +103,22 @@ def test_rank_deficient_product_state(pkg, oracle):
         assert np.allclose(c.get_lambda(3), np.eye(chi)[0], atol=1e-14)
 
 
-@pytest.mark.parametrize("chi,d", [(9, 3), (40, 2)])
-def test_exact_zero_lambdas_anywhere(pkg, oracle, chi, d):
+@pytest.mark.parametrize("svd_mode", [0, 3])
+@pytest.mark.parametrize("chi,d,fracs", [(9, 3, (0.5, 0.3, 0.7)), (40, 2, (0.5, 0.3, 0.7)),
+                                         (40, 2, (0.2, 0.3, 0.6))])
+def test_exact_zero_lambdas_anywhere(pkg, oracle, chi, d, fracs, svd_mode):
     """Rows/columns of exactly-zero Lambdas are dropped from the SVD; zeros at
     interior positions and differing counts on the three links must give the
-    reference's Lambdas and Gammas' physics."""
+    reference's Lambdas and Gammas' physics.  The compacted Theta is wide in the
+    first two cases (the bidiagonal mode works on Theta^H) and tall in the last."""
     gam, lam = random_bond(chi, d, 31 + chi)
     rng = np.random.default_rng(chi)
-    for l, frac in zip(lam[1:4], (0.5, 0.3, 0.7)):
+    for l, frac in zip(lam[1:4], fracs):
         l[rng.random(chi) < frac] = 0.0
         l[0] = max(l[0], 0.1)
         l /= np.linalg.norm(l)
     U = random_unitary(d * d, rng)
-    with pkg.Chain(4, d, chi) as c:
+    with pkg.Chain(4, d, chi, svd_mode=svd_mode) as c:
         c.set_state(gam, lam)
         te = c.two_site_op(2, U)
         s = c.singular_values(2)
@@ -143,8 +152,9 @@ def test_golden_reference_propagators(pkg):
             assert abs(te - float(z["truncerr_" + key])) < 1e-11
 
 
+@pytest.mark.parametrize("svd_mode", [0, 3])
 @pytest.mark.parametrize("order", [2, 5])
-def test_trotter_steps_match_oracle(pkg, oracle, order):
+def test_trotter_steps_match_oracle(pkg, oracle, order, svd_mode):
     """Full sweeps (batched same-parity bonds on the GPU vs sequential bonds in the
     oracle) on a Heisenberg chain; compares every Lambda, <Sz>, bond energies and
     the overlap of the two states."""
@@ -156,7 +166,7 @@ def test_trotter_steps_match_oracle(pkg, oracle, order):
     gam, lam = H.product_state(c0, chi)
     Hb = H.heisenberg(L, 1.0, 1.0, 0.5)
     U = H.construct_propagators(Hb, 0.1, order)
-    with pkg.Chain(L, d, chi) as c:
+    with pkg.Chain(L, d, chi, svd_mode=svd_mode) as c:
         c.set_state(gam, lam)
         for _ in range(3):
             te = c.trotter_step(U, order)
@@ -171,25 +181,35 @@ def test_trotter_steps_match_oracle(pkg, oracle, order):
     assert abs(abs(obs.inner_product(gam, lam, g_gpu, l_gpu)) - 1.0) < 1e-10
 
 
-def test_bose_hubbard_full_size_single_bond(pkg, oracle):
+@pytest.mark.parametrize("svd_mode,drop", [(0, None), (4, None), (0, "left"), (0, "right")])
+def test_bose_hubbard_full_size_single_bond(pkg, oracle, svd_mode, drop):
     """Bond of the d=5, chi=128 Bose-Hubbard workload (n = 640) against LAPACK, plus
     size-independent properties: sum lambda^2 = 1, truncerr = 1 - sum of kept S^2,
-    and left/right canonical conditions of the new Gammas."""
+    and left/right canonical conditions of the new Gammas.  The default route takes
+    the bidiagonal path here (640 columns); mode 4 forces QR + Jacobi.  Three exact
+    zeros in the left (right) Lambda make the compacted Theta 625 x 640 (640 x 625):
+    the wide one is bidiagonalised as Theta^H."""
     chi, d = 128, 5
     gam, lam = random_bond(chi, d, 77)
     for l in lam:
         l[:] = np.exp(-np.arange(chi) / 16.0)
         l /= np.linalg.norm(l)
+    if drop is not None:
+        l = lam[1] if drop == "left" else lam[3]
+        l[[5, 40, 90]] = 0.0
+        l /= np.linalg.norm(l)
     Hb = pkg.hamiltonians.bose_hubbard(4, d, 1.0, 2.0)
     U = pkg.hamiltonians.matrix_exponential(Hb[1], 0.005)
-    with pkg.Chain(4, d, chi) as c:
+    with pkg.Chain(4, d, chi, svd_mode=svd_mode) as c:
         c.set_state(gam, lam)
         te = c.two_site_op(2, U)
         s = c.singular_values(2)
         g1, g2, l1 = c.get_gamma(2), c.get_gamma(3), c.get_lambda(3)
+        assert c.stats()["bidiag_updates"] == (1 if svd_mode == 0 else 0)
     rg1, rg2, rl1, rte, rs = oracle.two_site_op(gam[1], gam[2], lam[1], lam[2], lam[3], U)
     ok, worst = sigma_ok(s, rs)
     assert ok, worst
+    assert len(s) >= chi
     assert np.allclose(l1, rl1, atol=1e-11)
     assert abs(te - rte) < 1e-11
     assert abs(np.sum(l1 ** 2) - 1) < 1e-12
