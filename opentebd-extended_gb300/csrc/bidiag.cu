@@ -36,7 +36,6 @@ namespace tebd {
 
 namespace {
 constexpr int kBW = 16;   // warps per CTA of the bidiagonalisation kernel
-constexpr int kCC = 64;   // column chunk of the right-reflector update
 
 __device__ __forceinline__ double bsum(double v) {
 #pragma unroll
@@ -62,45 +61,126 @@ __host__ __device__ __forceinline__ size_t bd_scratch(int n, int kk) {
   return ((size_t)2 * n + kk + 1) & ~(size_t)1;
 }
 
-// ZLARFG on (alpha, x[0..len)) with x strided; one warp.  Returns beta in *beta,
-// tau in *tau and scales x in place (x <- x / (alpha - beta)).
-__device__ void warp_larfg(double2 alpha, double2 *x, size_t stride, int len, int lane,
-                           double *beta_out, double2 *tau_out, bool conj_in, bool conj_out) {
-  double acc = 0.0;
-  for (int r = lane; r < len; r += 32) {
-    const double2 v = __ldcg(x + (size_t)r * stride);
-    acc = fma(v.x, v.x, fma(v.y, v.y, acc));
-  }
-  const double xnorm = sqrt(bsum(acc));
-  if (xnorm == 0.0 && alpha.y == 0.0) {
-    *beta_out = alpha.x;
-    *tau_out = make_double2(0.0, 0.0);
-    if (conj_in != conj_out)
-      for (int r = lane; r < len; r += 32) {
-        const double2 v = __ldcg(x + (size_t)r * stride);
-        x[(size_t)r * stride] = make_double2(v.x, -v.y);
-      }
-    return;
-  }
-  const double beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm), alpha.x);
-  const double2 tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-  const double dr = alpha.x - beta, di = alpha.y, den = dr * dr + di * di;
-  const double2 sc = make_double2(dr / den, -di / den);
-  for (int r = lane; r < len; r += 32) {
-    double2 v = __ldcg(x + (size_t)r * stride);
-    if (conj_in) v.y = -v.y;
-    double2 o = make_double2(v.x * sc.x - v.y * sc.y, v.x * sc.y + v.y * sc.x);
-    if (conj_out) o.y = -o.y;
-    x[(size_t)r * stride] = o;
-  }
-  *beta_out = beta;
-  *tau_out = tau;
-}
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// 1. Householder bidiagonalisation, in place on X (m x n, ld m), m >= n.
+// 1. Householder bidiagonalisation of the M x N matrix in S.X (ld M), M >= N,
+//    in panels of kPanel columns (the delayed-update scheme of LAPACK's ZGEBRD /
+//    ZLABRD).  Inside a panel the trailing matrix keeps its panel-start values A0
+//    and the current matrix is A0 - V Y^H - Xp U^H, with v_k, u_k the panel's
+//    left/right reflectors, y_k = tauq_k A^H v_k and x_k = taup_k A u_k.  Each
+//    column costs two read-only passes over A0 (z = A0^H v, w = A0 u) plus
+//    rank-2j corrections; at the panel end A0 <- A0 - V Y^H - Xp U^H.
+//    One cluster per bond, four cluster barriers per column:
+//      S1  column i corrected and its norm partials posted
+//      S2  z = A0^H v and the small dots V^H v, Xp^H v posted
+//      S3  y_i and row i corrected, row-norm partials posted, v_i stored
+//      S4  w = A0 u by column chunks, Y^H u and U^H u posted, u_i stored
+//    Every CTA recomputes the reflector scalars from the posted partial norms
+//    (same values, same order), so no barrier waits on a single CTA's scalar work.
+//    Output (as ZGEBD2): d, e in bdws; tauq in S.tau, v_i below the diagonal of
+//    column i; taup in S.taup, u_i in column i of Pv with u_i(i+1) = 1.
 // ---------------------------------------------------------------------------
+constexpr int kPanel = 32;  // columns per panel
+constexpr int kChunk = 32;  // columns per task of the w = A0 u pass
+constexpr int kTile = 64;   // trailing-update tile (rows and columns)
+constexpr int kKc = 16;     // trailing-update k chunk staged in shared memory
+constexpr int kS = kTile + 8;  // staging stride (doubles): a fragment load is two wavefronts
+constexpr size_t kStageDoubles = 4 * (size_t)kKc * kS;
+
+// D += A B on the FP64 tensor pipe: mma m8n8k4, one A element (row lane/4, col lane%4),
+// one B element (row lane%4, col lane/4), two D elements (row lane/4, cols 2(lane%4)+{0,1})
+__device__ __forceinline__ void dmma(double &d0, double &d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+
+struct BdAux {
+  double2 *Pv, *Yb, *Xb, *zb, *s1, *s2, *t1, *t2, *part;
+  double *nrmL, *nrmR;
+};
+
+__host__ __device__ __forceinline__ size_t bd_aux_elems(int M, int N) {
+  const int P = N < kPanel ? N : kPanel;
+  return (size_t)N * N + (size_t)(N + M) * P + N + 4 * (size_t)P +
+         (size_t)((N + kChunk - 1) / kChunk) * M + 16;
+}
+
+__device__ __forceinline__ BdAux bd_aux(double2 *aux, int M, int N) {
+  const int P = min(kPanel, N);
+  BdAux a;
+  size_t o = 0;
+  a.Pv = aux;
+  o += (size_t)N * N;
+  a.Yb = aux + o;  // N x P, ld N
+  o += (size_t)N * P;
+  a.Xb = aux + o;  // M x P, ld M
+  o += (size_t)M * P;
+  a.zb = aux + o;
+  o += N;
+  a.s1 = aux + o;
+  a.s2 = a.s1 + P;
+  a.t1 = a.s2 + P;
+  a.t2 = a.t1 + P;
+  o += 4 * (size_t)P;
+  a.part = aux + o;  // ceil(N / kChunk) x M
+  o += (size_t)((N + kChunk - 1) / kChunk) * M;
+  a.nrmL = reinterpret_cast<double *>(aux + o);  // 8 per-CTA partial norms each
+  a.nrmR = a.nrmL + 8;
+  return a;
+}
+
+__device__ __forceinline__ double2 ldc(const double2 *p) { return __ldcg(p); }
+
+// acc += conj(a) b
+__device__ __forceinline__ void mac_ca(double2 &acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, fma(a.y, b.y, acc.x));
+  acc.y = fma(a.x, b.y, fma(-a.y, b.x, acc.y));
+}
+// acc += a b
+__device__ __forceinline__ void mac(double2 &acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
+  acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
+}
+// acc -= a b
+__device__ __forceinline__ void msub(double2 &acc, double2 a, double2 b) {
+  acc.x = fma(-a.x, b.x, fma(a.y, b.y, acc.x));
+  acc.y = fma(-a.x, b.y, fma(-a.y, b.x, acc.y));
+}
+// acc -= a conj(b)
+__device__ __forceinline__ void msub_cb(double2 &acc, double2 a, double2 b) {
+  acc.x = fma(-a.x, b.x, fma(-a.y, b.y, acc.x));
+  acc.y = fma(a.x, b.y, fma(-a.y, b.x, acc.y));
+}
+
+// ZLARFG's scalars from alpha and ||x||^2: beta (real), tau, and 1/(alpha - beta),
+// the factor that turns x into the reflector's tail.
+__device__ void larfg_scalars(double2 alpha, double xn2, double &beta, double2 &tau, double2 &sc) {
+  if (xn2 == 0.0 && alpha.y == 0.0) {  // H = I, x left as it is
+    beta = alpha.x;
+    tau = make_double2(0.0, 0.0);
+    sc = make_double2(1.0, 0.0);
+    return;
+  }
+  beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+  tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+  const double dr = alpha.x - beta, di = alpha.y, den = dr * dr + di * di;
+  sc = make_double2(dr / den, -di / den);
+}
+
+// CTA-wide sum, valid in every thread
+__device__ double block_sum(double v, double *red) {
+  v = bsum(v);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+  return t;
+}
+
 __global__ void __launch_bounds__(kBW * 32) k_gebrd(Slot *slots, const int *path) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
@@ -108,165 +188,424 @@ __global__ void __launch_bounds__(kBW * 32) k_gebrd(Slot *slots, const int *path
   const int route = path[s];
   if (!on_route(route)) return;  // uniform per cluster
   const Slot S = slots[s];
-  int m, n;
-  bd_dims(*S.cp, route, m, n);
-  double2 *X = S.X;
-  double *dd = S.bdws, *ee = S.bdws + n;
-  double2 *Pv = S.aux;                        // n x n: right reflector vectors by column
-  double2 *part = S.aux + (size_t)n * n;      // column-chunk partial sums (<= n/kCC+1) x m
-  const int crank = (int)cluster.block_rank(), C = (int)cluster.num_blocks();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int gw = crank * kBW + warp, nw = C * kBW;
-  for (int i = 0; i < n; ++i) {
-    // (a) left reflector on column i, rows i..m-1
-    if (crank == 0 && warp == 0) {
+  int M, N;
+  bd_dims(*S.cp, route, M, N);
+  double2 *A = S.X;
+  double *dd = S.bdws, *ee = S.bdws + N;
+  const BdAux ax = bd_aux(S.aux, M, N);
+  const int C = (int)cluster.num_blocks(), crank = (int)cluster.block_rank();
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int gt = crank * nthr + tid, gthr = C * nthr;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int gw = crank * (nthr >> 5) + warp, nw = C * (nthr >> 5);
+  extern __shared__ double2 sh[];
+  double2 *vec = sh;                    // max(M, N): v or u of the current column
+  double2 *sm = sh + max(M, N);         // 4 kPanel small per-column vectors
+  double *stg = reinterpret_cast<double *>(sm + 4 * kPanel);  // trailing-update staging
+  __shared__ double red[32];
+#define AE(r, c) A[(size_t)(r) + (size_t)M * (c)]
+#define YB(c, k) ax.Yb[(size_t)(c) + (size_t)N * (k)]
+#define XB(r, k) ax.Xb[(size_t)(r) + (size_t)M * (k)]
+#define PV(c, k) ax.Pv[(size_t)(c) + (size_t)N * (k)]
+  {  // norm partials of column 0 below the diagonal
+    double acc = 0.0;
+    for (int r = 1 + gt; r < M; r += gthr) {
+      const double2 a = ldc(&AE(r, 0));
+      acc = fma(a.x, a.x, fma(a.y, a.y, acc));
+    }
+    acc = block_sum(acc, red);
+    if (tid == 0) ax.nrmL[crank] = acc;
+  }
+  cluster.sync();
+  for (int p = 0; p < N; p += kPanel) {
+    const int jb = min(kPanel, N - p);
+    for (int j = 0; j < jb; ++j) {
+      const int i = p + j;
+      // ---- left reflector of column i (every CTA, identical inputs) ----
       double beta;
-      double2 tau;
-      const double2 alpha = __ldcg(X + i + (size_t)m * i);
-      warp_larfg(alpha, X + (i + 1) + (size_t)m * i, 1, m - i - 1, lane, &beta, &tau, false, false);
-      if (lane == 0) {
+      double2 tau, sc;
+      {
+        double xn2 = 0.0;
+        for (int q = 0; q < C; ++q) xn2 += __ldcg(&ax.nrmL[q]);
+        larfg_scalars(ldc(&AE(i, i)), xn2, beta, tau, sc);
+      }
+      if (crank == 0 && tid == 0) {
         dd[i] = beta;
         S.tau[i] = tau;
-        X[i + (size_t)m * i] = make_double2(beta, 0.0);
+      }
+      if (i == N - 1) {  // last column: left reflector only
+        for (int r = i + 1 + gt; r < M; r += gthr) AE(r, i) = cmul(ldc(&AE(r, i)), sc);
+        break;
+      }
+      // ---- S2: z = A0(i:M, i+1:N)^H v, s1 = V^H v, s2 = Xp^H v ----
+      for (int r = i + tid; r < M; r += nthr)
+        vec[r - i] = r == i ? make_double2(1.0, 0.0) : cmul(ldc(&AE(r, i)), sc);
+      __syncthreads();
+      {
+        const int ncol = N - i - 1, items = ncol + 2 * j;
+        for (int it = gw; it < items; it += nw) {
+          const double2 *col = it < ncol       ? &AE(0, i + 1 + it)
+                               : it < ncol + j ? &AE(0, p + (it - ncol))
+                                               : &XB(0, it - ncol - j);
+          double2 acc = make_double2(0.0, 0.0);  // sum_r conj(col(r)) v(r)
+          int r = i + lane;
+          for (; r + 224 < M; r += 256) {
+            double2 c[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) c[q] = ldc(col + r + 32 * q);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) mac_ca(acc, c[q], vec[r + 32 * q - i]);
+          }
+          for (; r < M; r += 32) mac_ca(acc, ldc(col + r), vec[r - i]);
+          acc.x = bsum(acc.x);
+          acc.y = bsum(acc.y);
+          if (lane == 0) {
+            if (it < ncol)
+              ax.zb[i + 1 + it] = acc;
+            else if (it < ncol + j)
+              ax.s1[it - ncol] = acc;
+            else
+              ax.s2[it - ncol - j] = acc;
+          }
+        }
+      }
+      cluster.sync();
+      // ---- S3: y_i = tauq (z - Y s1 - U s2); row i of the current matrix ----
+      if (tid < j) {
+        sm[tid] = ldc(&ax.s1[tid]);
+        sm[kPanel + tid] = ldc(&ax.s2[tid]);
+        sm[2 * kPanel + tid] = ldc(&AE(i, p + tid));  // v_k(i)
+        sm[3 * kPanel + tid] = ldc(&XB(i, tid));      // x_k(i)
+      }
+      __syncthreads();
+      {
+        double acc = 0.0;
+        for (int c = i + 1 + gt; c < N; c += gthr) {
+          double2 y = ldc(&ax.zb[c]);
+          double2 rr = ldc(&AE(i, c));
+          for (int k = 0; k < j; ++k) {
+            const double2 yk = ldc(&YB(c, k)), uk = ldc(&PV(c, p + k));
+            msub(y, yk, sm[k]);
+            msub(y, uk, sm[kPanel + k]);
+            msub_cb(rr, sm[2 * kPanel + k], yk);
+            msub_cb(rr, sm[3 * kPanel + k], uk);
+          }
+          y = cmul(tau, y);
+          YB(c, j) = y;
+          rr.x -= y.x;  // v_i(i) = 1: rr -= conj(y)
+          rr.y += y.y;
+          AE(i, c) = rr;
+          if (c >= i + 2) acc = fma(rr.x, rr.x, fma(rr.y, rr.y, acc));
+        }
+        acc = block_sum(acc, red);
+        if (tid == 0) ax.nrmR[crank] = acc;
+      }
+      for (int r = i + 1 + gt; r < M; r += gthr) AE(r, i) = cmul(ldc(&AE(r, i)), sc);  // v_i
+      cluster.sync();
+      // ---- right reflector of row i (every CTA) ----
+      double beta2;
+      double2 tau2, sc2;
+      {
+        double xn2 = 0.0;
+        for (int q = 0; q < C; ++q) xn2 += __ldcg(&ax.nrmR[q]);
+        larfg_scalars(cconj(ldc(&AE(i, i + 1))), xn2, beta2, tau2, sc2);
+      }
+      if (crank == 0 && tid == 0) {
+        ee[i] = beta2;
+        S.taup[i] = tau2;
+      }
+      // ---- S4: w = A0(i+1:M, i+1:N) u by column chunks, t1 = Y^H u, t2 = U^H u ----
+      for (int c = i + 1 + tid; c < N; c += nthr)
+        vec[c - i - 1] = c == i + 1 ? make_double2(1.0, 0.0) : cmul(cconj(ldc(&AE(i, c))), sc2);
+      __syncthreads();
+      {
+        const int rows = M - i - 1, cols = N - i - 1;
+        const int nrb = (rows + 31) / 32, ncc = (cols + kChunk - 1) / kChunk;
+        const int tasks = nrb * ncc, items = tasks + 2 * j + 1;
+        for (int it = gw; it < items; it += nw) {
+          if (it < tasks) {
+            const int rb = it % nrb, cc = it / nrb;
+            const int r = i + 1 + rb * 32 + lane;
+            const int c0 = i + 1 + cc * kChunk, c1 = min(N, c0 + kChunk);
+            if (r < M) {
+              double2 acc = make_double2(0.0, 0.0);
+              const double2 *rp = &AE(r, 0);
+              int c = c0;
+              for (; c + 7 < c1; c += 8) {
+                double2 a[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) a[q] = ldc(rp + (size_t)M * (c + q));
+#pragma unroll
+                for (int q = 0; q < 8; ++q) mac(acc, a[q], vec[c + q - i - 1]);
+              }
+              for (; c < c1; ++c) mac(acc, ldc(rp + (size_t)M * c), vec[c - i - 1]);
+              ax.part[(size_t)cc * M + r] = acc;
+            }
+          } else {
+            const int k = it - tasks;  // 0..j: t1 over y_k; j+1..2j: t2 over u_(k-j-1)
+            const double2 *cp = k <= j ? &YB(0, k) : &PV(0, p + k - j - 1);
+            double2 acc = make_double2(0.0, 0.0);
+            for (int c = i + 1 + lane; c < N; c += 32) mac_ca(acc, ldc(cp + c), vec[c - i - 1]);
+            acc.x = bsum(acc.x);
+            acc.y = bsum(acc.y);
+            if (lane == 0) {
+              if (k <= j)
+                ax.t1[k] = acc;
+              else
+                ax.t2[k - j - 1] = acc;
+            }
+          }
+        }
+        for (int c = i + 1 + gt; c < N; c += gthr) PV(c, i) = vec[c - i - 1];  // u_i
+      }
+      cluster.sync();
+      // ---- x_i = taup (w - V t1 - Xp t2); then column i+1 of the current matrix ----
+      const bool next_in_panel = j + 1 < jb;
+      if (tid <= j) {
+        sm[tid] = ldc(&ax.t1[tid]);
+        if (tid < j) sm[kPanel + tid] = ldc(&ax.t2[tid]);
+        if (next_in_panel) {
+          sm[2 * kPanel + tid] = ldc(&YB(i + 1, tid));      // y_k(i+1)
+          sm[3 * kPanel + tid] = ldc(&PV(i + 1, p + tid));  // u_k(i+1)
+        }
+      }
+      __syncthreads();
+      {
+        const int ncc = (N - i - 1 + kChunk - 1) / kChunk;
+        double acc = 0.0;
+        for (int r = i + 1 + gt; r < M; r += gthr) {
+          double2 w = make_double2(0.0, 0.0);
+          for (int q = 0; q < ncc; ++q) {  // fixed order
+            const double2 t = ldc(&ax.part[(size_t)q * M + r]);
+            w.x += t.x;
+            w.y += t.y;
+          }
+          for (int k = 0; k <= j; ++k) msub(w, ldc(&AE(r, p + k)), sm[k]);
+          for (int k = 0; k < j; ++k) msub(w, ldc(&XB(r, k)), sm[kPanel + k]);
+          const double2 x = cmul(tau2, w);
+          XB(r, j) = x;
+          if (next_in_panel) {
+            double2 a = ldc(&AE(r, i + 1));
+            for (int k = 0; k <= j; ++k) {
+              msub_cb(a, ldc(&AE(r, p + k)), sm[2 * kPanel + k]);
+              msub_cb(a, k < j ? ldc(&XB(r, k)) : x, sm[3 * kPanel + k]);
+            }
+            AE(r, i + 1) = a;
+            if (r >= i + 2) acc = fma(a.x, a.x, fma(a.y, a.y, acc));
+          }
+        }
+        if (next_in_panel) {
+          acc = block_sum(acc, red);
+          if (tid == 0) ax.nrmL[crank] = acc;
+        }
+      }
+      cluster.sync();
+    }
+    const int q = p + jb;
+    if (q >= N) break;
+    // ---- panel end: A0(q:M, q:N) -= V Y^H + Xp U^H (inner dimension 2 jb) ----
+    // 64 x 64 tiles over the cluster's CTAs; each warp owns a 16 x 16 block and
+    // accumulates its real and imaginary parts with four real DMMAs per k-step:
+    //   Re -= Lr Rr^T + Li Ri^T,  Im -= Li Rr^T - Lr Ri^T   (L = [V Xp], R = [Y U])
+    {
+      const int K2 = 2 * jb;
+      const int ntr = (M - q + kTile - 1) / kTile, ntc = (N - q + kTile - 1) / kTile;
+      double *Lr = stg, *Li = stg + kKc * kS, *Rr = stg + 2 * kKc * kS, *Ri = stg + 3 * kKc * kS;
+      const int wr = (warp & 3) * 16, wc = (warp >> 2) * 16;
+      const int fr = lane >> 2, fk = lane & 3;
+      for (int t = crank; t < ntr * ntc; t += C) {
+        const int r0 = q + (t % ntr) * kTile, c0 = q + (t / ntr) * kTile;
+        double cr[2][2][2], ci[2][2][2];
+#pragma unroll
+        for (int x = 0; x < 2; ++x)
+#pragma unroll
+          for (int y = 0; y < 2; ++y)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) cr[x][y][e] = ci[x][y][e] = 0.0;
+        for (int kc = 0; kc < K2; kc += kKc) {
+          __syncthreads();
+          for (int e = tid; e < kKc * kTile; e += nthr) {
+            const int rr = e % kTile, kk = e / kTile, k = kc + kk;
+            const int r = r0 + rr, c = c0 + rr;
+            double2 l = make_double2(0.0, 0.0), g = make_double2(0.0, 0.0);
+            if (k < K2) {
+              if (r < M) l = k < jb ? ldc(&AE(r, p + k)) : ldc(&XB(r, k - jb));
+              if (c < N) g = k < jb ? ldc(&YB(c, k)) : ldc(&PV(c, p + k - jb));
+            }
+            Lr[kk * kS + rr] = l.x;
+            Li[kk * kS + rr] = l.y;
+            Rr[kk * kS + rr] = g.x;
+            Ri[kk * kS + rr] = g.y;
+          }
+          __syncthreads();
+#pragma unroll
+          for (int ks = 0; ks < kKc; ks += 4) {
+            const int ko = (ks + fk) * kS;
+            double ar[2], ai[2], br[2], bi[2];
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+              ar[b] = Lr[ko + wr + 8 * b + fr];
+              ai[b] = Li[ko + wr + 8 * b + fr];
+              br[b] = Rr[ko + wc + 8 * b + fr];
+              bi[b] = Ri[ko + wc + 8 * b + fr];
+            }
+#pragma unroll
+            for (int x = 0; x < 2; ++x)
+#pragma unroll
+              for (int y = 0; y < 2; ++y) {
+                dmma(cr[x][y][0], cr[x][y][1], -ar[x], br[y]);
+                dmma(cr[x][y][0], cr[x][y][1], -ai[x], bi[y]);
+                dmma(ci[x][y][0], ci[x][y][1], -ai[x], br[y]);
+                dmma(ci[x][y][0], ci[x][y][1], ar[x], bi[y]);
+              }
+          }
+        }
+#pragma unroll
+        for (int x = 0; x < 2; ++x) {
+          const int r = r0 + wr + 8 * x + fr;
+          if (r >= M) continue;
+#pragma unroll
+          for (int y = 0; y < 2; ++y)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+              const int c = c0 + wc + 8 * y + 2 * fk + e;
+              if (c >= N) continue;
+              double2 v = ldc(&AE(r, c));
+              v.x += cr[x][y][e];
+              v.y += ci[x][y][e];
+              AE(r, c) = v;
+            }
+        }
       }
     }
     cluster.sync();
-    if (i < n - 1) {
-      // (b) H(i)^H = I - conj(tauq) v v^H on columns i+1..n-1
-      const double2 tq = __ldcg(&S.tau[i]);
-      for (int c = i + 1 + gw; c < n; c += nw) {
-        double wr = 0.0, wi = 0.0;
-        for (int r = i + lane; r < m; r += 32) {
-          const double2 x = __ldcg(X + r + (size_t)m * c);
-          const double2 v = r == i ? make_double2(1.0, 0.0) : __ldcg(X + r + (size_t)m * i);
-          wr = fma(v.x, x.x, fma(v.y, x.y, wr));
-          wi = fma(v.x, x.y, fma(-v.y, x.x, wi));
-        }
-        wr = bsum(wr);
-        wi = bsum(wi);
-        const double fr = tq.x * wr + tq.y * wi, fi = tq.x * wi - tq.y * wr;  // conj(tq) w
-        for (int r = i + lane; r < m; r += 32) {
-          const double2 v = r == i ? make_double2(1.0, 0.0) : __ldcg(X + r + (size_t)m * i);
-          double2 x = __ldcg(X + r + (size_t)m * c);
-          x.x -= v.x * fr - v.y * fi;
-          x.y -= v.x * fi + v.y * fr;
-          X[r + (size_t)m * c] = x;
-        }
+    {  // norm partials of column q below the diagonal
+      double acc = 0.0;
+      for (int r = q + 1 + gt; r < M; r += gthr) {
+        const double2 a = ldc(&AE(r, q));
+        acc = fma(a.x, a.x, fma(a.y, a.y, acc));
       }
-      cluster.sync();
-      // (c) right reflector on row i, columns i+1..n-1 (ZLACGV, ZLARFG, ZLACGV)
-      if (crank == 0 && warp == 0) {
-        double beta;
-        double2 tau;
-        double2 alpha = __ldcg(X + i + (size_t)m * (i + 1));
-        alpha.y = -alpha.y;
-        // scaled vector, unconjugated, goes to Pv(:, i); the row keeps its conjugate
-        double2 *row = X + i + (size_t)m * (i + 2);
-        warp_larfg(alpha, row, (size_t)m, n - i - 2, lane, &beta, &tau, true, false);
-        __syncwarp();
-        for (int c = i + 2 + lane; c < n; c += 32) {
-          const double2 u = __ldcg(X + i + (size_t)m * c);
-          Pv[c + (size_t)n * i] = u;
-          X[i + (size_t)m * c] = make_double2(u.x, -u.y);
-        }
-        if (lane == 0) {
-          ee[i] = beta;
-          S.taup[i] = tau;
-          X[i + (size_t)m * (i + 1)] = make_double2(beta, 0.0);
-          Pv[(i + 1) + (size_t)n * i] = make_double2(1.0, 0.0);
-        }
-      }
-      cluster.sync();
-      // (d) C = X(i+1:m, i+1:n) <- C (I - taup u u^H): w = C u by column chunks
-      const double2 tp = __ldcg(&S.taup[i]);
-      const int rows = m - i - 1, cols = n - i - 1;
-      const int nrc = (rows + 31) / 32, ncc = (cols + kCC - 1) / kCC;
-      for (int t = gw; t < nrc * ncc; t += nw) {
-        const int rc = t % nrc, cc = t / nrc;
-        const int r = i + 1 + rc * 32 + lane;
-        const int c0 = i + 1 + cc * kCC, c1 = min(n, c0 + kCC);
-        double wr = 0.0, wi = 0.0;
-        if (r < m)
-          for (int c = c0; c < c1; ++c) {
-            const double2 x = __ldcg(X + r + (size_t)m * c);
-            const double2 u = __ldcg(Pv + c + (size_t)n * i);
-            wr = fma(x.x, u.x, fma(-x.y, u.y, wr));
-            wi = fma(x.x, u.y, fma(x.y, u.x, wi));
-          }
-        if (r < m) part[(size_t)cc * m + r] = make_double2(wr, wi);
-      }
-      cluster.sync();
-      for (int t = gw; t < nrc * ncc; t += nw) {
-        const int rc = t % nrc, cc = t / nrc;
-        const int r = i + 1 + rc * 32 + lane;
-        if (r >= m) continue;
-        double wr = 0.0, wi = 0.0;
-        for (int q = 0; q < ncc; ++q) {  // fixed order
-          const double2 p = __ldcg(part + (size_t)q * m + r);
-          wr += p.x;
-          wi += p.y;
-        }
-        // f = taup * w
-        const double fr = tp.x * wr - tp.y * wi, fi = tp.x * wi + tp.y * wr;
-        const int c0 = i + 1 + cc * kCC, c1 = min(n, c0 + kCC);
-        for (int c = c0; c < c1; ++c) {
-          const double2 u = __ldcg(Pv + c + (size_t)n * i);  // subtract f conj(u)
-          double2 x = __ldcg(X + r + (size_t)m * c);
-          x.x -= fr * u.x + fi * u.y;
-          x.y -= fi * u.x - fr * u.y;
-          X[r + (size_t)m * c] = x;
-        }
-      }
-      cluster.sync();
-    } else if (crank == 0 && threadIdx.x == 0) {
-      S.taup[i] = make_double2(0.0, 0.0);
+      acc = block_sum(acc, red);
+      if (tid == 0) ax.nrmL[crank] = acc;
     }
+    cluster.sync();
   }
+#undef AE
+#undef YB
+#undef XB
+#undef PV
 }
 
 // ---------------------------------------------------------------------------
 // 2. bisection: sigma_i of B for i < kk (one thread each), Golub-Kahan Sturm counts
 // ---------------------------------------------------------------------------
-__device__ int gk_count_less(const double *dd, const double *ee, int n, double x) {
-  // eigenvalues of the zero-diagonal tridiagonal with off-diagonals d0,e0,d1,... below x
-  const double pivmin = 1e-290;
+// Sturm count of the Golub-Kahan matrix: eigenvalues below x; sq = squared
+// off-diagonals (2n-1 of them).  Two independent recurrences interleave.
+__device__ __forceinline__ void gk_count2(const double *sq, int n1, double x0, double x1, double pivmin,
+                                          int &c0, int &c1) {
+  double q0 = -x0, q1 = -x1;
+  c0 = q0 < 0.0;
+  c1 = q1 < 0.0;
+  for (int j = 0; j < n1; ++j) {
+    const double o2 = sq[j];
+    if (fabs(q0) < pivmin) q0 = -pivmin;
+    if (fabs(q1) < pivmin) q1 = -pivmin;
+    q0 = -x0 - o2 / q0;
+    q1 = -x1 - o2 / q1;
+    c0 += q0 < 0.0;
+    c1 += q1 < 0.0;
+  }
+}
+
+__device__ __forceinline__ int gk_count(const double *sq, int n1, double x, double pivmin) {
   double q = -x;
   int c = q < 0.0;
-  for (int j = 1; j < 2 * n; ++j) {
-    const double o = (j & 1) ? dd[j >> 1] : ee[(j >> 1) - 1];
+  for (int j = 0; j < n1; ++j) {
     if (fabs(q) < pivmin) q = -pivmin;
-    q = -x - (o * o) / q;
+    q = -x - sq[j] / q;
     c += q < 0.0;
   }
   return c;
 }
 
-__global__ void k_bd_sigma(Slot *slots, const int *path, int kk) {
+// the same count in FP32 on off-diagonals scaled by 1/hi (values in [0, 1])
+__device__ __forceinline__ int gk_count_f32(const float *sqf, int n1, float x) {
+  float q = -x;
+  int c = q < 0.0f;
+  for (int j = 0; j < n1; ++j) {
+    if (fabsf(q) < 1e-30f) q = -1e-30f;
+    q = -x - __fdividef(sqf[j], q);
+    c += q < 0.0f;
+  }
+  return c;
+}
+
+// sigma_i of B for i < min(kk, n), descending.  One thread per value, one warp
+// per block so that the FP64 work spreads over the SMs:
+//   1. FP32 bisection on the scaled problem to width 2^-22 ||T||; FP32 Sturm counts
+//      are exact for a T perturbed by a few float ulps, so the bracket widened by
+//      2^-18 ||T|| holds sigma_i; two FP64 counts check it (reset to [0, ||T||]
+//      otherwise).
+//   2. FP64 bisection to width 2 eps sigma + eps ||T||: the absolute accuracy
+//      LAPACK's bidiagonal SVD reaches on Theta as a whole.
+constexpr int kSigmaThreads = 32;
+__global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const int *path, int kk) {
   const int s = blockIdx.y;
   const int route = path[s];
   if (!on_route(route)) return;
   const Slot S = slots[s];
   int m, n;
   bd_dims(*S.cp, route, m, n);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int kk_s = min(kk, n);
-  if (i >= kk_s) return;
+  const int K = min(kk, n);
+  if ((int)(blockIdx.x * blockDim.x) >= K) return;  // uniform per block
+  const int n1 = 2 * n - 1;
+  extern __shared__ double sq[];  // n1 squared off-diagonals, then n1 scaled FP32 copies
+  float *sqf = reinterpret_cast<float *>(sq + n1);
   const double *dd = S.bdws, *ee = S.bdws + n;
-  double hi = 0.0;
-  for (int j = 0; j < n; ++j) {
-    const double a = fabs(dd[j]) + (j < n - 1 ? fabs(ee[j]) : 0.0) + (j > 0 ? fabs(ee[j - 1]) : 0.0);
-    hi = fmax(hi, a);
+  double hl = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x)
+    hl = fmax(hl, fabs(dd[j]) + (j < n - 1 ? fabs(ee[j]) : 0.0) + (j > 0 ? fabs(ee[j - 1]) : 0.0));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) hl = fmax(hl, __shfl_xor_sync(0xffffffffu, hl, o));
+  const double hi = hl * (1.0 + 1e-12) + 1e-300;  // Gershgorin bound of the Golub-Kahan matrix
+  const double inv_hi = 1.0 / hi;
+  for (int j = threadIdx.x; j < n1; j += blockDim.x) {
+    const double o = (j & 1) ? ee[j >> 1] : dd[j >> 1];
+    sq[j] = o * o;
+    sqf[j] = (float)((o * inv_hi) * (o * inv_hi));
   }
-  hi = hi * (1.0 + 1e-12) + 1e-300;
-  double lo = 0.0, h = hi;
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K) return;
   const int target = 2 * n - 1 - i;  // count(< x) <= target  <=>  x <= sigma_i
-  for (int it = 0; it < 256; ++it) {
+  const double pivmin = 1e-290 * fmax(1.0, hi * hi);
+  // 1. FP32 bracket
+  float lf = 0.0f, hf = 1.0f;
+  for (int it = 0; it < 22; ++it) {
+    const float mid = 0.5f * (lf + hf);
+    if (gk_count_f32(sqf, n1, mid) <= target)
+      lf = mid;
+    else
+      hf = mid;
+  }
+  double lo = fmax(0.0, ((double)lf - 3.814697265625e-06) * hi);  // widened by 2^-18
+  double h = fmin(1.0, (double)hf + 3.814697265625e-06) * hi;
+  {
+    int c0, c1;
+    gk_count2(sq, n1, lo, h, pivmin, c0, c1);
+    if (!(c0 <= target && c1 > target)) {
+      lo = 0.0;
+      h = hi;
+    }
+  }
+  // 2. FP64 bisection
+  for (int it = 0; it < 160; ++it) {
+    if (h - lo <= 4.440892098500626e-16 * h + 2.220446049250313e-16 * hi || h < 1e-30 * hi) break;
     const double mid = 0.5 * (lo + h);
-    if (gk_count_less(dd, ee, n, mid) <= target)
+    if (gk_count(sq, n1, mid, pivmin) <= target)
       lo = mid;
     else
       h = mid;
-    if (h - lo <= 4.440892098500626e-16 * h || h < 1e-30 * hi) break;
   }
   const double sg = 0.5 * (lo + h);
   S.bdws[2 * n + i] = sg < 1e-30 * hi ? 0.0 : sg;
@@ -275,8 +614,8 @@ __global__ void k_bd_sigma(Slot *slots, const int *path, int kk) {
 // ---------------------------------------------------------------------------
 // 3a. inverse iteration on (T_GK - sigma_i I), one thread per value.
 // Scratch per value (transposed so that threads of a warp touch adjacent words):
-//   U0, U1, U2 (upper factor of the pivoted LU), PV (multipliers), Y (swap flags),
-//   then the vector Z itself.
+//   U0 (reciprocal pivots), U1, U2 (upper factor of the pivoted LU), PV (multipliers),
+//   Y (swap flags), then the vector Z itself.
 // ---------------------------------------------------------------------------
 __global__ void k_bd_invit(Slot *slots, const int *path, int kk) {
   const int s = blockIdx.y;
@@ -312,8 +651,8 @@ __global__ void k_bd_invit(Slot *slots, const int *path, int kk) {
     const double sub = off(j);
     const double nd0 = -lam, nd1 = j + 1 < N - 1 ? off(j + 1) : 0.0;
     if (fabs(d0) >= fabs(sub)) {  // keep row j as the pivot row
-      const double piv = guard(d0), mult = sub / piv;
-      AT(U0, j) = piv;
+      const double piv = guard(d0), rp = 1.0 / piv, mult = sub * rp;
+      AT(U0, j) = rp;
       AT(U1, j) = d1;
       AT(U2, j) = 0.0;
       AT(PV, j) = mult;
@@ -322,7 +661,7 @@ __global__ void k_bd_invit(Slot *slots, const int *path, int kk) {
       d1 = nd1;
     } else {  // row j+1 becomes the pivot row
       const double mult = d0 / sub;
-      AT(U0, j) = sub;
+      AT(U0, j) = 1.0 / sub;
       AT(U1, j) = nd0;
       AT(U2, j) = nd1;
       AT(PV, j) = mult;
@@ -331,7 +670,7 @@ __global__ void k_bd_invit(Slot *slots, const int *path, int kk) {
       d1 = -mult * nd1;
     }
   }
-  AT(U0, N - 1) = guard(d0);
+  AT(U0, N - 1) = 1.0 / guard(d0);  // U0 holds the reciprocal pivots
   // start vector: fixed pseudo-random (splitmix-style hash of (i, j)), max-norm 1/2
   for (int j = 0; j < N; ++j) {
     unsigned long long x = (unsigned long long)(i + 1) * 0x9E3779B97F4A7C15ull +
@@ -364,7 +703,7 @@ __global__ void k_bd_invit(Slot *slots, const int *path, int kk) {
       double sacc = AT(Z, j);
       if (j + 1 < N) sacc -= AT(U1, j) * x1;
       if (j + 2 < N) sacc -= AT(U2, j) * x2;
-      double x = sacc / AT(U0, j);
+      double x = sacc * AT(U0, j);
       if (fabs(x) > 3.273390607896142e150) {
         const double r = 3.054936363499605e-151;  // 2^-500
         for (int q = j + 1; q < N; ++q) AT(Z, q) *= r;
@@ -392,51 +731,128 @@ __global__ void k_bd_invit(Slot *slots, const int *path, int kk) {
 #undef AT
 }
 
-// 3b. split z into v (even) and u (odd) and re-orthogonalise each set, in order
-// of descending sigma, by classical Gram-Schmidt applied twice.  One CTA per
-// bond; the dot products of vector i against all earlier ones are one warp each.
-__global__ void __launch_bounds__(512) k_bd_orth(Slot *slots, const int *path, int kk) {
-  const int s = blockIdx.x;
+// 3b. split z into v (even rows) and u (odd rows) and re-orthogonalise each set in
+// order of descending sigma by classical Gram-Schmidt, with a second pass only
+// when the first removed more than 1 - 1/sqrt(2) of the vector's norm (the
+// "twice is enough" test of Daniel, Gragg, Kaufman and Stewart).  A cluster of
+// kOrthCluster CTAs per (bond, set) splits the rows; partial dot products and
+// norms meet in the (free by now) inverse-iteration scratch, double-buffered.
+// Z is row-major (element (j, i) at j*K + i): the dot products run one thread per
+// earlier vector over a quarter of the CTA's rows (coalesced across threads), the
+// subtraction one warp per row.
+constexpr int kOrthThreads = 512;
+constexpr int kOrthCluster = 2;
+__global__ void __launch_bounds__(kOrthThreads) k_bd_orth(Slot *slots, const int *path, int kk) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks(), crank = (int)cluster.block_rank();
+  const int s = blockIdx.y, part = blockIdx.x / C;  // part 0: v = z[2j], 1: u = z[2j+1]
   const int route = path[s];
-  if (!on_route(route)) return;
+  if (!on_route(route)) return;  // uniform per cluster
   const Slot S = slots[s];
   int m, n;
   bd_dims(*S.cp, route, m, n);
   const int N = 2 * n, K = min(kk, n);
-  double *Z = S.bdws + bd_scratch(n, kk) + 5 * (size_t)N * K;  // element (j, i) at [j * K + i]
-  extern __shared__ double dots[];                        // K
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int part = 0; part < 2; ++part) {  // 0: v = z[2j], 1: u = z[2j+1]
+  double *Z = S.bdws + bd_scratch(n, kk) + 5 * (size_t)N * K;
+  double *xch = S.bdws + bd_scratch(n, kk) + (size_t)part * N * K;  // 2 x C x (K + 1)
+  const int j0 = (int)((long long)n * crank / C), j1 = (int)((long long)n * (crank + 1) / C);
+  extern __shared__ double dots[];  // K dot products, then 4 x K partial sums
+  double *psum = dots + K;
+  __shared__ double red[kOrthThreads / 32];
+  __shared__ double nrm_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarp = kOrthThreads / 32;
+  const int qt = tid & 127, jc = tid >> 7;  // 128 vector slots x 4 row quarters
+  int post = 0;                             // postings so far (buffer = post & 1)
 #define ZE(j, i) Z[(size_t)(2 * (j) + part) * K + (i)]
-    for (int i = 0; i < K; ++i) {
-      for (int pass = 0; pass < 2; ++pass) {
-        for (int q = warp; q < i; q += nw) {
-          double a = 0.0;
-          for (int j = lane; j < n; j += 32) a = fma(ZE(j, q), ZE(j, i), a);
-          a = bsum(a);
-          if (lane == 0) dots[q] = a;
-        }
-        __syncthreads();
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          double v = ZE(j, i);
-          for (int q = 0; q < i; ++q) v = fma(-dots[q], ZE(j, q), v);
-          ZE(j, i) = v;
-        }
-        __syncthreads();
+#define XC(buf, r, q) xch[((size_t)(buf) * C + (r)) * (K + 1) + (q)]
+  // CTA sum of the squared norm of z_i over this CTA's rows
+  auto norm_part = [&](int i) -> double {
+    double a = 0.0;
+    for (int j = j0 + tid; j < j1; j += kOrthThreads) a = fma(ZE(j, i), ZE(j, i), a);
+    a = bsum(a);
+    __syncthreads();
+    if (lane == 0) red[warp] = a;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < nwarp; ++w) t += red[w];
+    return t;
+  };
+  // post this CTA's dot products of z_i with z_q (q < i) and, optionally, a norm
+  auto post_dots = [&](int i, bool with_norm) {
+    const int buf = post & 1;
+    for (int q = qt; q < i; q += 128) {
+      double a0 = 0.0, a1 = 0.0;
+      int j = j0 + jc;
+      for (; j + 4 < j1; j += 8) {
+        a0 = fma(ZE(j, q), ZE(j, i), a0);
+        a1 = fma(ZE(j + 4, q), ZE(j + 4, i), a1);
       }
-      if (warp == 0) {
-        double a = 0.0;
-        for (int j = lane; j < n; j += 32) a = fma(ZE(j, i), ZE(j, i), a);
-        a = bsum(a);
-        if (lane == 0) dots[0] = a > 0.0 ? 1.0 / sqrt(a) : 0.0;
-      }
-      __syncthreads();
-      const double inv = dots[0];
-      for (int j = threadIdx.x; j < n; j += blockDim.x) ZE(j, i) *= inv;
-      __syncthreads();
+      for (; j < j1; j += 4) a0 = fma(ZE(j, q), ZE(j, i), a0);
+      psum[jc * K + q] = a0 + a1;
     }
-#undef ZE
+    const double nr = with_norm ? norm_part(i) : 0.0;  // (its barriers also order psum)
+    __syncthreads();
+    for (int q = tid; q < i; q += kOrthThreads)
+      XC(buf, crank, q) = (psum[q] + psum[K + q]) + (psum[2 * K + q] + psum[3 * K + q]);
+    if (with_norm && tid == 0) XC(buf, crank, K) = nr;
+  };
+  // gather the posted dots (q < i) into shared memory and return the posted norm
+  auto gather = [&](int i, bool dots_too) -> double {
+    const int buf = post & 1;
+    if (dots_too)
+      for (int q = tid; q < i; q += kOrthThreads) {
+        double t = 0.0;
+        for (int r = 0; r < C; ++r) t += __ldcg(&XC(buf, r, q));
+        dots[q] = t;
+      }
+    if (tid == 0) {
+      double t = 0.0;
+      for (int r = 0; r < C; ++r) t += __ldcg(&XC(buf, r, K));
+      nrm_s = t;
+    }
+    __syncthreads();
+    ++post;
+    return nrm_s;
+  };
+  auto subtract = [&](int i) {
+    for (int j = j0 + warp; j < j1; j += nwarp) {
+      double a = 0.0;
+      for (int q = lane; q < i; q += 32) a = fma(dots[q], ZE(j, q), a);
+      a = bsum(a);
+      if (lane == 0) ZE(j, i) -= a;
+    }
+    __syncthreads();
+  };
+  auto post_norm = [&](int i) {
+    const double nr = norm_part(i);
+    if (tid == 0) XC(post & 1, crank, K) = nr;
+  };
+  for (int i = 0; i < K; ++i) {
+    post_dots(i, true);
+    cluster.sync();
+    const double nrm0 = gather(i, true);
+    double nrm = nrm0;
+    if (i > 0) {
+      subtract(i);
+      post_norm(i);
+      cluster.sync();
+      nrm = gather(i, false);
+      if (nrm < 0.5 * nrm0) {  // second pass
+        post_dots(i, false);
+        cluster.sync();
+        gather(i, true);
+        subtract(i);
+        post_norm(i);
+        cluster.sync();
+        nrm = gather(i, false);
+      }
+    }
+    const double inv = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+    for (int j = j0 + tid; j < j1; j += kOrthThreads) ZE(j, i) *= inv;
+    __syncthreads();
   }
+#undef ZE
+#undef XC
 }
 
 // ---------------------------------------------------------------------------
@@ -584,6 +1000,8 @@ __global__ void k_bd_transpose(Slot *slots, const int *path) {
 // ---------------------------------------------------------------------------
 // host orchestration: bidiagonal route for the slots flagged kPathBidiag / kPathBidiagT
 // ---------------------------------------------------------------------------
+size_t bidiag_aux_elems(int n) { return bd_aux_elems(n, n); }
+
 size_t bidiag_ws_doubles(int n, int chi) {
   const int K = std::min(chi, n);
   return bd_scratch(n, chi) + 6 * (size_t)(2 * n) * K + 2 * (size_t)n * K;
@@ -604,29 +1022,83 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     TEBD_LAUNCHED(h);
   }
   {
-    int C = (nmax + kBW * 8 - 1) / (kBW * 8);
-    C = C < 1 ? 1 : (C > 8 ? 8 : C);
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(C, nb, 1);
+    const size_t smem = sizeof(double2) * ((size_t)nmax + 4 * kPanel) + sizeof(double) * kStageDoubles;
+    if ((rc = check_cuda(h, cudaFuncSetAttribute(k_gebrd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem),
+                         "bidiagonalisation shared memory")))
+      return rc;
     cfg.blockDim = dim3(kBW * 32, 1, 1);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = C;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    // Cluster size: the kernel is bound by the SMs' FP64 pipes, so the batch's time
+    // goes as waves / C; clusters must fit in one GPC, so the co-resident count
+    // (occupancy query) decides how many waves a size needs.  Ties keep the
+    // smaller size (fewer barriers' worth of idle SMs in a partial wave).
+    const int cmax = std::max(1, std::min(8, (nmax + 127) / 128));
+    int C = 1;
+    double best = 1e300;
+    for (int c = 1; c <= cmax; ++c) {
+      cfg.gridDim = dim3(c, nb, 1);
+      attr[0].val.clusterDim.x = c;
+      int ncl = 0;
+      if (cudaOccupancyMaxActiveClusters(&ncl, (const void *)k_gebrd, &cfg) != cudaSuccess || ncl < 1) {
+        cudaGetLastError();
+        continue;
+      }
+      const double cost = (double)((nb + ncl - 1) / ncl) / c;
+      if (cost < best * (1.0 - 1e-9)) {
+        best = cost;
+        C = c;
+      }
+    }
+    cfg.gridDim = dim3(C, nb, 1);
+    attr[0].val.clusterDim.x = C;
     rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_gebrd, h->slots_d, (const int *)h->path_d),
                     "bidiagonalisation launch");
     if (rc) return rc;
     TEBD_LAUNCHED(h);
   }
-  k_bd_sigma<<<dim3(cdiv(kk, 128), nb), 128, 0, st>>>(h->slots_d, h->path_d, kk);
+  {
+    const size_t smem = (sizeof(double) + sizeof(float)) * (size_t)(2 * nmax);
+    if ((rc = check_cuda(h, cudaFuncSetAttribute(k_bd_sigma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem),
+                         "bisection shared memory")))
+      return rc;
+    k_bd_sigma<<<dim3(cdiv(kk, kSigmaThreads), nb), kSigmaThreads, smem, st>>>(h->slots_d, h->path_d,
+                                                                                kk);
+  }
   TEBD_LAUNCHED(h);
-  k_bd_invit<<<dim3(cdiv(kk, 128), nb), 128, 0, st>>>(h->slots_d, h->path_d, kk);
+  k_bd_invit<<<dim3(cdiv(kk, 32), nb), 32, 0, st>>>(h->slots_d, h->path_d, kk);
   TEBD_LAUNCHED(h);
-  k_bd_orth<<<nb, 512, sizeof(double) * (size_t)(kk > 1 ? kk : 1), st>>>(h->slots_d, h->path_d, kk);
+  {
+    const size_t smem = sizeof(double) * 5 * (size_t)(kk > 1 ? kk : 1);
+    if ((rc = check_cuda(h, cudaFuncSetAttribute(k_bd_orth, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem),
+                         "orthogonalisation shared memory")))
+      return rc;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * kOrthCluster, nb, 1);
+    cfg.blockDim = dim3(kOrthThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kOrthCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if ((rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_bd_orth, h->slots_d, (const int *)h->path_d, kk),
+                         "orthogonalisation launch")))
+      return rc;
+  }
   TEBD_LAUNCHED(h);
   k_bd_apply<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
   TEBD_LAUNCHED(h);

@@ -182,7 +182,7 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
   const size_t nn = (size_t)n * n;
   // per slot: X, V (n^2 each), S, perm, QR buffers (jpvt, tau, 2n norms), aux (3 n^2)
   // (the QR buffers and aux serve the dense path only; NC blocks live in X and V)
-  const size_t aux_elems = mode == TEBD_MODE_DENSE ? 3 * nn : 0;
+  const size_t aux_elems = mode == TEBD_MODE_DENSE ? std::max(3 * nn, bidiag_aux_elems(n)) : 0;
   const size_t bd_elems = mode == TEBD_MODE_DENSE ? bidiag_ws_doubles(n, chi) : 0;
   size_t per = al(sizeof(double2) * nn) * 2 + al(sizeof(double) * n) + al(sizeof(int) * n) +
                al(sizeof(int) * n) + al(sizeof(double2) * n) * 2 + al(sizeof(double) * 2 * n) +
@@ -440,9 +440,10 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
       int nbd = 0, nbd_max = 0;
       for (int s = 0; s < nb; ++s) {
         const int mn = std::min(cps[s].m, cps[s].n), mx = std::max(cps[s].m, cps[s].n);
-        const bool bd = h->opts.svd_mode == TEBD_SVD_BIDIAG ? mn >= 2
-                        : h->opts.svd_mode == TEBD_SVD_QRJ  ? false
-                                                            : mn >= kBidiagMinDim;
+        const bool bd = mx > kBidiagMaxDim                   ? false
+                        : h->opts.svd_mode == TEBD_SVD_BIDIAG ? mn >= 2
+                        : h->opts.svd_mode == TEBD_SVD_QRJ    ? false
+                                                              : mn >= kBidiagMinDim;
         h->path_h[s] = !bd ? kPathQRJ : (cps[s].m >= cps[s].n ? kPathBidiag : kPathBidiagT);
         if (bd) {
           ++nbd;

@@ -66,7 +66,6 @@ struct NcWorkspace {
   JacobiProblem<double> *probs_d;  // nslots * bmax problems
 };
 
-inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 
 }  // namespace
 

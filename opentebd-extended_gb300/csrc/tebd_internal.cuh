@@ -185,6 +185,8 @@ int jacobi_persistent_double(tebd_handle *h, const JacobiProblem<double> *probs_
 int run_qrj(tebd_handle *h, int nb, int nmax);
 int run_bidiag(tebd_handle *h, int nb, int nmax);
 size_t bidiag_ws_doubles(int n, int chi);
+size_t bidiag_aux_elems(int n);
+constexpr int kBidiagMaxDim = 4096;  // larger compacted Theta take the QR + Jacobi route
 int jacobi_collect(tebd_handle *h);
 int measure_fp64_peak(int device, double *tflops);
 int run_nc_batch(tebd_handle *h, int nb, const int *links_host, double *truncerr_host);
