@@ -81,7 +81,7 @@ __host__ __device__ __forceinline__ size_t bd_scratch(int n, int kk) {
 //    Output (as ZGEBD2): d, e in bdws; tauq in S.tau, v_i below the diagonal of
 //    column i; taup in S.taup, u_i in column i of Pv with u_i(i+1) = 1.
 // ---------------------------------------------------------------------------
-constexpr int kPanel = 32;  // columns per panel
+constexpr int kPanel = 8;   // columns per panel (narrow: the per-column corrections grow with it)
 constexpr int kChunk = 32;  // columns per task of the w = A0 u pass
 constexpr int kTile = 64;   // trailing-update tile (rows and columns)
 constexpr int kKc = 16;     // trailing-update k chunk staged in shared memory
