@@ -8,11 +8,18 @@ entry, renormalised.  One step = one Trotter step = 95 bond updates (32 odd +
 31 even + 32 odd, each sweep batched on the GPU).  Data are synthetic (the
 reference has no dataset); the configuration is the one the metric is quoted on.
 
-value: updates/s with the chain resident in HBM, CUDA events on the library's
-       stream around exactly K steps.
-e2e:   the same through the reference-facing C ABI with host buffers: every step
-       uploads all Gammas/Lambdas from pinned host memory, runs TrotterStep and
-       downloads the chain again (a Fortran host that keeps its own arrays).
+A bench run is the configured run itself: K Trotter steps (default 200, the whole
+configuration) from the initial state, after W warm-up steps on a copy.
+value: updates/s with the chain resident in HBM: CUDA events on the library's
+       stream around exactly the K steps (one more event per step gives the
+       per-step costs: early steps are cheap, the chain saturates chi = 128 near
+       step 50 and the SVD dimension then stays near 600).
+e2e:   the same K steps end to end through the reference-facing C ABI: the chain
+       is uploaded from pinned host buffers (tebd_set_gamma/lambda), every step
+       passes its gates from host memory and returns the truncation error to the
+       host (tebd_trotter_step), and the chain is read back at the end
+       (tebd_get_gamma/lambda): the drop-in keeps Gammas/Lambdas resident across
+       steps, as a Fortran host calling it would.  Host wall clock, synchronised.
 --impl reference: the reference's CPU algorithm (the C restatement in oracle/,
        naive FormTheta/ThetaOperation loops + LAPACK ZGESVD) on all host cores,
        one bond update per core per step.
@@ -209,97 +216,98 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t[0])
 
-    # warm-up on the same chain, then restart from the initial state, so that the
-    # timed K steps are steps 1..K of the configured run (the update's cost grows
-    # with the Schmidt rank as the state entangles)
+    # warm-up on the same chain; the timed pass then uploads the initial state
+    # again, so that the timed K steps are steps 1..K of the configured run (the
+    # update's cost grows with the Schmidt rank as the state entangles)
     for _ in range(args.warmup):
         chain.trotter_step(Udt, ORDER)
-    chain.set_state(gam, lam)
 
-    # ---- value: device-resident chain --------------------------------------
-    chain.reset_stats()
-    chain.set_profiling(True)
-    launches0 = chain.kernel_launches()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    with ClockSampler(os.path.join(args.outdir, "clocks.csv")) as clk:
-        ev0.record(stream)
-        te_total = 0.0
-        for _ in range(args.steps):
-            te_total += chain.trotter_step(Udt, ORDER)
-        ev1.record(stream)
-        barrier()
-    ms = maxall(ev0.elapsed_time(ev1))
-    launches = chain.kernel_launches() - launches0
-    st = chain.stats()
-    chain.set_profiling(False)
-    value = world * UPDATES_PER_STEP * args.steps / (ms / 1e3)
-
-    # ---- e2e: host buffers through the C ABI ---------------------------------
-    state_g, state_l = chain.get_state()
+    # host-side inputs of the end-to-end path: the initial chain in pinned memory
+    # (Fortran order, as the reference holds it) and the gates
     pin_g = [torch.empty((CHI, D, CHI)[::-1], dtype=torch.complex128, pin_memory=True).numpy().T
              for _ in range(L)]
     pin_l = [torch.empty(CHI, dtype=torch.float64, pin_memory=True).numpy() for _ in range(L + 1)]
-    for a, b in zip(pin_g, state_g):
-        a[...] = b
-    for a, b in zip(pin_l, state_l):
-        a[...] = b
-    gates = [np.asfortranarray(g, dtype=np.complex128) for g in Udt]
-    h2d = sum(a.nbytes for a in pin_g) + sum(a.nbytes for a in pin_l) + sum(g.nbytes for g in gates)
-    d2h = sum(a.nbytes for a in pin_g) + sum(a.nbytes for a in pin_l) + 8
-    # same window as `value`: steps 1..K from the initial state, through host buffers
     for a, b in zip(pin_g, gam):
         a[...] = b
     for a, b in zip(pin_l, lam):
         a[...] = b
-    e2e_steps = args.steps
+    gates = [np.asfortranarray(g, dtype=np.complex128) for g in Udt]
+    state_bytes = sum(a.nbytes for a in pin_g) + sum(a.nbytes for a in pin_l)
+    # per step: odd sweep, even sweep, odd sweep (order 2)
+    gate_bytes = sum(Udt[k].nbytes for k in range(L - 1)) + sum(Udt[k].nbytes for k in range(0, L - 1, 2))
+
+    chain.reset_stats()
+    chain.set_profiling(True)
+    launches0 = chain.kernel_launches()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    te_total = 0.0
     barrier()
-    ev0.record(stream)
-    for _ in range(e2e_steps):
+    with ClockSampler(os.path.join(args.outdir, "clocks.csv")) as clk:
+        t0 = time.perf_counter()
         for s in range(1, L + 1):
             chain.set_gamma(s, pin_g[s - 1])
         for l in range(1, L + 2):
             chain.set_lambda(l, pin_l[l - 1])
-        chain.trotter_step(gates, ORDER)
+        evs[0].record(stream)
+        for k in range(args.steps):
+            te_total += chain.trotter_step(gates, ORDER)
+            evs[k + 1].record(stream)
         for s in range(1, L + 1):
             chain.get_gamma_into(s, pin_g[s - 1])
         for l in range(1, L + 2):
             chain.get_lambda_into(l, pin_l[l - 1])
-    ev1.record(stream)
-    barrier()
-    e2e_ms = maxall(ev0.elapsed_time(ev1))
-    e2e = world * UPDATES_PER_STEP * e2e_steps / (e2e_ms / 1e3)
+        torch.cuda.synchronize()
+        e2e_wall = time.perf_counter() - t0
+        barrier()
+    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    ms = maxall(sum(step_ms))
+    e2e_ms = maxall(e2e_wall * 1e3)
+    launches = chain.kernel_launches() - launches0
+    st = chain.stats()
+    chain.set_profiling(False)
+    state_g, state_l = pin_g, pin_l
+    value = world * UPDATES_PER_STEP * args.steps / (ms / 1e3)
+    e2e = world * UPDATES_PER_STEP * args.steps / (e2e_ms / 1e3)
+    h2d = gate_bytes + state_bytes / args.steps
+    d2h = 8 * UPDATES_PER_STEP + 16 * 3 + state_bytes / args.steps
+    sat = step_ms[49:] if args.steps > 60 else []
+    phases = {"ms_per_step_steps_1_20": sum(step_ms[:20]) / min(20, args.steps),
+              "ms_per_step_steps_50_end": (sum(sat) / len(sat)) if sat else None,
+              "ms_step_1": step_ms[0], "ms_step_last": step_ms[-1]}
 
     # ---- CPU baseline: the oracle port on a bounded sample ------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
-        links = [1, 3, 5, 7][: args.cpu_updates]
+        links = [L // 2 - 1, L // 2 + 1, L // 2 - 3, L // 2 + 3][: args.cpu_updates]  # interior bonds
         v, wall = cpu_sample(state_g, state_l, Udt, links, 1)
         cpu = {"value": v, "unit": "updates/s", "cores": 1, "kind": "port",
                "sample": "%d bond updates (links %s of an odd sweep) of the timed chain, d=5, chi=128: "
                          "C restatement of TwoSiteOp_c (naive loops) + LAPACK ZGESVD, 1 thread, %.1f s"
                          % (len(links), ",".join(map(str, links)), wall)}
 
-    # ---- roofline of the dominant kernel (Jacobi rounds, FP64 pipe) ---------
+    # ---- roofline of the dominant kernel: the bidiagonalisation, FP64 pipe ----
     prof = {}
-    pth = os.path.join(ROOT, "profiles", "jacobi_round_traffic.json")
+    pth = os.path.join(ROOT, "profiles", "k_gebrd_traffic.json")
     if os.path.exists(pth):
         prof = json.load(open(pth))
-    achieved = st["jacobi_flops"] / (st["jacobi_ms"] / 1e3) / 1e12 if st["jacobi_ms"] > 0 else None
+    nl = max(1, st["gebrd_launches"])
+    flops_launch = st["gebrd_flops"] / nl
+    achieved = st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12 if st["gebrd_ms"] > 0 else None
     roof = {
-        "kernel": "k_jacobi_persistent<double>", "bound": "fp64", "achieved": achieved, "peak": fp64_peak,
-        "unit": "TFLOP/s", "frac": (achieved / fp64_peak) if achieved else None,
-        "traffic": prof.get("dram_bytes_per_launch"),
-        "peak_source": "measured DFMA throughput of this GPU (tebd_measure_fp64_peak); "
+        "kernel": "k_gebrd", "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+        "frac": (achieved / fp64_peak) if achieved else None,
+        "traffic": prof["dram_bytes_per_flop"] * flops_launch if prof else None,
+        "peak_source": "measured FP64 FMA throughput of this GPU (tebd_measure_fp64_peak); "
                        "MEASURED_PEAKS.json carries no FP64 figure",
-        "jacobi_share_of_step": st["jacobi_ms"] / ms if ms > 0 else None,
-        "achieved_gbs_algorithmic": st["jacobi_bytes"] / (st["jacobi_ms"] / 1e3) / 1e9 if st["jacobi_ms"] > 0 else None,
-        "jacobi_flops_per_launch": st["jacobi_flops"] / max(1, st["jacobi_launches"]),
-        "jacobi_launches": st["jacobi_launches"], "jacobi_rotations": st["jacobi_rotations"],
-        "jacobi_pairs": st["jacobi_pairs"],
-        "qr": {"kernel": "k_qrp", "achieved": st["qr_flops"] / (st["qr_ms"] / 1e3) / 1e12 if st["qr_ms"] > 0 else None,
-               "unit": "TFLOP/s", "share_of_step": st["qr_ms"] / ms if ms > 0 else None},
+        "algorithmic": "16 M N^2 - 16 N^3/3 real flops per bond (complex Householder bidiagonalisation, M >= N)",
+        "flops_per_launch": flops_launch, "launches": st["gebrd_launches"],
+        "avg_launch_ms": st["gebrd_ms"] / nl, "share_of_timed": st["gebrd_ms"] / ms if ms > 0 else None,
+        "traffic_source": prof.get("source"),
+        "bidiag_route_share_of_timed": st["bidiag_ms"] / ms if ms > 0 else None,
+        "qrj": {"kernel": "k_jacobi_persistent<double>",
+                "achieved": st["jacobi_flops"] / (st["jacobi_ms"] / 1e3) / 1e12 if st["jacobi_ms"] > 0 else None,
+                "share_of_timed": (st["jacobi_ms"] + st["qr_ms"]) / ms if ms > 0 else None},
     }
     clocks = clk.summary()
     out = {
@@ -308,16 +316,19 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
         "config": {"workload": WORKLOAD, "L": L, "d": D, "chi": CHI, "J": J, "U": U, "mu": MU, "dt": DT,
                    "trotter_order": ORDER, "updates_per_step": UPDATES_PER_STEP,
-                   "svd": "fp64: pivoted Householder QR to the numerical rank + one-sided Jacobi on R^H",
-                   "timed_window": "Trotter steps 1..%d of the configured 200-step run (warm-up on a reset copy)" % args.steps,
-                   "mean_rank": st["rank_sum"] / max(1, st["updates"]),
+                   "svd": "fp64 per bond: Householder bidiagonalisation + bisection + inverse iteration "
+                          "(both compacted dimensions >= 64), else pivoted QR + one-sided Jacobi on R^H",
+                   "timed_window": "Trotter steps 1..%d of the configured 200-step run (warm-up on a copy)" % args.steps,
+                   "bidiag_updates": st["bidiag_updates"], "updates": st["updates"],
                    "mean_svd_cols": st["compact_cols"] / max(1, st["updates"]),
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "no flush: per-step working set (64 Gammas 84 MB + 32 Jacobi slots 420 MB) exceeds the 129 MB L2"},
+                   "l2": "no flush: per-step working set (64 Gammas 84 MB + 32 SVD slots ~1 GB) exceeds the 129 MB L2"},
+        "phases": phases,
         "steps_per_sec": value / UPDATES_PER_STEP,
         "total_truncerr_timed": te_total,
         "e2e": {"value": e2e, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps},
+                "steps": args.steps, "path": "tebd_set_gamma/lambda + tebd_trotter_step (host gates) + "
+                                              "tebd_get_gamma/lambda, host wall clock"},
         "gpu_launches": launches,
         "roofline": roof,
         "cpu_baseline": cpu,
@@ -378,13 +389,65 @@ def run_nc(args):
     chain.close()
 
 
+# ---------------------------------------------------------------------------
+# saturated-bond batch (extra line, not the headline): the cost regime that
+# dominates the configured run after step ~50.  The same chain shape (L=64, d=5,
+# chi=128) with every Lambda full (lambda_k ~ exp(-k/16), normalised) and complex
+# Gaussian Gammas (seed 5): each of the 32 odd bonds has a full 640 x 640 Theta.
+# One step = one batched TwoSiteOp sweep over the 32 odd bonds with the
+# Bose-Hubbard bond gate exp(-i dt h) (dt = 0.005).
+# ---------------------------------------------------------------------------
+def run_saturated(args):
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    pkg = ge.load_package()
+    H = pkg.hamiltonians
+    rng = np.random.default_rng(5)
+    gam = [np.asfortranarray(rng.standard_normal((CHI, D, CHI)) + 1j * rng.standard_normal((CHI, D, CHI)))
+           for _ in range(L)]
+    lam = []
+    for _ in range(L + 1):
+        l = np.exp(-np.arange(CHI) / 16.0)
+        lam.append(l / np.linalg.norm(l))
+    gate = H.matrix_exponential(H.bose_hubbard(L, D, J, U, MU)[1], DT)
+    links = list(range(1, L, 2))
+    chain = pkg.Chain(L, D, CHI)
+    chain.set_state(gam, lam)
+    stream = torch.cuda.ExternalStream(chain.stream())
+    for _ in range(args.warmup):
+        chain.apply_bonds(links, [gate] * len(links))
+    chain.reset_stats()
+    chain.set_profiling(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        chain.apply_bonds(links, [gate] * len(links))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    st = chain.stats()
+    out = {"metric": "two-site updates/sec, saturated bonds (640 x 640 Theta)",
+           "value": len(links) * args.steps / (ms / 1e3), "unit": "updates/s", "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "config": {"workload": "saturated_bonds_L64_d5_chi128", "bonds_per_step": len(links)},
+           "gebrd_tflops": st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12 if st["gebrd_ms"] > 0 else None,
+           "gebrd_share": st["gebrd_ms"] / ms, "bidiag_share": st["bidiag_ms"] / ms,
+           "gpu_launches": st["kernel_launches"]}
+    print(json.dumps(out), flush=True)
+    chain.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "nc"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "nc", "saturated"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-updates", type=int, default=2)
     ap.add_argument("--outdir", default=os.path.join(ROOT, "gpurun_out"))
@@ -394,6 +457,8 @@ def main():
         run_reference(args)
     elif args.workload == "nc":
         run_nc(args)
+    elif args.workload == "saturated":
+        run_saturated(args)
     else:
         run_ours(args)
 

@@ -59,11 +59,12 @@ extern "C" {
 #define TEBD_MODE_NC 1            /* TwoSiteOpNC: U(1) number conservation             */
 
 /* SVD algorithm (all FP64) */
-#define TEBD_SVD_FP64 0           /* default: per bond, bidiagonalisation for a large
-                                     tall/square compacted Theta (>= 256 columns), else
-                                     column-pivoted QR + one-sided Jacobi on R^H        */
+#define TEBD_SVD_FP64 0           /* default: per bond, bidiagonalisation when both
+                                     dimensions of the compacted Theta are >= 64 (a wide
+                                     one as Theta^H), else column-pivoted QR + one-sided
+                                     Jacobi on R^H                                       */
 #define TEBD_SVD_JACOBI 2         /* one-sided Jacobi on the whole (compacted) Theta    */
-#define TEBD_SVD_BIDIAG 3         /* bidiagonalisation for every tall/square Theta      */
+#define TEBD_SVD_BIDIAG 3         /* bidiagonalisation for every Theta (>= 2 x 2)       */
 #define TEBD_SVD_QRJ 4            /* pivoted QR + Jacobi on R^H for every bond          */
 
 #define TEBD_OPTS_VERSION 1
@@ -156,6 +157,10 @@ typedef struct tebd_stats {
   long long rank_sum;          /* sum over updates of the numerical rank k              */
   double bidiag_ms;            /* device time of the bidiagonal route (profiling on)     */
   long long bidiag_updates;    /* updates that took the bidiagonal route                */
+  double gebrd_flops;          /* algorithmic FP64 flops of the bidiagonalisations:
+                                  16 M N^2 - 16 N^3 / 3 per bond (M >= N)                  */
+  double gebrd_ms;             /* device time of the bidiagonalisation kernel (profiling on) */
+  long long gebrd_launches;    /* bidiagonalisation kernel launches                        */
 } tebd_stats;
 int tebd_set_profiling(tebd_handle *h, int on);
 int tebd_get_stats(tebd_handle *h, tebd_stats *stats);

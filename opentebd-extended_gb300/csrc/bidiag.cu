@@ -1042,6 +1042,8 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     // (occupancy query) decides how many waves a size needs.  Ties keep the
     // smaller size (fewer barriers' worth of idle SMs in a partial wave).
     const int cmax = std::max(1, std::min(8, (nmax + 127) / 128));
+    int nbd = 0;  // bonds on this route (the others' clusters exit at once)
+    for (int s = 0; s < nb; ++s) nbd += h->path_h[s] != kPathQRJ;
     int C = 1;
     double best = 1e300;
     for (int c = 1; c <= cmax; ++c) {
@@ -1052,7 +1054,7 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
         cudaGetLastError();
         continue;
       }
-      const double cost = (double)((nb + ncl - 1) / ncl) / c;
+      const double cost = (double)((nbd + ncl - 1) / ncl) / c;
       if (cost < best * (1.0 - 1e-9)) {
         best = cost;
         C = c;
@@ -1060,10 +1062,13 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     }
     cfg.gridDim = dim3(C, nb, 1);
     attr[0].val.clusterDim.x = C;
+    if (h->profiling) cudaEventRecord(h->ev[4], st);
     rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_gebrd, h->slots_d, (const int *)h->path_d),
                     "bidiagonalisation launch");
     if (rc) return rc;
+    if (h->profiling) cudaEventRecord(h->ev[5], st);
     TEBD_LAUNCHED(h);
+    ++h->stats.gebrd_launches;
   }
   {
     const size_t smem = (sizeof(double) + sizeof(float)) * (size_t)(2 * nmax);
@@ -1109,6 +1114,7 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     if ((rc = check_cuda(h, cudaStreamSynchronize(st), "bidiag"))) return rc;
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]) == cudaSuccess) h->stats.bidiag_ms += ms;
+    if (cudaEventElapsedTime(&ms, h->ev[4], h->ev[5]) == cudaSuccess) h->stats.gebrd_ms += ms;
   }
   return check_cuda(h, cudaGetLastError(), "bidiag launch");
 }

@@ -87,7 +87,7 @@ static void free_all(tebd_handle *h) {
   cudaFree(h->js.sweeps);
   cudaFree(h->js.pending);
   cudaFree(h->js.counters);
-  for (int e = 0; e < 4; ++e)
+  for (int e = 0; e < 6; ++e)
     if (h->ev[e]) cudaEventDestroy(h->ev[e]);
   cudaFree(h->jprob_d);
   cudaFree(h->jprobf_d);
@@ -258,7 +258,7 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
   if ((rc = dalloc(h, &h->js.counters, sizeof(unsigned long long) * 4, "alloc counters"))) FAIL(rc);
   if ((rc = check_cuda(h, cudaMemset(h->js.counters, 0, sizeof(unsigned long long) * 4), "memset")))
     FAIL(rc);
-  for (int e = 0; e < 4; ++e)
+  for (int e = 0; e < 6; ++e)
     if ((rc = check_cuda(h, cudaEventCreate(&h->ev[e]), "cudaEventCreate"))) FAIL(rc);
   if ((rc = dalloc(h, &h->status_d, sizeof(int) * 4, "alloc status"))) FAIL(rc);
   if ((rc = dalloc(h, &h->sig_link_d, sizeof(double) * (size_t)(L - 1) * n, "alloc spectra")))
@@ -448,6 +448,7 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
         if (bd) {
           ++nbd;
           nbd_max = std::max(nbd_max, mx);
+          h->stats.gebrd_flops += 16.0 * mx * (double)mn * mn - 16.0 / 3.0 * (double)mn * mn * mn;
         }
       }
       h->stats.bidiag_updates += nbd;

@@ -117,7 +117,7 @@ struct Slot {
 constexpr int kPathQRJ = 0;      // pivoted QR + one-sided Jacobi on R^H (qrj.cu)
 constexpr int kPathBidiag = 1;   // bidiagonalisation + bisection + inverse iteration (bidiag.cu)
 constexpr int kPathBidiagT = 2;  // the same on Theta^H, for a wide compacted Theta (m < n)
-constexpr int kBidiagMinDim = 256;  // default route switch: min(m, n) of the compacted Theta
+constexpr int kBidiagMinDim = 64;  // default route switch: min(m, n) of the compacted Theta
 
 }  // namespace tebd
 
@@ -165,7 +165,7 @@ struct tebd_handle {
   // diagnostics
   tebd_stats stats;
   int profiling;
-  cudaEvent_t ev[4];
+  cudaEvent_t ev[6];
 };
 
 namespace tebd {

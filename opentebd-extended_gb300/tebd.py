@@ -107,6 +107,9 @@ class Stats(ctypes.Structure):
         ("rank_sum", ctypes.c_longlong),
         ("bidiag_ms", ctypes.c_double),
         ("bidiag_updates", ctypes.c_longlong),
+        ("gebrd_flops", ctypes.c_double),
+        ("gebrd_ms", ctypes.c_double),
+        ("gebrd_launches", ctypes.c_longlong),
     ]
 
     def as_dict(self):
