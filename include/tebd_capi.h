@@ -171,6 +171,34 @@ int tebd_measure_fp64_peak(int device, double *tflops);
  * their own work against the library's. */
 void *tebd_get_stream(tebd_handle *h);
 
+/* Observables of the device-resident chain (VidalCore_v_2.0/observables_module.f90),
+ * open boundary, computed on the GPU so that the chain is not downloaded to be
+ * measured.  Complex outputs are interleaved (re, im); matrices column-major.
+ * They run on the handle's stream after any pending update and use the handle's
+ * SVD workspace, plus a small buffer allocated on first use.
+ *   tebd_single_site_rho   SingleSiteDensityMatrix / FormSingleSiteRho (:95-131):
+ *                          rho[s] (d x d) for s = 1..L, rho(i,j) = sum l0^2 l1^2 G(a,i,b) conj(G(a,j,b))
+ *   tebd_one_site_expval   OneSiteExpVal_c (:224-252): Tr(Op rho_s), Op complex d x d,
+ *                          exp_list: L complex
+ *   tebd_one_site_expval_r OneSiteExpVal_r (:194-222): Op real d x d, exp_list: L real
+ *   tebd_two_site_rho      ThetaKernal + TwoSiteRho (:704-832) on sites link, link+1:
+ *                          d^2 x d^2 complex, rows (i-1)*d+j and columns (l-1)*d+k as the gates
+ *   tebd_local_energy      LocalEnergy (:1346-1387): energy[l-1] = Re Tr(H(l) rho2(l)),
+ *                          H[l-1] complex d^2 x d^2, l = 1..L-1 (n_ops >= L-1)
+ *   tebd_total_energy      TotalEnergy (:1432-1466): sum of the bond energies
+ *   tebd_inner_product     InnerProduct (:1031-1089): <left|right>, complex; the two handles
+ *                          must have equal L, d, chi and device
+ *   tebd_chain_entropy     ChainEntropy (:1583-1602) for links 1..L+1:
+ *                          -sum_{lambda != 0} lambda^2 ln|lambda^2| / ln d */
+int tebd_single_site_rho(tebd_handle *h, double *rho);
+int tebd_one_site_expval(tebd_handle *h, const double *op, double *exp_list);
+int tebd_one_site_expval_r(tebd_handle *h, const double *op, double *exp_list);
+int tebd_two_site_rho(tebd_handle *h, int link, double *rho2);
+int tebd_local_energy(tebd_handle *h, int n_ops, const double *const *H, double *energy);
+int tebd_total_energy(tebd_handle *h, int n_ops, const double *const *H, double *energy);
+int tebd_inner_product(tebd_handle *left, tebd_handle *right, double *value);
+int tebd_chain_entropy(tebd_handle *h, double *entropy);
+
 /* Allocation-free dense update of bond `link` of a chain the caller already
  * holds in device memory.  No counterpart in the reference: it exists for
  * callers that must not allocate (a region under CUDA-graph capture, a device

@@ -92,6 +92,7 @@ static void free_all(tebd_handle *h) {
   cudaFree(h->jprob_d);
   cudaFree(h->jprobf_d);
   cudaFree(h->status_d);
+  cudaFree(h->obs_buf);
   cudaFree(h->sig_link_d);
   cudaFree(h->sig_count_d);
   cudaFree(h->sweeps_link_d);

@@ -149,6 +149,8 @@ struct tebd_handle {
   void *jprob_d;          // device array of JacobiProblem<double>
   void *jprobf_d;         // device array of JacobiProblem<float>
   int *status_d;          // [0] non-finite flag, [1] NC block error flag
+  void *obs_buf;          // observables workspace, allocated on first use (obs.cu)
+  size_t obs_bytes;
   // NC workspaces (allocated in NC mode)
   void *nc_ws;
   size_t nc_ws_bytes;

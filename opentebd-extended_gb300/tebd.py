@@ -63,6 +63,8 @@ EXPORTED_SYMBOLS = (
     "tebd_apply_bonds", "tebd_trotter_step", "tebd_get_singular_values", "tebd_get_sweeps",
     "tebd_sync", "tebd_last_error", "tebd_kernel_launches", "tebd_set_profiling", "tebd_get_stats",
     "tebd_reset_stats", "tebd_measure_fp64_peak", "tebd_get_stream", "tebd_two_site_op_noalloc",
+    "tebd_single_site_rho", "tebd_one_site_expval", "tebd_one_site_expval_r", "tebd_two_site_rho",
+    "tebd_local_energy", "tebd_total_energy", "tebd_inner_product", "tebd_chain_entropy",
 )
 
 
@@ -158,6 +160,14 @@ def load_library(path: str = LIB_PATH):
     L.tebd_get_stream.argtypes = [vp]
     L.tebd_get_stream.restype = ctypes.c_void_p
     L.tebd_two_site_op_noalloc.argtypes = [ctypes.c_int] * 4 + [vp, vp, vp, dp, vp]
+    L.tebd_single_site_rho.argtypes = [vp, dp]
+    L.tebd_one_site_expval.argtypes = [vp, dp, dp]
+    L.tebd_one_site_expval_r.argtypes = [vp, dp, dp]
+    L.tebd_two_site_rho.argtypes = [vp, ctypes.c_int, dp]
+    L.tebd_local_energy.argtypes = [vp, ctypes.c_int, ctypes.POINTER(dp), dp]
+    L.tebd_total_energy.argtypes = [vp, ctypes.c_int, ctypes.POINTER(dp), dp]
+    L.tebd_inner_product.argtypes = [vp, vp, dp]
+    L.tebd_chain_entropy.argtypes = [vp, dp]
     _lib = L
     return L
 
@@ -344,6 +354,66 @@ class Chain:
     def reset_stats(self):
         self._check(self._lib.tebd_reset_stats(self.h))
 
+    # -- observables on the device (observables_module.f90) ----------------------
+    def single_site_rho(self):
+        """SingleSiteDensityMatrix: (L, d, d) complex, rho[s-1] for site s."""
+        r = np.zeros((self.L, self.d, self.d), dtype=np.complex128)
+        buf = np.zeros(self.L * self.d * self.d, dtype=np.complex128)
+        self._check(self._lib.tebd_single_site_rho(self.h, _dp(buf)))
+        for s in range(self.L):
+            r[s] = buf[s * self.d ** 2:(s + 1) * self.d ** 2].reshape(self.d, self.d, order="F")
+        return r
+
+    def one_site_expval(self, op):
+        """OneSiteExpVal: Tr(Op rho_s) for s = 1..L (complex Op -> complex, real Op -> real)."""
+        op = np.asarray(op)
+        if np.iscomplexobj(op):
+            o = np.asfortranarray(op, dtype=np.complex128)
+            out = np.zeros(self.L, dtype=np.complex128)
+            self._check(self._lib.tebd_one_site_expval(self.h, _dp(o), _dp(out)))
+        else:
+            o = np.asfortranarray(op, dtype=np.float64)
+            out = np.zeros(self.L)
+            self._check(self._lib.tebd_one_site_expval_r(self.h, _dp(o), _dp(out)))
+        return out
+
+    def two_site_rho(self, link):
+        """TwoSiteRho on sites link, link+1: (d^2, d^2), rows (i-1)*d+j as the gates."""
+        r = np.zeros((self.d ** 2, self.d ** 2), dtype=np.complex128, order="F")
+        self._check(self._lib.tebd_two_site_rho(self.h, link, _dp(r)))
+        return r
+
+    def _bond_ops(self, H):
+        hs = [np.asfortranarray(h, dtype=np.complex128) for h in H]
+        arr = (ctypes.POINTER(ctypes.c_double) * len(hs))(*[_dp(h) for h in hs])
+        return hs, arr
+
+    def local_energy(self, H):
+        """LocalEnergy: Re Tr(H(l) rho2(l)) for bonds l = 1..L-1 (H[l-1] is H(l))."""
+        hs, arr = self._bond_ops(H)
+        out = np.zeros(self.L - 1)
+        self._check(self._lib.tebd_local_energy(self.h, len(hs), arr, _dp(out)))
+        return out
+
+    def total_energy(self, H):
+        """TotalEnergy (open boundary)."""
+        hs, arr = self._bond_ops(H)
+        out = np.zeros(1)
+        self._check(self._lib.tebd_total_energy(self.h, len(hs), arr, _dp(out)))
+        return float(out[0])
+
+    def inner_product(self, other):
+        """InnerProduct(self, other) = <self|other>."""
+        out = np.zeros(1, dtype=np.complex128)
+        self._check(self._lib.tebd_inner_product(self.h, other.h, _dp(out)))
+        return complex(out[0])
+
+    def chain_entropy(self):
+        """ChainEntropy(link) for links 1..L+1 (entropy in base d, as the reference)."""
+        out = np.zeros(self.L + 1)
+        self._check(self._lib.tebd_chain_entropy(self.h, _dp(out)))
+        return out
+
     def stream(self):
         """The handle's cudaStream_t as an integer."""
         return int(self._lib.tebd_get_stream(self.h) or 0)
@@ -377,3 +447,28 @@ def TwoSiteOpNC(link, Op2, chain: Chain) -> float:
 def TrotterStep(Udt, chain: Chain, order=2) -> float:
     """propagation_module.f90 TrotterStep / TrotterStepNC (BoundaryCond='O')."""
     return chain.trotter_step(Udt, order)
+
+
+def OneSiteExpVal(Op, chain: Chain):
+    """OneSiteExpVal(expList, Op, Gammas, Lambdas) on the GPU: returns expList."""
+    return chain.one_site_expval(Op)
+
+
+def TotalEnergy(H, chain: Chain) -> float:
+    """TotalEnergy(energy, H, Gammas, Lambdas), open boundary: returns energy."""
+    return chain.total_energy(H)
+
+
+def LocalEnergy(H, chain: Chain):
+    """LocalEnergy(energy, H, Gammas, Lambdas), open boundary: returns energy(1:L-1)."""
+    return chain.local_energy(H)
+
+
+def InnerProduct(chain_left: Chain, chain_right: Chain) -> complex:
+    """InnerProduct(GammasL, LambdasL, GammasR, LambdasR)."""
+    return chain_left.inner_product(chain_right)
+
+
+def ChainEntropy(link, chain: Chain) -> float:
+    """ChainEntropy(link, Lambdas)."""
+    return float(chain.chain_entropy()[link - 1])

@@ -7,7 +7,7 @@ numpy restatements of the reference's observables (VidalCore_v_2.0/observables_m
 * :func:`two_site_rho`     -- ThetaKernal + TwoSiteRho for neighbouring sites (:704-835)
 * :func:`bond_energy`      -- the per-bond term of TotalEnergy (:1432-1466)
 * :func:`inner_product`    -- InnerProduct (:1031-1089)
-* :func:`chain_entropy`    -- von Neumann entropy of each Lambda (ChainEntropy, :1583)
+* :func:`chain_entropy`    -- entanglement entropy of each Lambda, base d (ChainEntropy, :1583)
 
 Gamma arrays are (chi, d, chi) complex, Lambdas (chi,) real, all 0-based lists.
 """
@@ -52,18 +52,27 @@ def bond_energy(gammas, lambdas, H):
 
 
 def inner_product(gL, lL, gR, lR):
-    """<psi_L|psi_R> by left-to-right transfer matrices of A_s = Gamma_s Lambda_{s+1}."""
-    E = np.outer(lL[0], lR[0]).astype(complex)
+    """<psi_L|psi_R> as InnerProduct computes it: transfer matrices of A_s = Gamma_s
+    Lambda_{s+1}, started from left index 1 of site 1 and closed on right index 1 of
+    site L, without the edge Lambdas themselves (they are e_1 for open chains)."""
+    chi = gL[0].shape[0]
+    E = np.zeros((chi, chi), complex)
+    E[0, 0] = 1.0
+    e1 = np.zeros(chi)
+    e1[0] = 1.0
     for s in range(len(gL)):
-        aL = gL[s] * lL[s + 1][None, None, :]
-        aR = gR[s] * lR[s + 1][None, None, :]
+        last = s == len(gL) - 1
+        aL = gL[s] * (e1 if last else lL[s + 1])[None, None, :]
+        aR = gR[s] * (e1 if last else lR[s + 1])[None, None, :]
         E = np.einsum("ab,aic,bid->cd", E, aL.conj(), aR, optimize=True)
-    return E.sum()
+    return E[0, 0]
 
 
-def chain_entropy(lambdas):
+def chain_entropy(lambdas, d):
+    """ChainEntropy(link) for every link: -sum_{lambda != 0} lambda^2 ln|lambda^2| / ln(d)
+    (observables_module.f90:1583-1602; the reference divides by LOG(localSize))."""
     out = []
     for l in lambdas:
-        p = l[l > 0] ** 2
-        out.append(float(-(p * np.log(p)).sum()))
+        p = l[l != 0] ** 2
+        out.append(float(-(p * np.log(np.abs(p))).sum() / np.log(d)))
     return np.array(out)
