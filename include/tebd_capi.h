@@ -124,9 +124,10 @@ int tebd_apply_bonds(tebd_handle *h, int nbonds, const int *links, const double 
 int tebd_trotter_step(tebd_handle *h, int order, int n_gates, const double *const *gates,
                       double *total_truncerr);
 
-/* All d*chi singular values of the normalised Theta from the last update of
- * `link` (descending; NC mode: the flattened block values in the reference's
- * order).  *count receives how many were written (buffer holds d*chi). */
+/* Singular values of the normalised Theta from the last update of `link`
+ * (descending; NC mode: the flattened block values in the reference's order).
+ * *count receives how many were written: all d*chi (zeros included) on the
+ * Jacobi routes, the chi kept ones on the bidiagonal route; the buffer holds d*chi. */
 int tebd_get_singular_values(tebd_handle *h, int link, double *sigma, int *count);
 
 /* Jacobi sweeps used by the last update of `link` (diagnostics). */
@@ -198,6 +199,28 @@ int tebd_local_energy(tebd_handle *h, int n_ops, const double *const *H, double 
 int tebd_total_energy(tebd_handle *h, int n_ops, const double *const *H, double *energy);
 int tebd_inner_product(tebd_handle *left, tebd_handle *right, double *value);
 int tebd_chain_entropy(tebd_handle *h, double *entropy);
+
+/* Chain state I/O in the reference's record formats (ToolsCore_v_2.0/io_module.f90),
+ * for checkpoints shared with a Fortran host.  kind 'S': Fortran E30.15 text,
+ * 15 significant digits; 'B': B80, the exact bit pattern in binary.  Files are
+ * named by path (the reference passes open units); append != 0 appends as the
+ * reference's openKind 'A' does, else the file is created or truncated.
+ *   tebd_record_lambdas   RecordLambdas (:191-220): L+1 records of chi values
+ *   tebd_record_gammas    RecordGammas (:222-264): per site, left index, right index a
+ *                         record of the d real parts; then the imaginary parts
+ *   tebd_record_labels    RecordLabel (:267-287) of LabelLeft and of LabelRight (NC mode;
+ *                         either path may be NULL), I16
+ *   tebd_read_gamma_lambda         readGammaLambda (:289-373): records of chi_now values
+ *                                  (chi_now <= chi); entries beyond chi_now are kept
+ *   tebd_read_gamma_lambda_labels  readGammaLambdaLabels (:376-472), NC mode */
+int tebd_record_lambdas(tebd_handle *h, const char *path, char kind, int append);
+int tebd_record_gammas(tebd_handle *h, const char *path, char kind, int append);
+int tebd_record_labels(tebd_handle *h, const char *path_left, const char *path_right);
+int tebd_read_gamma_lambda(tebd_handle *h, const char *lambda_path, const char *gamma_path, char kind,
+                           int chi_now);
+int tebd_read_gamma_lambda_labels(tebd_handle *h, const char *lambda_path, const char *gamma_path,
+                                  const char *label_left_path, const char *label_right_path, char kind,
+                                  int chi_now);
 
 /* Allocation-free dense update of bond `link` of a chain the caller already
  * holds in device memory.  No counterpart in the reference: it exists for

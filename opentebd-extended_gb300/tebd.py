@@ -65,6 +65,8 @@ EXPORTED_SYMBOLS = (
     "tebd_reset_stats", "tebd_measure_fp64_peak", "tebd_get_stream", "tebd_two_site_op_noalloc",
     "tebd_single_site_rho", "tebd_one_site_expval", "tebd_one_site_expval_r", "tebd_two_site_rho",
     "tebd_local_energy", "tebd_total_energy", "tebd_inner_product", "tebd_chain_entropy",
+    "tebd_record_lambdas", "tebd_record_gammas", "tebd_record_labels", "tebd_read_gamma_lambda",
+    "tebd_read_gamma_lambda_labels",
 )
 
 
@@ -168,6 +170,12 @@ def load_library(path: str = LIB_PATH):
     L.tebd_total_energy.argtypes = [vp, ctypes.c_int, ctypes.POINTER(dp), dp]
     L.tebd_inner_product.argtypes = [vp, vp, dp]
     L.tebd_chain_entropy.argtypes = [vp, dp]
+    cp = ctypes.c_char_p
+    L.tebd_record_lambdas.argtypes = [vp, cp, ctypes.c_char, ctypes.c_int]
+    L.tebd_record_gammas.argtypes = [vp, cp, ctypes.c_char, ctypes.c_int]
+    L.tebd_record_labels.argtypes = [vp, cp, cp]
+    L.tebd_read_gamma_lambda.argtypes = [vp, cp, cp, ctypes.c_char, ctypes.c_int]
+    L.tebd_read_gamma_lambda_labels.argtypes = [vp, cp, cp, cp, cp, ctypes.c_char, ctypes.c_int]
     _lib = L
     return L
 
@@ -407,6 +415,31 @@ class Chain:
         out = np.zeros(1, dtype=np.complex128)
         self._check(self._lib.tebd_inner_product(self.h, other.h, _dp(out)))
         return complex(out[0])
+
+    # -- state I/O in the reference's record formats (io_module.f90) ------------
+    def record_lambdas(self, path, kind="S", append=False):
+        """RecordLambdas: kind 'S' (E30.15) or 'B' (B80, exact)."""
+        self._check(self._lib.tebd_record_lambdas(self.h, os.fsencode(path), kind.encode(), int(append)))
+
+    def record_gammas(self, path, kind="S", append=False):
+        """RecordGammas: real parts, then imaginary parts, one record per (site, alpha, beta)."""
+        self._check(self._lib.tebd_record_gammas(self.h, os.fsencode(path), kind.encode(), int(append)))
+
+    def record_labels(self, path_left=None, path_right=None):
+        """RecordLabel of LabelLeft and LabelRight (NC mode)."""
+        self._check(self._lib.tebd_record_labels(self.h, None if path_left is None else os.fsencode(path_left),
+                                                 None if path_right is None else os.fsencode(path_right)))
+
+    def read_gamma_lambda(self, lambda_path, gamma_path, kind="S", chi_now=None):
+        """readGammaLambda into this chain (records of chi_now values; default chi)."""
+        self._check(self._lib.tebd_read_gamma_lambda(self.h, os.fsencode(lambda_path), os.fsencode(gamma_path),
+                                                     kind.encode(), chi_now or self.chi))
+
+    def read_gamma_lambda_labels(self, lambda_path, gamma_path, left_path, right_path, kind="S", chi_now=None):
+        """readGammaLambdaLabels into this chain (NC mode)."""
+        self._check(self._lib.tebd_read_gamma_lambda_labels(
+            self.h, os.fsencode(lambda_path), os.fsencode(gamma_path), os.fsencode(left_path),
+            os.fsencode(right_path), kind.encode(), chi_now or self.chi))
 
     def chain_entropy(self):
         """ChainEntropy(link) for links 1..L+1 (entropy in base d, as the reference)."""
