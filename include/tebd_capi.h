@@ -124,6 +124,22 @@ int tebd_apply_bonds(tebd_handle *h, int nbonds, const int *links, const double 
 int tebd_trotter_step(tebd_handle *h, int order, int n_gates, const double *const *gates,
                       double *total_truncerr);
 
+/* Swapping(link, truncerr, Gammas, Lambdas) (local_operations_module.f90:651-689):
+ * exchange the physical indices of sites link and link+1 (SwapTheta), SVD of the
+ * unnormalised Theta, FormLambda1/FormGamma1/FormGamma2.  Dense mode. */
+int tebd_swapping(tebd_handle *h, int link, double *truncerr);
+
+/* TrotterStep2ndOrderPBC (propagation_module.f90:116-198), dense mode, order 2:
+ * gates[g-1] = Udt(g), g = 1..L (n_gates >= L), Udt(L) the edge bond applied on
+ * bond 1 after Swapping site L down to site 2 (and back).  The Forest-Ruth PBC
+ * step (TrotterStep5thOrderPBC) is not provided (order != 2 -> TEBD_ERR_ARG). */
+int tebd_trotter_step_pbc(tebd_handle *h, int order, int n_gates, const double *const *gates,
+                          double *total_truncerr);
+
+/* CanonicalFormAllNC (propagation_module.f90:1943-1983, no intDegFree): the
+ * identity TwoSiteOpNC on links 1..L-1 then L-1..1.  NC mode. */
+int tebd_canonical_form_all_nc(tebd_handle *h);
+
 /* Singular values of the normalised Theta from the last update of `link`
  * (descending; NC mode: the flattened block values in the reference's order).
  * *count receives how many were written: all d*chi (zeros included) on the

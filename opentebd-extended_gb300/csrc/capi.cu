@@ -459,6 +459,7 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
       if (nbd < nb && (rc = run_qrj(h, nb, nmax))) return rc;
       if (nbd > 0 && (rc = run_bidiag(h, nb, nbd_max))) return rc;
     }
+    if (h->unnormalized && (rc = launch_unit_norm(h, nb))) return rc;
     if ((rc = launch_dense_finish(h, nb))) return rc;
   } else {
     if ((rc = run_nc_batch(h, nb, links, nullptr))) return rc;
@@ -600,3 +601,104 @@ extern "C" int tebd_measure_fp64_peak(int device, double *tflops) {
 }
 
 extern "C" void *tebd_get_stream(tebd_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+// ---------------------------------------------------------------------------
+// Swapping, the periodic-boundary Trotter step, CanonicalFormAllNC
+// ---------------------------------------------------------------------------
+// SWAP in the gates' order: Op2((i-1)d+j, (k-1)d+l) = delta(i,l) delta(j,k)
+static std::vector<double> swap_gate(int d) {
+  const int d2 = d * d;
+  std::vector<double> g((size_t)2 * d2 * d2, 0.0);
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < d; ++j) g[2 * ((size_t)(i * d + j) + (size_t)d2 * (j * d + i))] = 1.0;
+  return g;
+}
+
+// Swapping (local_operations_module.f90:651-689): SwapTheta exchanges the two
+// physical indices of the unnormalised Theta, which equals applying SWAP as the
+// gate; the SVD then runs without ReshapeTheta's 1/||Theta||, as Swapping calls
+// SVDTruncation directly (truncerr = |1 - sum of kept S^2| of the raw Theta).
+extern "C" int tebd_swapping(tebd_handle *h, int link, double *truncerr) {
+  if (!h || !truncerr) return TEBD_ERR_ARG;
+  if (h->mode != TEBD_MODE_DENSE) return set_error(h, TEBD_ERR_STATE, "Swapping needs a TEBD_MODE_DENSE handle");
+  const std::vector<double> g = swap_gate(h->d);
+  const double *gp = g.data();
+  h->unnormalized = 1;
+  const int rc = apply_bonds_impl(h, 1, &link, &gp, truncerr);
+  h->unnormalized = 0;
+  return rc;
+}
+
+// TrotterStep2ndOrderPBC (propagation_module.f90:116-198): gates[g-1] = Udt(g),
+// g = 1..L, Udt(L) the edge gate.  Site L is swapped down to position 2, the
+// edge gate acts on bond 1 and the swaps are undone; truncation errors of every
+// update and swap are summed in the reference's order.
+extern "C" int tebd_trotter_step_pbc(tebd_handle *h, int order, int n_gates, const double *const *gates,
+                                     double *total_truncerr) {
+  if (!h || !gates || !total_truncerr) return TEBD_ERR_ARG;
+  if (h->mode != TEBD_MODE_DENSE) return set_error(h, TEBD_ERR_STATE, "the PBC Trotter step needs a dense handle");
+  if (order != 2) return set_error(h, TEBD_ERR_ARG, "periodic boundaries: only the 2nd-order step is provided");
+  const int L = h->L;
+  if (L < 3) return set_error(h, TEBD_ERR_ARG, "periodic boundaries need L >= 3");
+  if (n_gates < L) return set_error(h, TEBD_ERR_ARG, "periodic boundaries need L gates (Udt(L) = edge)");
+  double total = 0.0;
+  std::vector<int> links;
+  std::vector<const double *> gp;
+  std::vector<double> te;
+  auto sweep = [&](int first) -> int {  // bonds first, first+2, ... with Udt(link)
+    links.clear();
+    gp.clear();
+    for (int link = first; link <= L - 1; link += 2) {
+      links.push_back(link);
+      gp.push_back(gates[link - 1]);
+    }
+    te.assign(links.size(), 0.0);
+    const int rc = apply_bonds_impl(h, (int)links.size(), links.data(), gp.data(), te.data());
+    for (double v : te) total = total + v;
+    return rc;
+  };
+  auto swap = [&](int link) -> int {
+    double t = 0.0;
+    const int rc = tebd_swapping(h, link, &t);
+    total = total + t;
+    return rc;
+  };
+  int rc;
+  if ((rc = sweep(1))) return rc;
+  if (L % 2 == 1 && (rc = sweep(2))) return rc;
+  for (int i = L - 1; i >= 2; --i)
+    if ((rc = swap(i))) return rc;
+  {
+    double t = 0.0;
+    const double *ge = gates[L - 1];
+    const int link = 1;
+    if ((rc = apply_bonds_impl(h, 1, &link, &ge, &t))) return rc;
+    total = total + t;
+  }
+  for (int i = 2; i <= L - 1; ++i)
+    if ((rc = swap(i))) return rc;
+  if ((rc = sweep(2))) return rc;
+  if ((rc = sweep(1))) return rc;
+  *total_truncerr = total;
+  return TEBD_OK;
+}
+
+// CanonicalFormAllNC (propagation_module.f90:1943-1983, no internal degrees of
+// freedom): TwoSiteOpNC with the identity gate on links 1..L-1, then L-1..1, one
+// bond at a time (each depends on the previous one).
+extern "C" int tebd_canonical_form_all_nc(tebd_handle *h) {
+  if (!h) return TEBD_ERR_ARG;
+  if (h->mode != TEBD_MODE_NC) return set_error(h, TEBD_ERR_STATE, "CanonicalFormAllNC needs a TEBD_MODE_NC handle");
+  const int d2 = h->d * h->d;
+  std::vector<double> eye((size_t)2 * d2 * d2, 0.0);
+  for (int k = 0; k < d2; ++k) eye[2 * ((size_t)k + (size_t)d2 * k)] = 1.0;
+  const double *gp = eye.data();
+  for (int pass = 0; pass < 2; ++pass)
+    for (int q = 1; q <= h->L - 1; ++q) {
+      const int link = pass == 0 ? q : h->L - q;
+      double t = 0.0;
+      const int rc = apply_bonds_impl(h, 1, &link, &gp, &t);
+      if (rc) return rc;
+    }
+  return TEBD_OK;
+}

@@ -409,6 +409,20 @@ int launch_dense_prepare(tebd_handle *h, int nb, bool /*real_gate: converted on 
   return check_cuda(h, cudaGetLastError(), "dense prepare launch");
 }
 
+// Swapping decomposes Theta without ReshapeTheta's normalisation: once the SVD
+// (which used the true norm for its negligible-column floor) is done, the norm
+// seen by the sort, FormLambda1 and the restores is set to 1.
+__global__ void k_unit_norm(double *nrm, int nb) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nb) nrm[s] = 1.0;
+}
+
+int launch_unit_norm(tebd_handle *h, int nb) {
+  k_unit_norm<<<cdiv(nb, 128), 128, 0, h->stream>>>(h->nrm, nb);
+  TEBD_LAUNCHED(h);
+  return check_cuda(h, cudaGetLastError(), "unit norm launch");
+}
+
 int launch_eye(tebd_handle *h, int nb) {
   const size_t total = (size_t)h->n * h->n;
   unsigned gx = cdiv(total, 256);

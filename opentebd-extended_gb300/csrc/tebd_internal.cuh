@@ -167,6 +167,7 @@ struct tebd_handle {
   // diagnostics
   tebd_stats stats;
   int profiling;
+  int unnormalized;        // 1 while Swapping runs: Theta is decomposed without 1/||Theta||
   cudaEvent_t ev[6];
 };
 
@@ -181,6 +182,7 @@ int run_jacobi(tebd_handle *h, int nb, int svd_mode, int nmax);
 int dense_compact_sizes(tebd_handle *h, int nb, int *nmax, std::vector<Compact> *out);
 int launch_dense_finish(tebd_handle *h, int nb);
 int launch_eye(tebd_handle *h, int nb);
+int launch_unit_norm(tebd_handle *h, int nb);
 int run_jacobi_problems(tebd_handle *h, const JacobiProblem<double> *probs_d, int nprob, int nmax);
 int jacobi_persistent_double(tebd_handle *h, const JacobiProblem<double> *probs_d, int nprob,
                              int nmax, double tol, int max_sweeps);

@@ -66,7 +66,7 @@ EXPORTED_SYMBOLS = (
     "tebd_single_site_rho", "tebd_one_site_expval", "tebd_one_site_expval_r", "tebd_two_site_rho",
     "tebd_local_energy", "tebd_total_energy", "tebd_inner_product", "tebd_chain_entropy",
     "tebd_record_lambdas", "tebd_record_gammas", "tebd_record_labels", "tebd_read_gamma_lambda",
-    "tebd_read_gamma_lambda_labels",
+    "tebd_read_gamma_lambda_labels", "tebd_swapping", "tebd_trotter_step_pbc", "tebd_canonical_form_all_nc",
 )
 
 
@@ -170,6 +170,9 @@ def load_library(path: str = LIB_PATH):
     L.tebd_total_energy.argtypes = [vp, ctypes.c_int, ctypes.POINTER(dp), dp]
     L.tebd_inner_product.argtypes = [vp, vp, dp]
     L.tebd_chain_entropy.argtypes = [vp, dp]
+    L.tebd_swapping.argtypes = [vp, ctypes.c_int, dp]
+    L.tebd_trotter_step_pbc.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(dp), dp]
+    L.tebd_canonical_form_all_nc.argtypes = [vp]
     cp = ctypes.c_char_p
     L.tebd_record_lambdas.argtypes = [vp, cp, ctypes.c_char, ctypes.c_int]
     L.tebd_record_gammas.argtypes = [vp, cp, ctypes.c_char, ctypes.c_int]
@@ -333,6 +336,24 @@ class Chain:
         te = np.zeros(1)
         self._check(self._lib.tebd_trotter_step(self.h, order, len(gs), arr, _dp(te)))
         return float(te[0])
+
+    def swapping(self, link):
+        """Swapping(link): exchange the physical indices of sites link, link+1; truncerr."""
+        te = np.zeros(1)
+        self._check(self._lib.tebd_swapping(self.h, link, _dp(te)))
+        return float(te[0])
+
+    def trotter_step_pbc(self, Udt):
+        """TrotterStep2ndOrderPBC; Udt[g-1] = Udt(g), g = 1..L, Udt(L) the edge bond."""
+        gs = [_as_gate(g, self.d) for g in Udt]
+        arr = (ctypes.POINTER(ctypes.c_double) * len(gs))(*[_dp(g) for g in gs])
+        te = np.zeros(1)
+        self._check(self._lib.tebd_trotter_step_pbc(self.h, 2, len(gs), arr, _dp(te)))
+        return float(te[0])
+
+    def canonical_form_all_nc(self):
+        """CanonicalFormAllNC: identity TwoSiteOpNC sweeps forward and back."""
+        self._check(self._lib.tebd_canonical_form_all_nc(self.h))
 
     def singular_values(self, link):
         s = np.zeros(self.d * self.chi)

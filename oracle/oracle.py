@@ -72,6 +72,8 @@ def lib():
     L.oracle_two_site_op.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp]
     L.oracle_two_site_op_nc.argtypes = [ctypes.c_int] * 4 + [dp] * 7 + [ip] * 4 + [dp, dp, ip]
     L.oracle_trotter_step.argtypes = [ctypes.c_int] * 4 + [ctypes.POINTER(dp)] * 3 + [dp]
+    L.oracle_swapping.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp]
+    L.oracle_trotter_step_pbc.argtypes = [ctypes.c_int] * 3 + [ctypes.POINTER(dp)] * 3 + [dp]
     L.oracle_trotter_step_nc.argtypes = (
         [ctypes.c_int] * 6 + [ctypes.POINTER(dp)] * 2 + [ctypes.POINTER(ip)] * 2 + [ctypes.POINTER(dp), dp]
     )
@@ -173,6 +175,34 @@ def trotter_step(gammas, lambdas, gates, order=2):
                                    _ptr_array(lambdas, ctypes.c_double),
                                    _ptr_array(gts, ctypes.c_double), _dptr(te))
     _check(st, "oracle_trotter_step")
+    return float(te[0])
+
+
+def swapping(gamma1, gamma2, lam0, lam1, lam2):
+    """Swapping on one bond (unnormalised Theta with its physical indices exchanged).
+    Returns ``(gamma1', gamma2', lam1', truncerr)`` without touching the inputs."""
+    chi, d, _ = gamma1.shape
+    g1 = _fcomplex(gamma1, (chi, d, chi)).copy(order="F")
+    g2 = _fcomplex(gamma2, (chi, d, chi)).copy(order="F")
+    l0 = np.ascontiguousarray(lam0, dtype=np.float64)
+    l1 = np.array(lam1, dtype=np.float64)
+    l2 = np.ascontiguousarray(lam2, dtype=np.float64)
+    te = np.zeros(1)
+    st = lib().oracle_swapping(chi, d, _dptr(g1), _dptr(g2), _dptr(l0), _dptr(l1), _dptr(l2), _dptr(te))
+    _check(st, "oracle_swapping")
+    return g1, g2, l1, float(te[0])
+
+
+def trotter_step_pbc(gammas, lambdas, gates):
+    """TrotterStep2ndOrderPBC in place; gates[g-1] = Udt(g), g = 1..L (Udt(L): bond L-1)."""
+    L = len(gammas)
+    chi, d, _ = gammas[0].shape
+    gts = [np.asfortranarray(g, dtype=np.complex128) for g in gates]
+    te = np.zeros(1)
+    st = lib().oracle_trotter_step_pbc(L, chi, d, _ptr_array(gammas, ctypes.c_double),
+                                       _ptr_array(lambdas, ctypes.c_double),
+                                       _ptr_array(gts, ctypes.c_double), _dptr(te))
+    _check(st, "oracle_trotter_step_pbc")
     return float(te[0])
 
 

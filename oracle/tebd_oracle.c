@@ -224,6 +224,44 @@ int oracle_two_site_op(int chi, int d, double *g1_, double *g2_, const double *l
   return st;
 }
 
+/* Swapping (:651-689): Theta without a gate or normalisation, physical indices
+ * exchanged by SwapTheta (:624-648): ThetaSW((j-1)chi+alpha, (i-1)chi+gamma) =
+ * Theta(alpha,i,j,gamma); then SVDTruncation, FormLambda1, FormGamma1/2. */
+int oracle_swapping(int chi, int d, double *g1_, double *g2_, const double *l0, double *l1,
+                    const double *l2, double *truncerr) {
+  if (chi < 1 || d < 1) return OR_ERR_ARG;
+  zc *g1 = (zc *)g1_, *g2 = (zc *)g2_;
+  const int n = chi * d;
+  const size_t nn = (size_t)n * n;
+  zc *theta = (zc *)malloc(sizeof(zc) * nn);
+  zc *sw = (zc *)malloc(sizeof(zc) * nn);
+  zc *u = (zc *)malloc(sizeof(zc) * nn);
+  zc *vt = (zc *)malloc(sizeof(zc) * nn);
+  double *s = (double *)malloc(sizeof(double) * n);
+  int st = OR_ERR_ALLOC;
+  if (theta && sw && u && vt && s) {
+    form_theta(chi, d, theta, l0, g1, l1, g2, l2);
+    for (int a = 0; a < chi; ++a)
+      for (int g = 0; g < chi; ++g)
+        for (int i = 0; i < d; ++i)
+          for (int j = 0; j < d; ++j)
+            sw[((size_t)j * chi + a) + (size_t)n * ((size_t)i * chi + g)] =
+                theta[a + (size_t)chi * (i + (size_t)d * (j + (size_t)d * g))];
+    st = zgesvd_all(n, n, sw, s, u, vt, 5 * n, 5 * n);
+    if (st == OR_OK) {
+      form_lambda1(chi, l1, truncerr, s);
+      form_gamma1(chi, d, l0, g1, u);
+      form_gamma2(chi, d, g2, l2, vt);
+    }
+  }
+  free(theta);
+  free(sw);
+  free(u);
+  free(vt);
+  free(s);
+  return st;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Number-conserving update (U(1) labels, no internal degrees of freedom)     */
 /* ------------------------------------------------------------------------- */
@@ -620,6 +658,41 @@ int oracle_trotter_step_nc(int L, int chi, int d, int totNum, int maxFilling, in
       if (st != OR_OK) return st;
       tot += te;
     }
+  *total_truncerr = tot;
+  return OR_OK;
+}
+
+/* TrotterStep2ndOrderPBC (propagation_module.f90:116-198): gates[g-1] = Udt(g),
+ * g = 1..L, Udt(L) the edge bond (L,1) applied on bond 1 after swapping site L
+ * down to site 2. */
+int oracle_trotter_step_pbc(int L, int chi, int d, double **gammas, double **lambdas,
+                            const double *const *gates, double *total_truncerr) {
+  double tot = 0.0, te = 0.0;
+  int st;
+#define OP(link, g)                                                                              \
+  do {                                                                                           \
+    st = oracle_two_site_op(chi, d, gammas[(link)-1], gammas[(link)], lambdas[(link)-1],         \
+                            lambdas[(link)], lambdas[(link) + 1], gates[(g)-1], 0, &te, 0);      \
+    if (st != OR_OK) return st;                                                                  \
+    tot += te;                                                                                   \
+  } while (0)
+#define SW(link)                                                                                 \
+  do {                                                                                           \
+    st = oracle_swapping(chi, d, gammas[(link)-1], gammas[(link)], lambdas[(link)-1],            \
+                         lambdas[(link)], lambdas[(link) + 1], &te);                             \
+    if (st != OR_OK) return st;                                                                  \
+    tot += te;                                                                                   \
+  } while (0)
+  for (int i = 1; i <= L - 1; i += 2) OP(i, i);
+  if (L % 2 == 1)
+    for (int i = 2; i <= L - 1; i += 2) OP(i, i);
+  for (int i = L - 1; i >= 2; --i) SW(i);
+  OP(1, L);
+  for (int i = 2; i <= L - 1; ++i) SW(i);
+  for (int i = 2; i <= L - 1; i += 2) OP(i, i);
+  for (int i = 1; i <= L - 1; i += 2) OP(i, i);
+#undef OP
+#undef SW
   *total_truncerr = tot;
   return OR_OK;
 }

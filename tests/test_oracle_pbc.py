@@ -1,0 +1,64 @@
+"""Known answers for the oracle's Swapping and periodic-boundary Trotter step."""
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def H(pkg):
+    return pkg.hamiltonians
+
+
+def _canonical_chain(H, oracle, L=6, d=2, chi=8, seed=4):
+    rng = np.random.default_rng(seed)
+    c0 = rng.standard_normal((d, L)) + 1j * rng.standard_normal((d, L))
+    c0 /= np.linalg.norm(c0, axis=0)
+    gam, lam = H.product_state(c0, chi)
+    U = H.construct_propagators(H.heisenberg(L, 1.0, 1.0, 0.3), 0.1, 2)
+    for _ in range(3):
+        oracle.trotter_step(gam, lam, U, 2)
+    return gam, lam
+
+
+def test_swapping_is_the_swap_gate_on_a_normalised_state(oracle, H):
+    from oracle import observables as obs
+    gam, lam = _canonical_chain(H, oracle)
+    d = 2
+    swap = np.zeros((d * d, d * d), complex)
+    for i in range(d):
+        for j in range(d):
+            swap[i * d + j, j * d + i] = 1.0
+    a = oracle.swapping(gam[2], gam[3], lam[2], lam[3], lam[4])
+    b = oracle.two_site_op(gam[2], gam[3], lam[2], lam[3], lam[4], swap)
+    assert np.allclose(a[2], b[2], atol=1e-13) and abs(a[3] - b[3]) < 1e-13
+    ra = obs.two_site_rho(lam[2], a[0], a[2], a[1], lam[4])
+    rb = obs.two_site_rho(lam[2], b[0], b[2], b[1], lam[4])
+    assert np.allclose(ra, rb, atol=1e-13)
+
+
+def test_swap_twice_restores_the_chain(oracle, H):
+    from oracle import observables as obs
+    gam, lam = _canonical_chain(H, oracle)
+    ref = ([g.copy(order="F") for g in gam], [l.copy() for l in lam])
+    for _ in range(2):
+        g1, g2, l1, te = oracle.swapping(gam[1], gam[2], lam[1], lam[2], lam[3])
+        gam[1], gam[2], lam[2] = g1, g2, l1
+        assert te < 1e-12
+    assert np.allclose(lam[2], ref[1][2], atol=1e-13)
+    assert abs(abs(obs.inner_product(ref[0], ref[1], gam, lam)) - 1.0) < 1e-12
+
+
+def test_pbc_step_on_a_product_gate_ring(oracle, H):
+    """Product gates (no entanglement) on a ring: the PBC step applies each local
+    factor once, so a product state stays a product state of the expected spinors."""
+    L, d, chi = 5, 2, 4
+    rng = np.random.default_rng(1)
+    c0 = rng.standard_normal((d, L)) + 1j * rng.standard_normal((d, L))
+    c0 /= np.linalg.norm(c0, axis=0)
+    gam, lam = H.product_state(c0, chi)
+    phase = np.diag(np.exp(1j * np.array([0.3, -0.3])))
+    eye = np.eye(d)
+    gates = [np.kron(phase, eye) for _ in range(L - 1)] + [np.kron(eye, eye)]
+    te = oracle.trotter_step_pbc(gam, lam, gates)
+    assert te < 1e-12
+    for l in lam:
+        assert abs(l[0] - 1.0) < 1e-12 and np.all(np.abs(l[1:]) < 1e-12)
