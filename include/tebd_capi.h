@@ -136,6 +136,14 @@ int tebd_swapping(tebd_handle *h, int link, double *truncerr);
 int tebd_trotter_step_pbc(tebd_handle *h, int order, int n_gates, const double *const *gates,
                           double *total_truncerr);
 
+/* CanonicalForm(Lambda0, Gamma1, Lambda1, Gamma2, Lambda2) on bond `link`
+ * (local_operations_module.f90:496-610) and CanonicalFormAll (propagation_module.f90:
+ * 617-634: links 1..L-1 then L-1..1), dense mode: the Schmidt bases of the bond are
+ * re-orthogonalised from the chi x chi overlap matrices of the two sides (three
+ * chi x chi SVDs, thresholds 1e-8 as the reference). */
+int tebd_canonical_form(tebd_handle *h, int link);
+int tebd_canonical_form_all(tebd_handle *h);
+
 /* CanonicalFormAllNC (propagation_module.f90:1943-1983, no intDegFree): the
  * identity TwoSiteOpNC on links 1..L-1 then L-1..1.  NC mode. */
 int tebd_canonical_form_all_nc(tebd_handle *h);

@@ -67,6 +67,7 @@ EXPORTED_SYMBOLS = (
     "tebd_local_energy", "tebd_total_energy", "tebd_inner_product", "tebd_chain_entropy",
     "tebd_record_lambdas", "tebd_record_gammas", "tebd_record_labels", "tebd_read_gamma_lambda",
     "tebd_read_gamma_lambda_labels", "tebd_swapping", "tebd_trotter_step_pbc", "tebd_canonical_form_all_nc",
+    "tebd_canonical_form", "tebd_canonical_form_all",
 )
 
 
@@ -173,6 +174,8 @@ def load_library(path: str = LIB_PATH):
     L.tebd_swapping.argtypes = [vp, ctypes.c_int, dp]
     L.tebd_trotter_step_pbc.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(dp), dp]
     L.tebd_canonical_form_all_nc.argtypes = [vp]
+    L.tebd_canonical_form.argtypes = [vp, ctypes.c_int]
+    L.tebd_canonical_form_all.argtypes = [vp]
     cp = ctypes.c_char_p
     L.tebd_record_lambdas.argtypes = [vp, cp, ctypes.c_char, ctypes.c_int]
     L.tebd_record_gammas.argtypes = [vp, cp, ctypes.c_char, ctypes.c_int]
@@ -350,6 +353,14 @@ class Chain:
         te = np.zeros(1)
         self._check(self._lib.tebd_trotter_step_pbc(self.h, 2, len(gs), arr, _dp(te)))
         return float(te[0])
+
+    def canonical_form(self, link):
+        """CanonicalForm on bond `link` (dense mode)."""
+        self._check(self._lib.tebd_canonical_form(self.h, link))
+
+    def canonical_form_all(self):
+        """CanonicalFormAll: CanonicalForm on links 1..L-1 then L-1..1 (dense mode)."""
+        self._check(self._lib.tebd_canonical_form_all(self.h))
 
     def canonical_form_all_nc(self):
         """CanonicalFormAllNC: identity TwoSiteOpNC sweeps forward and back."""

@@ -73,6 +73,7 @@ def lib():
     L.oracle_two_site_op_nc.argtypes = [ctypes.c_int] * 4 + [dp] * 7 + [ip] * 4 + [dp, dp, ip]
     L.oracle_trotter_step.argtypes = [ctypes.c_int] * 4 + [ctypes.POINTER(dp)] * 3 + [dp]
     L.oracle_swapping.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp]
+    L.oracle_canonical_form.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp]
     L.oracle_trotter_step_pbc.argtypes = [ctypes.c_int] * 3 + [ctypes.POINTER(dp)] * 3 + [dp]
     L.oracle_trotter_step_nc.argtypes = (
         [ctypes.c_int] * 6 + [ctypes.POINTER(dp)] * 2 + [ctypes.POINTER(ip)] * 2 + [ctypes.POINTER(dp), dp]
@@ -191,6 +192,27 @@ def swapping(gamma1, gamma2, lam0, lam1, lam2):
     st = lib().oracle_swapping(chi, d, _dptr(g1), _dptr(g2), _dptr(l0), _dptr(l1), _dptr(l2), _dptr(te))
     _check(st, "oracle_swapping")
     return g1, g2, l1, float(te[0])
+
+
+def canonical_form(lam0, gamma1, lam1, gamma2, lam2):
+    """CanonicalForm on one bond; returns ``(gamma1', lam1', gamma2')`` (inputs untouched)."""
+    chi, d, _ = gamma1.shape
+    g1 = _fcomplex(gamma1, (chi, d, chi)).copy(order="F")
+    g2 = _fcomplex(gamma2, (chi, d, chi)).copy(order="F")
+    l0 = np.ascontiguousarray(lam0, dtype=np.float64)
+    l1 = np.array(lam1, dtype=np.float64)
+    l2 = np.ascontiguousarray(lam2, dtype=np.float64)
+    st = lib().oracle_canonical_form(chi, d, _dptr(l0), _dptr(g1), _dptr(l1), _dptr(g2), _dptr(l2))
+    _check(st, "oracle_canonical_form")
+    return g1, l1, g2
+
+
+def canonical_form_all(gammas, lambdas):
+    """CanonicalFormAll in place: CanonicalForm on links 1..L-1, then L-1..1."""
+    L = len(gammas)
+    for k in list(range(1, L)) + list(range(L - 1, 0, -1)):
+        gammas[k - 1], lambdas[k], gammas[k] = canonical_form(lambdas[k - 1], gammas[k - 1], lambdas[k],
+                                                               gammas[k], lambdas[k + 1])
 
 
 def trotter_step_pbc(gammas, lambdas, gates):

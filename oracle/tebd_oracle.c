@@ -61,6 +61,7 @@ typedef void (*zgesvd_fn)(char *jobu, char *jobvt, int *m, int *n, zc *a, int *l
 static zgesvd_fn g_zgesvd = 0;
 
 #define GUARD_DENSE ((double)1e-15f) /* Fortran `1E-15` (default REAL)      */
+#define GUARD_CANON ((double)1e-8f)  /* CanonicalForm's `1E-8` (default REAL) */
 #define GUARD_NC ((double)1e-10f)    /* Fortran `10.0**(-10)` (default REAL) */
 #define LABEL_UNUSED 10000
 
@@ -259,6 +260,102 @@ int oracle_swapping(int chi, int d, double *g1_, double *g2_, const double *l0, 
   free(u);
   free(vt);
   free(s);
+  return st;
+}
+
+/* CanonicalForm (:496-610): loop for loop, with ZGESVD('A','A') on the chi x chi
+ * matrices (SVD :612-622; workspaces 5 chi as SVDInit :84-122 sets them). */
+int oracle_canonical_form(int chi, int d, const double *l0, double *g1_, double *l1, double *g2_,
+                          const double *l2) {
+  zc *g1 = (zc *)g1_, *g2 = (zc *)g2_;
+  const size_t cc = (size_t)chi * chi, gs = (size_t)chi * d * chi;
+  zc *M = (zc *)malloc(sizeof(zc) * cc), *X = (zc *)malloc(sizeof(zc) * cc), *Y = (zc *)malloc(sizeof(zc) * cc);
+  zc *U = (zc *)malloc(sizeof(zc) * cc), *VT = (zc *)malloc(sizeof(zc) * cc);
+  zc *g1t = (zc *)malloc(sizeof(zc) * gs), *g2t = (zc *)malloc(sizeof(zc) * gs);
+  double *S = (double *)malloc(sizeof(double) * chi);
+  int st = OR_ERR_ALLOC;
+  if (!(M && X && Y && U && VT && g1t && g2t && S)) goto done;
+#define G1(a, i, b) g1[(a) + (size_t)chi * ((i) + (size_t)d * (b))]
+#define G2(a, i, b) g2[(a) + (size_t)chi * ((i) + (size_t)d * (b))]
+#define T1(a, i, b) g1t[(a) + (size_t)chi * ((i) + (size_t)d * (b))]
+#define T2(a, i, b) g2t[(a) + (size_t)chi * ((i) + (size_t)d * (b))]
+#define MM(a, b) M[(a) + (size_t)chi * (b)]
+  for (int a = 0; a < chi; ++a)
+    for (int b = 0; b < chi; ++b) {
+      zc acc = 0.0;
+      for (int i = 0; i < d; ++i)
+        for (int g = 0; g < chi; ++g) acc = acc + conj(G1(g, i, a)) * l0[g] * l0[g] * G1(g, i, b);
+      MM(a, b) = acc;
+    }
+  if ((st = zgesvd_all(chi, chi, M, S, U, VT, 5 * chi, 5 * chi)) != OR_OK) goto done;
+  for (int a = 0; a < chi; ++a)
+    for (int b = 0; b < chi; ++b)
+      for (int i = 0; i < d; ++i) {
+        zc acc = 0.0;
+        if (S[b] > GUARD_CANON)
+          for (int g = 0; g < chi; ++g) acc = acc + G1(a, i, g) * U[g + (size_t)chi * b] * (1.0 / sqrt(S[b]));
+        T1(a, i, b) = acc;
+      }
+  for (int a = 0; a < chi; ++a)
+    for (int b = 0; b < chi; ++b) X[a + (size_t)chi * b] = sqrt(S[a]) * conj(U[b + (size_t)chi * a]);
+  for (int a = 0; a < chi; ++a)
+    for (int b = 0; b < chi; ++b) {
+      zc acc = 0.0;
+      for (int i = 0; i < d; ++i)
+        for (int g = 0; g < chi; ++g) acc = acc + G2(a, i, g) * l2[g] * l2[g] * conj(G2(b, i, g));
+      MM(a, b) = acc;
+    }
+  if ((st = zgesvd_all(chi, chi, M, S, U, VT, 5 * chi, 5 * chi)) != OR_OK) goto done;
+  for (int a = 0; a < chi; ++a)
+    for (int b = 0; b < chi; ++b)
+      for (int i = 0; i < d; ++i) {
+        zc acc = 0.0;
+        if (S[a] > GUARD_CANON)
+          for (int g = 0; g < chi; ++g) acc = acc + (1.0 / sqrt(S[a])) * conj(U[g + (size_t)chi * a]) * G2(g, i, b);
+        T2(a, i, b) = acc;
+      }
+  for (int a = 0; a < chi; ++a)
+    for (int b = 0; b < chi; ++b) Y[a + (size_t)chi * b] = l1[a] * U[a + (size_t)chi * b] * sqrt(S[b]);
+  for (int a = 0; a < chi; ++a) /* M = MATMUL(X, Y) */
+    for (int b = 0; b < chi; ++b) {
+      zc acc = 0.0;
+      for (int g = 0; g < chi; ++g) acc = acc + X[a + (size_t)chi * g] * Y[g + (size_t)chi * b];
+      MM(a, b) = acc;
+    }
+  if ((st = zgesvd_all(chi, chi, M, S, U, VT, 5 * chi, 5 * chi)) != OR_OK) goto done;
+  {
+    double normsq = 0.0;
+    for (int a = 0; a < chi; ++a) normsq = normsq + S[a] * S[a];
+    for (int a = 0; a < chi; ++a) l1[a] = S[a] / sqrt(normsq);
+  }
+  for (int a = 0; a < chi; ++a)
+    for (int b = 0; b < chi; ++b)
+      for (int i = 0; i < d; ++i) {
+        zc acc = 0.0;
+        for (int g = 0; g < chi; ++g) acc = acc + T1(a, i, g) * U[g + (size_t)chi * b];
+        G1(a, i, b) = acc;
+      }
+  for (int a = 0; a < chi; ++a)
+    for (int b = 0; b < chi; ++b)
+      for (int i = 0; i < d; ++i) {
+        zc acc = 0.0;
+        for (int g = 0; g < chi; ++g) acc = acc + VT[a + (size_t)chi * g] * T2(g, i, b);
+        G2(a, i, b) = acc;
+      }
+#undef G1
+#undef G2
+#undef T1
+#undef T2
+#undef MM
+done:
+  free(M);
+  free(X);
+  free(Y);
+  free(U);
+  free(VT);
+  free(g1t);
+  free(g2t);
+  free(S);
   return st;
 }
 

@@ -107,3 +107,44 @@ def test_canonical_form_all_nc_matches_oracle(pkg, oracle):
     num = np.diag(np.arange(d, dtype=float))
     assert np.allclose(obs.one_site_expval(g2, l2, num), obs.one_site_expval(gam, lam, num), atol=1e-10)
     assert abs(abs(obs.inner_product(gam, lam, g2, l2)) - 1.0) < 1e-10
+
+
+def _rho_normalised(l0, g1, l1, g2, l2):
+    r = obs.two_site_rho(l0, g1, l1, g2, l2)
+    return r / np.trace(r).real
+
+
+@pytest.mark.parametrize("chi,d", [(6, 2), (16, 3)])
+def test_canonical_form_matches_oracle(pkg, oracle, chi, d):
+    """One bond of a random (non-canonical) chain: the new Lambda1 and the bond's
+    normalised two-site density matrix (Gammas only up to the SVD gauge)."""
+    gam, lam = random_bond(chi, d, 70 + chi)
+    with pkg.Chain(4, d, chi) as c:
+        c.set_state(gam, lam)
+        c.canonical_form(2)
+        g1, g2, l1 = c.get_gamma(2), c.get_gamma(3), c.get_lambda(3)
+    rg1, rl1, rg2 = oracle.canonical_form(lam[1], gam[1], lam[2], gam[2], lam[3])
+    assert np.allclose(l1, rl1, atol=1e-11)
+    assert rel_close(_rho_normalised(lam[1], g1, l1, g2, lam[3]), _rho_normalised(lam[1], rg1, rl1, rg2, lam[3]),
+                     1e-10)
+
+
+def test_canonical_form_all_matches_oracle(pkg, oracle):
+    rng = np.random.default_rng(9)
+    L, d, chi = 6, 2, 6
+    gam = [np.asfortranarray(rng.standard_normal((chi, d, chi)) + 1j * rng.standard_normal((chi, d, chi)))
+           for _ in range(L)]
+    lam = [np.sort(rng.random(chi))[::-1] for _ in range(L + 1)]
+    lam[0] = np.eye(chi)[0]
+    lam[L] = np.eye(chi)[0]
+    with pkg.Chain(L, d, chi) as c:
+        c.set_state(gam, lam)
+        c.canonical_form_all()
+        g_gpu, l_gpu = c.get_state()
+    oracle.canonical_form_all(gam, lam)
+    for a, b in zip(l_gpu, lam):
+        assert np.allclose(a, b, atol=1e-10)
+    sz = np.diag([0.5, -0.5])
+    ea = obs.one_site_expval(g_gpu, l_gpu, sz) / obs.one_site_expval(g_gpu, l_gpu, np.eye(2))
+    eb = obs.one_site_expval(gam, lam, sz) / obs.one_site_expval(gam, lam, np.eye(2))
+    assert np.allclose(ea, eb, atol=1e-10)

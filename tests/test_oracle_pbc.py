@@ -62,3 +62,32 @@ def test_pbc_step_on_a_product_gate_ring(oracle, H):
     assert te < 1e-12
     for l in lam:
         assert abs(l[0] - 1.0) < 1e-12 and np.all(np.abs(l[1:]) < 1e-12)
+
+
+def test_canonical_form_keeps_a_canonical_chain(oracle, H):
+    from oracle import observables as obs
+    gam, lam = _canonical_chain(H, oracle)
+    g1, l1, g2 = oracle.canonical_form(lam[1], gam[1], lam[2], gam[2], lam[3])
+    assert np.allclose(l1, lam[2], atol=1e-12)
+    r0 = obs.two_site_rho(lam[1], gam[1], lam[2], gam[2], lam[3])
+    r1 = obs.two_site_rho(lam[1], g1, l1, g2, lam[3])
+    assert np.allclose(r0, r1, atol=1e-12)
+
+
+def test_canonical_form_all_makes_a_random_chain_canonical(oracle):
+    rng = np.random.default_rng(7)
+    L, d, chi = 5, 2, 4
+    gam = [np.asfortranarray(rng.standard_normal((chi, d, chi)) + 1j * rng.standard_normal((chi, d, chi)))
+           for _ in range(L)]
+    lam = [np.sort(rng.random(chi))[::-1] for _ in range(L + 1)]
+    lam[0] = np.eye(chi)[0]
+    lam[L] = np.eye(chi)[0]
+    oracle.canonical_form_all(gam, lam)
+    for l in lam[1:L]:
+        assert abs(np.sum(l ** 2) - 1.0) < 1e-12
+    # left-canonical condition on the bulk sites: sum conj(G) l0^2 G = 1 on the kept indices
+    for s in range(1, L - 1):
+        A = (gam[s] * lam[s][:, None, None]).reshape(chi * d, chi)
+        keep = lam[s + 1] > 1e-6
+        Mx = A.conj().T @ A
+        assert np.allclose(Mx[np.ix_(keep, keep)], np.eye(keep.sum()), atol=1e-8)
