@@ -44,6 +44,7 @@ J, U, MU, DT, ORDER = 1.0, 2.0, 0.0, 0.005, 2
 AMP, SEED = 1e-3, 1
 UPDATES_PER_STEP = (L // 2) * 2 + (L - 1) // 2  # 32 + 31 + 32 = 95
 METRIC = "two-site updates/sec (Trotter steps/sec = value/95)"
+SVD_MODES = {"fp64": 0, "df": 5}  # plain FP64 / precision form (double-float bidiagonalisation)
 WORKLOAD = "bose_hubbard_L64_d5_chi128_fp64_trotter2"
 
 
@@ -200,7 +201,7 @@ def run_ours(args):
     gam, lam, Udt = workload(H)
     fp64_peak = pkg.measure_fp64_peak(local)
 
-    chain = pkg.Chain(L, D, CHI, device=local)
+    chain = pkg.Chain(L, D, CHI, device=local, svd_mode=SVD_MODES[args.svd])
     chain.set_state(gam, lam)
     stream = torch.cuda.ExternalStream(chain.stream(), device=local)
 
@@ -313,7 +314,9 @@ def run_ours(args):
     out = {
         "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 (f64)" if args.svd == "fp64" else "c128 (f64; bidiagonalisation passes in double-float)",
+        "data": "synthetic",
         "config": {"workload": WORKLOAD, "L": L, "d": D, "chi": CHI, "J": J, "U": U, "mu": MU, "dt": DT,
                    "trotter_order": ORDER, "updates_per_step": UPDATES_PER_STEP,
                    "svd": "fp64 per bond: Householder bidiagonalisation + bisection + inverse iteration "
@@ -414,7 +417,7 @@ def run_saturated(args):
         lam.append(l / np.linalg.norm(l))
     gate = H.matrix_exponential(H.bose_hubbard(L, D, J, U, MU)[1], DT)
     links = list(range(1, L, 2))
-    chain = pkg.Chain(L, D, CHI)
+    chain = pkg.Chain(L, D, CHI, svd_mode=SVD_MODES[args.svd])
     chain.set_state(gam, lam)
     stream = torch.cuda.ExternalStream(chain.stream())
     for _ in range(args.warmup):
@@ -449,6 +452,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="headline", choices=["headline", "nc", "saturated"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--svd", default="fp64", choices=sorted(SVD_MODES))
     ap.add_argument("--cpu-updates", type=int, default=2)
     ap.add_argument("--outdir", default=os.path.join(ROOT, "gpurun_out"))
     args = ap.parse_args()

@@ -66,6 +66,10 @@ extern "C" {
 #define TEBD_SVD_JACOBI 2         /* one-sided Jacobi on the whole (compacted) Theta    */
 #define TEBD_SVD_BIDIAG 3         /* bidiagonalisation for every Theta (>= 2 x 2)       */
 #define TEBD_SVD_QRJ 4            /* pivoted QR + Jacobi on R^H for every bond          */
+#define TEBD_SVD_DF 5             /* precision form: as TEBD_SVD_FP64, but the bidiagonal
+                                     route's two passes over the trailing matrix and its
+                                     trailing updates run in double-float (pairs of FP32,
+                                     48-bit significands) on the FP32 pipe               */
 
 #define TEBD_OPTS_VERSION 1
 

@@ -497,6 +497,359 @@ __global__ void __launch_bounds__(kBW * 32) k_gebrd(Slot *slots, const int *path
 }
 
 // ---------------------------------------------------------------------------
+// Double-float arithmetic for the precision form of the bidiagonalisation: a
+// real number is an unevaluated sum hi + lo of two floats (48 significant bits),
+// products by Dekker's method with the FMA giving the exact error of hi*hi,
+// sums by Knuth's two-sum; __fadd_rn/__fmul_rn keep the compiler from fusing the
+// error-free steps.  A complex element is float4 (re_hi, re_lo, im_hi, im_lo),
+// the same 16 bytes as a double2.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float4 dfs(double2 v) {  // double2 -> double-float
+  const float rh = (float)v.x, ih = (float)v.y;
+  return make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
+}
+__device__ __forceinline__ double2 dfd(float4 v) {
+  return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+}
+__device__ __forceinline__ double2 dfl(const float4 *p) { return dfd(__ldcg(p)); }
+
+// (sh, sl) += (xh, xl) * (yh, yl)
+__device__ __forceinline__ void df_mac(float &sh, float &sl, float xh, float xl, float yh, float yl) {
+  const float pr = __fmul_rn(xh, yh);
+  float e = fmaf(xh, yh, -pr);
+  e = fmaf(xh, yl, e);
+  e = fmaf(xl, yh, e);
+  const float t = __fadd_rn(sh, pr);
+  const float bp = __fadd_rn(t, -sh);
+  const float err = __fadd_rn(__fadd_rn(sh, -__fadd_rn(t, -bp)), __fadd_rn(pr, -bp));
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+  sh = t;
+}
+// acc += conj(a) v (real and imaginary double-float accumulators)
+__device__ __forceinline__ void df_cmac_ca(float &rh, float &rl, float &ih, float &il, float4 a, float4 v) {
+  df_mac(rh, rl, a.x, a.y, v.x, v.y);   // + ar vr
+  df_mac(rh, rl, a.z, a.w, v.z, v.w);   // + ai vi
+  df_mac(ih, il, a.x, a.y, v.z, v.w);   // + ar vi
+  df_mac(ih, il, -a.z, -a.w, v.x, v.y); // - ai vr
+}
+// acc += a v
+__device__ __forceinline__ void df_cmac(float &rh, float &rl, float &ih, float &il, float4 a, float4 v) {
+  df_mac(rh, rl, a.x, a.y, v.x, v.y);
+  df_mac(rh, rl, -a.z, -a.w, v.z, v.w);
+  df_mac(ih, il, a.x, a.y, v.z, v.w);
+  df_mac(ih, il, a.z, a.w, v.x, v.y);
+}
+// acc -= l conj(g)
+__device__ __forceinline__ void df_cmsub_cb(float4 &acc, float4 l, float4 g) {
+  df_mac(acc.x, acc.y, -l.x, -l.y, g.x, g.y);  // - lr gr
+  df_mac(acc.x, acc.y, -l.z, -l.w, g.z, g.w);  // - li gi
+  df_mac(acc.z, acc.w, l.x, l.y, g.z, g.w);    // + lr gi
+  df_mac(acc.z, acc.w, -l.z, -l.w, g.x, g.y);  // - li gr
+}
+__device__ __forceinline__ float4 df_norm4(float4 v) {  // renormalise hi + lo (fast two-sum)
+  const float rh = __fadd_rn(v.x, v.y), ih = __fadd_rn(v.z, v.w);
+  return make_float4(rh, __fadd_rn(v.y, -__fadd_rn(rh, -v.x)), ih, __fadd_rn(v.w, -__fadd_rn(ih, -v.z)));
+}
+// warp sum of a double-float, as a double (each lane's pair is exact in FP64)
+__device__ __forceinline__ double df_warp_sum(float h, float l) { return bsum((double)h + (double)l); }
+
+__global__ void __launch_bounds__(kBW * 32) k_gebrd_df(Slot *slots, const int *path) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int s = blockIdx.y;
+  const int route = path[s];
+  if (!on_route(route)) return;  // uniform per cluster
+  const Slot S = slots[s];
+  int M, N;
+  bd_dims(*S.cp, route, M, N);
+  float4 *A = reinterpret_cast<float4 *>(S.X);  // (re_hi, re_lo, im_hi, im_lo)
+  double *dd = S.bdws, *ee = S.bdws + N;
+  const BdAux ax = bd_aux(S.aux, M, N);
+  const int C = (int)cluster.num_blocks(), crank = (int)cluster.block_rank();
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int gt = crank * nthr + tid, gthr = C * nthr;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int gw = crank * (nthr >> 5) + warp, nw = C * (nthr >> 5);
+  extern __shared__ double2 sh[];
+  float4 *vec = reinterpret_cast<float4 *>(sh);  // max(M, N): v or u of the current column
+  double2 *sm = sh + max(M, N);         // 4 kPanel small per-column vectors
+  double *stg = reinterpret_cast<double *>(sm + 4 * kPanel);  // trailing-update staging
+  __shared__ double red[32];
+#define AE(r, c) A[(size_t)(r) + (size_t)M * (c)]
+#define YB(c, k) ax.Yb[(size_t)(c) + (size_t)N * (k)]
+#define XB(r, k) ax.Xb[(size_t)(r) + (size_t)M * (k)]
+#define PV(c, k) ax.Pv[(size_t)(c) + (size_t)N * (k)]
+  {  // norm partials of column 0 below the diagonal
+    double acc = 0.0;
+    for (int r = 1 + gt; r < M; r += gthr) {
+      const double2 a = dfl(&AE(r, 0));
+      acc = fma(a.x, a.x, fma(a.y, a.y, acc));
+    }
+    acc = block_sum(acc, red);
+    if (tid == 0) ax.nrmL[crank] = acc;
+  }
+  cluster.sync();
+  for (int p = 0; p < N; p += kPanel) {
+    const int jb = min(kPanel, N - p);
+    for (int j = 0; j < jb; ++j) {
+      const int i = p + j;
+      // ---- left reflector of column i (every CTA, identical inputs) ----
+      double beta;
+      double2 tau, sc;
+      {
+        double xn2 = 0.0;
+        for (int q = 0; q < C; ++q) xn2 += __ldcg(&ax.nrmL[q]);
+        larfg_scalars(dfl(&AE(i, i)), xn2, beta, tau, sc);
+      }
+      if (crank == 0 && tid == 0) {
+        dd[i] = beta;
+        S.tau[i] = tau;
+      }
+      if (i == N - 1) {  // last column: left reflector only
+        for (int r = i + 1 + gt; r < M; r += gthr) AE(r, i) = dfs(cmul(dfl(&AE(r, i)), sc));
+        break;
+      }
+      // ---- S2: z = A0(i:M, i+1:N)^H v, s1 = V^H v, s2 = Xp^H v ----
+      for (int r = i + tid; r < M; r += nthr)
+        vec[r - i] = dfs(r == i ? make_double2(1.0, 0.0) : cmul(dfl(&AE(r, i)), sc));
+      __syncthreads();
+      {
+        const int ncol = N - i - 1, items = ncol + 2 * j;
+        for (int it = gw; it < items; it += nw) {
+          double2 acc = make_double2(0.0, 0.0);  // sum_r conj(col(r)) v(r)
+          if (it < ncol + j) {  // columns of A0 / of V: double-float on the FP32 pipe
+            const float4 *col = &AE(0, it < ncol ? i + 1 + it : p + (it - ncol));
+            float ar = 0.f, arl = 0.f, ai = 0.f, ail = 0.f;
+            int r = i + lane;
+            for (; r + 96 < M; r += 128) {
+              float4 c[4];
+#pragma unroll
+              for (int q = 0; q < 4; ++q) c[q] = __ldcg(col + r + 32 * q);
+#pragma unroll
+              for (int q = 0; q < 4; ++q) df_cmac_ca(ar, arl, ai, ail, c[q], vec[r + 32 * q - i]);
+            }
+            for (; r < M; r += 32) df_cmac_ca(ar, arl, ai, ail, __ldcg(col + r), vec[r - i]);
+            acc = make_double2(df_warp_sum(ar, arl), df_warp_sum(ai, ail));
+          } else {  // x_k columns (FP64)
+            const double2 *col = &XB(0, it - ncol - j);
+            for (int r = i + lane; r < M; r += 32) mac_ca(acc, ldc(col + r), dfd(vec[r - i]));
+            acc.x = bsum(acc.x);
+            acc.y = bsum(acc.y);
+          }
+          if (lane == 0) {
+            if (it < ncol)
+              ax.zb[i + 1 + it] = acc;
+            else if (it < ncol + j)
+              ax.s1[it - ncol] = acc;
+            else
+              ax.s2[it - ncol - j] = acc;
+          }
+        }
+      }
+      cluster.sync();
+      // ---- S3: y_i = tauq (z - Y s1 - U s2); row i of the current matrix ----
+      if (tid < j) {
+        sm[tid] = ldc(&ax.s1[tid]);
+        sm[kPanel + tid] = ldc(&ax.s2[tid]);
+        sm[2 * kPanel + tid] = dfl(&AE(i, p + tid));  // v_k(i)
+        sm[3 * kPanel + tid] = ldc(&XB(i, tid));      // x_k(i)
+      }
+      __syncthreads();
+      {
+        double acc = 0.0;
+        for (int c = i + 1 + gt; c < N; c += gthr) {
+          double2 y = ldc(&ax.zb[c]);
+          double2 rr = dfl(&AE(i, c));
+          for (int k = 0; k < j; ++k) {
+            const double2 yk = ldc(&YB(c, k)), uk = ldc(&PV(c, p + k));
+            msub(y, yk, sm[k]);
+            msub(y, uk, sm[kPanel + k]);
+            msub_cb(rr, sm[2 * kPanel + k], yk);
+            msub_cb(rr, sm[3 * kPanel + k], uk);
+          }
+          y = cmul(tau, y);
+          YB(c, j) = y;
+          rr.x -= y.x;  // v_i(i) = 1: rr -= conj(y)
+          rr.y += y.y;
+          AE(i, c) = dfs(rr);
+          if (c >= i + 2) acc = fma(rr.x, rr.x, fma(rr.y, rr.y, acc));
+        }
+        acc = block_sum(acc, red);
+        if (tid == 0) ax.nrmR[crank] = acc;
+      }
+      for (int r = i + 1 + gt; r < M; r += gthr) AE(r, i) = dfs(cmul(dfl(&AE(r, i)), sc));  // v_i
+      cluster.sync();
+      // ---- right reflector of row i (every CTA) ----
+      double beta2;
+      double2 tau2, sc2;
+      {
+        double xn2 = 0.0;
+        for (int q = 0; q < C; ++q) xn2 += __ldcg(&ax.nrmR[q]);
+        larfg_scalars(cconj(dfl(&AE(i, i + 1))), xn2, beta2, tau2, sc2);
+      }
+      if (crank == 0 && tid == 0) {
+        ee[i] = beta2;
+        S.taup[i] = tau2;
+      }
+      // ---- S4: w = A0(i+1:M, i+1:N) u by column chunks, t1 = Y^H u, t2 = U^H u ----
+      for (int c = i + 1 + tid; c < N; c += nthr)
+        vec[c - i - 1] = dfs(c == i + 1 ? make_double2(1.0, 0.0) : cmul(cconj(dfl(&AE(i, c))), sc2));
+      __syncthreads();
+      {
+        const int rows = M - i - 1, cols = N - i - 1;
+        const int nrb = (rows + 31) / 32, ncc = (cols + kChunk - 1) / kChunk;
+        const int tasks = nrb * ncc, items = tasks + 2 * j + 1;
+        for (int it = gw; it < items; it += nw) {
+          if (it < tasks) {
+            const int rb = it % nrb, cc = it / nrb;
+            const int r = i + 1 + rb * 32 + lane;
+            const int c0 = i + 1 + cc * kChunk, c1 = min(N, c0 + kChunk);
+            if (r < M) {
+              float ar = 0.f, arl = 0.f, ai = 0.f, ail = 0.f;
+              const float4 *rp = &AE(r, 0);
+              int c = c0;
+              for (; c + 3 < c1; c += 4) {
+                float4 a[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) a[q] = __ldcg(rp + (size_t)M * (c + q));
+#pragma unroll
+                for (int q = 0; q < 4; ++q) df_cmac(ar, arl, ai, ail, a[q], vec[c + q - i - 1]);
+              }
+              for (; c < c1; ++c) df_cmac(ar, arl, ai, ail, __ldcg(rp + (size_t)M * c), vec[c - i - 1]);
+              ax.part[(size_t)cc * M + r] = make_double2((double)ar + (double)arl, (double)ai + (double)ail);
+            }
+          } else {
+            const int k = it - tasks;  // 0..j: t1 over y_k; j+1..2j: t2 over u_(k-j-1)
+            const double2 *cp = k <= j ? &YB(0, k) : &PV(0, p + k - j - 1);
+            double2 acc = make_double2(0.0, 0.0);
+            for (int c = i + 1 + lane; c < N; c += 32) mac_ca(acc, ldc(cp + c), dfd(vec[c - i - 1]));
+            acc.x = bsum(acc.x);
+            acc.y = bsum(acc.y);
+            if (lane == 0) {
+              if (k <= j)
+                ax.t1[k] = acc;
+              else
+                ax.t2[k - j - 1] = acc;
+            }
+          }
+        }
+        for (int c = i + 1 + gt; c < N; c += gthr) PV(c, i) = dfd(vec[c - i - 1]);  // u_i
+      }
+      cluster.sync();
+      // ---- x_i = taup (w - V t1 - Xp t2); then column i+1 of the current matrix ----
+      const bool next_in_panel = j + 1 < jb;
+      if (tid <= j) {
+        sm[tid] = ldc(&ax.t1[tid]);
+        if (tid < j) sm[kPanel + tid] = ldc(&ax.t2[tid]);
+        if (next_in_panel) {
+          sm[2 * kPanel + tid] = ldc(&YB(i + 1, tid));      // y_k(i+1)
+          sm[3 * kPanel + tid] = ldc(&PV(i + 1, p + tid));  // u_k(i+1)
+        }
+      }
+      __syncthreads();
+      {
+        const int ncc = (N - i - 1 + kChunk - 1) / kChunk;
+        double acc = 0.0;
+        for (int r = i + 1 + gt; r < M; r += gthr) {
+          double2 w = make_double2(0.0, 0.0);
+          for (int q = 0; q < ncc; ++q) {  // fixed order
+            const double2 t = ldc(&ax.part[(size_t)q * M + r]);
+            w.x += t.x;
+            w.y += t.y;
+          }
+          for (int k = 0; k <= j; ++k) msub(w, dfl(&AE(r, p + k)), sm[k]);
+          for (int k = 0; k < j; ++k) msub(w, ldc(&XB(r, k)), sm[kPanel + k]);
+          const double2 x = cmul(tau2, w);
+          XB(r, j) = x;
+          if (next_in_panel) {
+            double2 a = dfl(&AE(r, i + 1));
+            for (int k = 0; k <= j; ++k) {
+              msub_cb(a, dfl(&AE(r, p + k)), sm[2 * kPanel + k]);
+              msub_cb(a, k < j ? ldc(&XB(r, k)) : x, sm[3 * kPanel + k]);
+            }
+            AE(r, i + 1) = dfs(a);
+            if (r >= i + 2) acc = fma(a.x, a.x, fma(a.y, a.y, acc));
+          }
+        }
+        if (next_in_panel) {
+          acc = block_sum(acc, red);
+          if (tid == 0) ax.nrmL[crank] = acc;
+        }
+      }
+      cluster.sync();
+    }
+    const int q = p + jb;
+    if (q >= N) break;
+    // ---- panel end: A0(q:M, q:N) -= V Y^H + Xp U^H (inner dimension 2 jb) ----
+    // 64 x 64 tiles over the cluster's CTAs, double-float on the FP32 pipe: each
+    // thread starts from its 8 elements of A0 and subtracts the 2 jb products
+    {
+      const int K2 = 2 * jb;
+      const int ntr = (M - q + kTile - 1) / kTile, ntc = (N - q + kTile - 1) / kTile;
+      float4 *Ls = reinterpret_cast<float4 *>(stg), *Rs = Ls + kKc * kTile;
+      const int tx = tid & 15, ty = tid >> 4;  // rows ty, ty + 32; columns tx + 16 b
+      for (int t = crank; t < ntr * ntc; t += C) {
+        const int r0 = q + (t % ntr) * kTile, c0 = q + (t / ntr) * kTile;
+        float4 acc[2][4];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int r = r0 + ty + 32 * a, c = c0 + tx + 16 * b;
+            acc[a][b] = (r < M && c < N) ? __ldcg(&AE(r, c)) : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        for (int kc = 0; kc < K2; kc += kKc) {
+          __syncthreads();
+          for (int e = tid; e < kKc * kTile; e += nthr) {
+            const int rr = e % kTile, kk = e / kTile, k = kc + kk;
+            const int r = r0 + rr, c = c0 + rr;
+            float4 l = make_float4(0.f, 0.f, 0.f, 0.f), g = l;
+            if (k < K2) {
+              if (r < M) l = k < jb ? __ldcg(&AE(r, p + k)) : dfs(ldc(&XB(r, k - jb)));
+              if (c < N) g = dfs(k < jb ? ldc(&YB(c, k)) : ldc(&PV(c, p + k - jb)));
+            }
+            Ls[kk * kTile + rr] = l;
+            Rs[kk * kTile + rr] = g;
+          }
+          __syncthreads();
+          for (int kk = 0; kk < kKc; ++kk) {
+            const float4 l0 = Ls[kk * kTile + ty], l1 = Ls[kk * kTile + ty + 32];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+              const float4 g = Rs[kk * kTile + tx + 16 * b];
+              df_cmsub_cb(acc[0][b], l0, g);  // acc -= l conj(g)
+              df_cmsub_cb(acc[1][b], l1, g);
+            }
+          }
+        }
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int r = r0 + ty + 32 * a, c = c0 + tx + 16 * b;
+            if (r < M && c < N) AE(r, c) = df_norm4(acc[a][b]);
+          }
+      }
+    }
+    cluster.sync();
+    {  // norm partials of column q below the diagonal
+      double acc = 0.0;
+      for (int r = q + 1 + gt; r < M; r += gthr) {
+        const double2 a = dfl(&AE(r, q));
+        acc = fma(a.x, a.x, fma(a.y, a.y, acc));
+      }
+      acc = block_sum(acc, red);
+      if (tid == 0) ax.nrmL[crank] = acc;
+    }
+    cluster.sync();
+  }
+#undef AE
+#undef YB
+#undef XB
+#undef PV
+}
+
+// ---------------------------------------------------------------------------
 // 2. bisection: sigma_i of B for i < kk (one thread each), Golub-Kahan Sturm counts
 // ---------------------------------------------------------------------------
 // Sturm count of the Golub-Kahan matrix: eigenvalues below x; sq = squared
@@ -960,6 +1313,32 @@ __global__ void k_bd_store(Slot *slots, const int *path, int kk) {
   if (blockIdx.x == 0 && threadIdx.x == 0) S.cp->k = K;
 }
 
+// Precision form: the M x N matrix of the route as double-float in place before
+// the bidiagonalisation (float4 per complex element), FP64 again after it.
+__global__ void k_bd_to_df(Slot *slots, const int *path) {
+  const int s = blockIdx.y;
+  const int route = path[s];
+  if (!on_route(route)) return;
+  const Slot S = slots[s];
+  int M, N;
+  bd_dims(*S.cp, route, M, N);
+  float4 *F = reinterpret_cast<float4 *>(S.X);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)M * N; e += (size_t)gridDim.x * blockDim.x)
+    F[e] = dfs(S.X[e]);
+}
+
+__global__ void k_bd_from_df(Slot *slots, const int *path) {
+  const int s = blockIdx.y;
+  const int route = path[s];
+  if (!on_route(route)) return;
+  const Slot S = slots[s];
+  int M, N;
+  bd_dims(*S.cp, route, M, N);
+  const float4 *F = reinterpret_cast<const float4 *>(S.X);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)M * N; e += (size_t)gridDim.x * blockDim.x)
+    S.X[e] = dfd(F[e]);
+}
+
 // Transposed route, before the bidiagonalisation: X (m x n, ld m) -> V (copy),
 // then X <- V^H (n x m, ld n).
 __global__ void k_bd_stage(Slot *slots, const int *path) {
@@ -1024,8 +1403,9 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
   {
     cudaLaunchConfig_t cfg = {};
     const size_t smem = sizeof(double2) * ((size_t)nmax + 4 * kPanel) + sizeof(double) * kStageDoubles;
-    if ((rc = check_cuda(h, cudaFuncSetAttribute(k_gebrd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem),
+    const bool dfp = h->opts.svd_mode == TEBD_SVD_DF;
+    auto kern = dfp ? k_gebrd_df : k_gebrd;
+    if ((rc = check_cuda(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                          "bidiagonalisation shared memory")))
       return rc;
     cfg.blockDim = dim3(kBW * 32, 1, 1);
@@ -1050,7 +1430,7 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
       cfg.gridDim = dim3(c, nb, 1);
       attr[0].val.clusterDim.x = c;
       int ncl = 0;
-      if (cudaOccupancyMaxActiveClusters(&ncl, (const void *)k_gebrd, &cfg) != cudaSuccess || ncl < 1) {
+      if (cudaOccupancyMaxActiveClusters(&ncl, (const void *)kern, &cfg) != cudaSuccess || ncl < 1) {
         cudaGetLastError();
         continue;
       }
@@ -1062,11 +1442,19 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     }
     cfg.gridDim = dim3(C, nb, 1);
     attr[0].val.clusterDim.x = C;
+    if (dfp) {
+      k_bd_to_df<<<dim3(128, nb), 256, 0, st>>>(h->slots_d, h->path_d);
+      TEBD_LAUNCHED(h);
+    }
     if (h->profiling) cudaEventRecord(h->ev[4], st);
-    rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_gebrd, h->slots_d, (const int *)h->path_d),
+    rc = check_cuda(h, cudaLaunchKernelEx(&cfg, kern, h->slots_d, (const int *)h->path_d),
                     "bidiagonalisation launch");
     if (rc) return rc;
     if (h->profiling) cudaEventRecord(h->ev[5], st);
+    if (dfp) {
+      k_bd_from_df<<<dim3(128, nb), 256, 0, st>>>(h->slots_d, h->path_d);
+      TEBD_LAUNCHED(h);
+    }
     TEBD_LAUNCHED(h);
     ++h->stats.gebrd_launches;
   }

@@ -123,7 +123,7 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
   }
   if (L < 2 || d < 1 || d > 8 || chi < 1 || (mode != TEBD_MODE_DENSE && mode != TEBD_MODE_NC) ||
       (o.svd_mode != TEBD_SVD_FP64 && o.svd_mode != TEBD_SVD_JACOBI &&
-       o.svd_mode != TEBD_SVD_BIDIAG && o.svd_mode != TEBD_SVD_QRJ)) {
+       o.svd_mode != TEBD_SVD_BIDIAG && o.svd_mode != TEBD_SVD_QRJ && o.svd_mode != TEBD_SVD_DF)) {
     g_noh_err = "tebd_create: invalid L/d/chi/mode (need L>=2, 1<=d<=8, chi>=1)";
     return TEBD_ERR_ARG;
   }

@@ -43,6 +43,7 @@ SVD_FP64 = 0
 SVD_JACOBI = 2
 SVD_BIDIAG = 3
 SVD_QRJ = 4
+SVD_DF = 5
 OPTS_VERSION = 1
 
 ERROR_NAMES = {

@@ -152,7 +152,7 @@ def test_golden_reference_propagators(pkg):
             assert abs(te - float(z["truncerr_" + key])) < 1e-11
 
 
-@pytest.mark.parametrize("svd_mode", [0, 3])
+@pytest.mark.parametrize("svd_mode", [0, 3, 5])
 @pytest.mark.parametrize("order", [2, 5])
 def test_trotter_steps_match_oracle(pkg, oracle, order, svd_mode):
     """Full sweeps (batched same-parity bonds on the GPU vs sequential bonds in the
@@ -181,12 +181,13 @@ def test_trotter_steps_match_oracle(pkg, oracle, order, svd_mode):
     assert abs(abs(obs.inner_product(gam, lam, g_gpu, l_gpu)) - 1.0) < 1e-10
 
 
-@pytest.mark.parametrize("svd_mode,drop", [(0, None), (4, None), (0, "left"), (0, "right")])
+@pytest.mark.parametrize("svd_mode,drop", [(0, None), (4, None), (0, "left"), (0, "right"), (5, None), (5, "left")])
 def test_bose_hubbard_full_size_single_bond(pkg, oracle, svd_mode, drop):
     """Bond of the d=5, chi=128 Bose-Hubbard workload (n = 640) against LAPACK, plus
     size-independent properties: sum lambda^2 = 1, truncerr = 1 - sum of kept S^2,
     and left/right canonical conditions of the new Gammas.  The default route takes
-    the bidiagonal path here (640 columns); mode 4 forces QR + Jacobi.  Three exact
+    the bidiagonal path here (640 columns); mode 4 forces QR + Jacobi; mode 5 runs
+    the bidiagonalisation's heavy passes in double-float.  Three exact
     zeros in the left (right) Lambda make the compacted Theta 625 x 640 (640 x 625):
     the wide one is bidiagonalised as Theta^H."""
     chi, d = 128, 5
@@ -205,7 +206,7 @@ def test_bose_hubbard_full_size_single_bond(pkg, oracle, svd_mode, drop):
         te = c.two_site_op(2, U)
         s = c.singular_values(2)
         g1, g2, l1 = c.get_gamma(2), c.get_gamma(3), c.get_lambda(3)
-        assert c.stats()["bidiag_updates"] == (1 if svd_mode == 0 else 0)
+        assert c.stats()["bidiag_updates"] == (1 if svd_mode in (0, 5) else 0)
     rg1, rg2, rl1, rte, rs = oracle.two_site_op(gam[1], gam[2], lam[1], lam[2], lam[3], U)
     ok, worst = sigma_ok(s, rs)
     assert ok, worst
