@@ -261,6 +261,11 @@ def run_ours(args):
         e2e_wall = time.perf_counter() - t0
         barrier()
     step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    if args.save_obs:  # final-state observables on the device, for comparing SVD modes
+        num = np.diag(np.arange(D, dtype=float))
+        Hb = H.bose_hubbard(L, D, J, U, MU)
+        np.savez(args.save_obs, n=chain.one_site_expval(num), e=chain.local_energy(Hb),
+                 lam=np.array(chain.get_state()[1]), ent=chain.chain_entropy(), step_ms=np.array(step_ms))
     ms = maxall(sum(step_ms))
     e2e_ms = maxall(e2e_wall * 1e3)
     launches = chain.kernel_launches() - launches0
@@ -453,6 +458,7 @@ def main():
     ap.add_argument("--workload", default="headline", choices=["headline", "nc", "saturated"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--svd", default="fp64", choices=sorted(SVD_MODES))
+    ap.add_argument("--save-obs", default=None, help="write final <n_i>, bond energies, Lambdas (npz)")
     ap.add_argument("--cpu-updates", type=int, default=2)
     ap.add_argument("--outdir", default=os.path.join(ROOT, "gpurun_out"))
     args = ap.parse_args()

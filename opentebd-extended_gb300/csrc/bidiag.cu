@@ -1313,8 +1313,98 @@ __global__ void k_bd_store(Slot *slots, const int *path, int kk) {
   if (blockIdx.x == 0 && threadIdx.x == 0) S.cp->k = K;
 }
 
+// Precision form of step 4: the same reflector products in double-float, reading
+// the left reflectors from the double-float matrix the bidiagonalisation left in
+// S.X and the right ones from Pv converted in place (k_bd_pv_to_df); the vectors
+// Yu / Ru are double-float too and k_bd_store_df converts them.
+__global__ void __launch_bounds__(256) k_bd_apply_df(Slot *slots, const int *path, int kk) {
+  const int s = blockIdx.y;
+  const int route = path[s];
+  if (!on_route(route)) return;
+  const Slot S = slots[s];
+  int m, n;
+  bd_dims(*S.cp, route, m, n);
+  const int N = 2 * n, K = min(kk, n);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int col = blockIdx.x * 8 + warp;
+  if (col >= 2 * K) return;
+  double *base = S.bdws + bd_scratch(n, kk);
+  const double *Z = base + 5 * (size_t)N * K;
+  float4 *Yu = reinterpret_cast<float4 *>(base + 6 * (size_t)N * K);
+  float4 *Ru = route == kPathBidiagT ? reinterpret_cast<float4 *>(base) : reinterpret_cast<float4 *>(S.V);
+  const float4 *Xf = reinterpret_cast<const float4 *>(S.X);
+  const float4 *Pf = reinterpret_cast<const float4 *>(S.aux);
+  const float4 one = make_float4(1.f, 0.f, 0.f, 0.f);
+  const bool left = col < K;
+  const int i = left ? col : col - K;
+  const int len = left ? m : n;
+  float4 *Y = left ? Yu + (size_t)m * i : Ru + (size_t)n * i;
+  for (int r = lane; r < len; r += 32)
+    Y[r] = dfs(make_double2(left ? (r < n ? Z[(size_t)(2 * r + 1) * K + i] : 0.0) : Z[(size_t)(2 * r) * K + i], 0.0));
+  __syncwarp();
+  for (int j = left ? n - 1 : n - 2; j >= 0; --j) {
+    // reflector j: left v (rows j.., v(j) = 1) or right u (rows j+1.., u(j+1) = 1)
+    const int r0 = left ? j : j + 1;
+    const float4 *vc = left ? Xf + (size_t)m * j : Pf + (size_t)n * j;
+    const double2 t = left ? S.tau[j] : S.taup[j];
+    float wrh = 0.f, wrl = 0.f, wih = 0.f, wil = 0.f;  // w = sum conj(v) y
+    for (int r = r0 + lane; r < len; r += 32)
+      df_cmac_ca(wrh, wrl, wih, wil, (left && r == j) ? one : __ldcg(vc + r), Y[r]);
+    const double wr = df_warp_sum(wrh, wrl), wi = df_warp_sum(wih, wil);
+    const float4 f = dfs(make_double2(t.x * wr - t.y * wi, t.x * wi + t.y * wr));  // tau w
+    const float4 nf = make_float4(-f.x, -f.y, -f.z, -f.w);
+    for (int r = r0 + lane; r < len; r += 32) {  // y -= v f
+      const float4 v = (left && r == j) ? one : __ldcg(vc + r);
+      float4 y = Y[r];
+      df_mac(y.x, y.y, v.x, v.y, nf.x, nf.y);
+      df_mac(y.x, y.y, v.z, v.w, f.z, f.w);
+      df_mac(y.z, y.w, v.x, v.y, nf.z, nf.w);
+      df_mac(y.z, y.w, v.z, v.w, nf.x, nf.y);
+      Y[r] = df_norm4(y);
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void k_bd_pv_to_df(Slot *slots, const int *path) {  // Pv in place, N x N
+  const int s = blockIdx.y;
+  const int route = path[s];
+  if (!on_route(route)) return;
+  const Slot S = slots[s];
+  int M, N;
+  bd_dims(*S.cp, route, M, N);
+  float4 *F = reinterpret_cast<float4 *>(S.aux);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)N * N; e += (size_t)gridDim.x * blockDim.x)
+    F[e] = dfs(S.aux[e]);
+}
+
+__global__ void k_bd_store_df(Slot *slots, const int *path, int kk) {
+  const int s = blockIdx.y;
+  const int route = path[s];
+  if (!on_route(route)) return;
+  const Slot S = slots[s];
+  int M, N;
+  bd_dims(*S.cp, route, M, N);
+  const int m = S.cp->m, n = S.cp->n, K = min(kk, N);
+  double *base = S.bdws + bd_scratch(N, kk);
+  const double *sig = S.bdws + 2 * N;
+  const float4 *Yu = reinterpret_cast<const float4 *>(base + 12 * (size_t)N * K);
+  const float4 *U = route == kPathBidiagT ? reinterpret_cast<const float4 *>(base) : Yu;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)m * K; e += stride) {
+    const int i = (int)(e / m);
+    const double2 y = dfd(U[e]);
+    S.X[e] = make_double2(y.x * sig[i], y.y * sig[i]);
+  }
+  const float4 *Vs = route == kPathBidiagT ? Yu : reinterpret_cast<const float4 *>(S.V);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * K; e += stride)
+    S.V[e] = dfd(Vs[e]);  // in place on the tall route (same element, same size)
+  if (blockIdx.x == 0 && threadIdx.x == 0) S.cp->k = K;
+}
+
 // Precision form: the M x N matrix of the route as double-float in place before
-// the bidiagonalisation (float4 per complex element), FP64 again after it.
+// the bidiagonalisation (float4 per complex element); its reflectors stay in that
+// form for k_bd_apply_df.
 __global__ void k_bd_to_df(Slot *slots, const int *path) {
   const int s = blockIdx.y;
   const int route = path[s];
@@ -1325,18 +1415,6 @@ __global__ void k_bd_to_df(Slot *slots, const int *path) {
   float4 *F = reinterpret_cast<float4 *>(S.X);
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)M * N; e += (size_t)gridDim.x * blockDim.x)
     F[e] = dfs(S.X[e]);
-}
-
-__global__ void k_bd_from_df(Slot *slots, const int *path) {
-  const int s = blockIdx.y;
-  const int route = path[s];
-  if (!on_route(route)) return;
-  const Slot S = slots[s];
-  int M, N;
-  bd_dims(*S.cp, route, M, N);
-  const float4 *F = reinterpret_cast<const float4 *>(S.X);
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)M * N; e += (size_t)gridDim.x * blockDim.x)
-    S.X[e] = dfd(F[e]);
 }
 
 // Transposed route, before the bidiagonalisation: X (m x n, ld m) -> V (copy),
@@ -1451,8 +1529,8 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
                     "bidiagonalisation launch");
     if (rc) return rc;
     if (h->profiling) cudaEventRecord(h->ev[5], st);
-    if (dfp) {
-      k_bd_from_df<<<dim3(128, nb), 256, 0, st>>>(h->slots_d, h->path_d);
+    if (dfp) {  // the reflectors stay double-float for k_bd_apply_df; Pv follows
+      k_bd_pv_to_df<<<dim3(128, nb), 256, 0, st>>>(h->slots_d, h->path_d);
       TEBD_LAUNCHED(h);
     }
     TEBD_LAUNCHED(h);
@@ -1493,10 +1571,17 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
       return rc;
   }
   TEBD_LAUNCHED(h);
-  k_bd_apply<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
-  TEBD_LAUNCHED(h);
-  k_bd_store<<<dim3(256, nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
-  TEBD_LAUNCHED(h);
+  if (h->opts.svd_mode == TEBD_SVD_DF) {
+    k_bd_apply_df<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
+    TEBD_LAUNCHED(h);
+    k_bd_store_df<<<dim3(256, nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
+    TEBD_LAUNCHED(h);
+  } else {
+    k_bd_apply<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
+    TEBD_LAUNCHED(h);
+    k_bd_store<<<dim3(256, nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
+    TEBD_LAUNCHED(h);
+  }
   if (h->profiling) {
     cudaEventRecord(h->ev[1], st);
     if ((rc = check_cuda(h, cudaStreamSynchronize(st), "bidiag"))) return rc;
