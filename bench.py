@@ -20,6 +20,10 @@ e2e:   the same K steps end to end through the reference-facing C ABI: the chain
        host (tebd_trotter_step), and the chain is read back at the end
        (tebd_get_gamma/lambda): the drop-in keeps Gammas/Lambdas resident across
        steps, as a Fortran host calling it would.  Host wall clock, synchronised.
+precision_form: the same K steps again with the precision form of the SVD
+       (TEBD_SVD_DF), its updates/s, the ratio to the plain FP64 value and the
+       largest differences of the final <n_i>, bond energies and entropies
+       (the metric's "mixed vs plain FP64 at error <= 1e-8"); --no-precision skips it.
 --impl reference: the reference's CPU algorithm (the C restatement in oracle/,
        naive FormTheta/ThetaOperation loops + LAPACK ZGESVD) on all host cores,
        one bond update per core per step.
@@ -281,6 +285,38 @@ def run_ours(args):
               "ms_per_step_steps_50_end": (sum(sat) / len(sat)) if sat else None,
               "ms_step_1": step_ms[0], "ms_step_last": step_ms[-1]}
 
+    # ---- precision form beside the plain FP64 run (the metric's "mixed vs plain") --
+    prec = None
+    if args.svd == "fp64" and not args.no_precision:
+        num = np.diag(np.arange(D, dtype=float))
+        Hb = H.bose_hubbard(L, D, J, U, MU)
+        ref_obs = (chain.one_site_expval(num), chain.local_energy(Hb), chain.chain_entropy())
+        pc = pkg.Chain(L, D, CHI, device=local, svd_mode=SVD_MODES["df"])
+        pc.set_state(gam, lam)
+        for _ in range(args.warmup):
+            pc.trotter_step(Udt, ORDER)
+        pc.set_state(gam, lam)
+        pstream = torch.cuda.ExternalStream(pc.stream(), device=local)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(pstream)
+        for _ in range(args.steps):
+            pc.trotter_step(Udt, ORDER)
+        e1.record(pstream)
+        barrier()
+        pms = maxall(e0.elapsed_time(e1))
+        obs_p = (pc.one_site_expval(num), pc.local_energy(Hb), pc.chain_entropy())
+        pv = world * UPDATES_PER_STEP * args.steps / (pms / 1e3)
+        prec = {"svd": "TEBD_SVD_DF: bidiagonal route's trailing-matrix passes, trailing updates and "
+                       "back-transformation in double-float on the FP32 pipe; the rest FP64",
+                "value": pv, "unit": "updates/s", "ms_per_step": pms / args.steps,
+                "speedup_vs_plain_fp64": pv / value,
+                "max_abs_err_vs_plain_fp64": {"n_i": float(np.max(np.abs(obs_p[0] - ref_obs[0]))),
+                                              "bond_energy": float(np.max(np.abs(obs_p[1] - ref_obs[1]))),
+                                              "entropy": float(np.max(np.abs(obs_p[2] - ref_obs[2])))},
+                "error_bound": 1e-8}
+        pc.close()
+
     # ---- CPU baseline: the oracle port on a bounded sample ------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -340,6 +376,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "roofline": roof,
         "cpu_baseline": cpu,
+        "precision_form": prec,
         "clocks": clocks,
     }
     if rank == 0:
@@ -459,6 +496,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--svd", default="fp64", choices=sorted(SVD_MODES))
     ap.add_argument("--save-obs", default=None, help="write final <n_i>, bond energies, Lambdas (npz)")
+    ap.add_argument("--no-precision", action="store_true", help="skip the precision-form leg")
     ap.add_argument("--cpu-updates", type=int, default=2)
     ap.add_argument("--outdir", default=os.path.join(ROOT, "gpurun_out"))
     args = ap.parse_args()
