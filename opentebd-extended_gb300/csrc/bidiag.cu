@@ -893,13 +893,50 @@ __device__ __forceinline__ int gk_count_f32(const float *sqf, int n1, float x) {
   return c;
 }
 
+// The count in double-float on off-diagonals scaled by 1/hi (FP32 pipe): each step
+// q = -x - o^2/q with Dekker's double-length division (quotient of the leading
+// parts, remainder from an exact product, one correction).  Sign decisions are
+// good to ~2^-44 ||T||; the FP64 stage checks the bracket it produces.
+__device__ __forceinline__ int gk_count_df(const float2 *sqd, int n1, float xh, float xl) {
+  float qh = -xh, ql = -xl;
+  int c = qh < 0.0f;
+  for (int j = 0; j < n1; ++j) {
+    if (fabsf(qh) < 1e-30f) {
+      qh = -1e-30f;
+      ql = 0.0f;
+    }
+    const float2 a = sqd[j];
+    const float q1 = __fdiv_rn(a.x, qh);
+    const float ph = __fmul_rn(q1, qh);
+    const float pe = fmaf(q1, qh, -ph);
+    // remainder a - q1 q (exact leading difference, then the small terms)
+    const float rh = __fadd_rn(a.x, -ph);
+    const float rr = __fadd_rn(__fadd_rn(rh, -pe), __fadd_rn(a.y, -__fmul_rn(q1, ql)));
+    const float q2 = __fdiv_rn(rr, qh);
+    // t = q1 + q2 (fast two-sum), then q = -x - t
+    const float th = __fadd_rn(q1, q2);
+    const float tl = __fadd_rn(q2, -__fadd_rn(th, -q1));
+    const float sh = __fadd_rn(-xh, -th);
+    const float bp = __fadd_rn(sh, xh);
+    const float err = __fadd_rn(__fadd_rn(-xh, -__fadd_rn(sh, -bp)), __fadd_rn(-th, -bp));
+    const float sl = __fadd_rn(err, __fadd_rn(-xl, -tl));
+    qh = __fadd_rn(sh, sl);
+    ql = __fadd_rn(sl, -__fadd_rn(qh, -sh));
+    c += qh < 0.0f;
+  }
+  return c;
+}
+
 // sigma_i of B for i < min(kk, n), descending.  One thread per value, one warp
 // per block so that the FP64 work spreads over the SMs:
 //   1. FP32 bisection on the scaled problem to width 2^-22 ||T||; FP32 Sturm counts
 //      are exact for a T perturbed by a few float ulps, so the bracket widened by
 //      2^-18 ||T|| holds sigma_i; two FP64 counts check it (reset to [0, ||T||]
 //      otherwise).
-//   2. FP64 bisection to width 2 eps sigma + eps ||T||: the absolute accuracy
+//   2. Double-float bisection (FP32 pipe) to width 2^-42 ||T||; the bracket widened
+//      by 2^-40 ||T|| is checked with two FP64 counts (reset to [0, ||T||]
+//      otherwise).
+//   3. FP64 bisection to width 2 eps sigma + eps ||T||: the absolute accuracy
 //      LAPACK's bidiagonal SVD reaches on Theta as a whole.
 constexpr int kSigmaThreads = 32;
 __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const int *path, int kk) {
@@ -912,8 +949,9 @@ __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const i
   const int K = min(kk, n);
   if ((int)(blockIdx.x * blockDim.x) >= K) return;  // uniform per block
   const int n1 = 2 * n - 1;
-  extern __shared__ double sq[];  // n1 squared off-diagonals, then n1 scaled FP32 copies
-  float *sqf = reinterpret_cast<float *>(sq + n1);
+  extern __shared__ double sq[];  // n1 squared off-diagonals, n1 scaled double-float, n1 scaled FP32
+  float2 *sqd = reinterpret_cast<float2 *>(sq + n1);
+  float *sqf = reinterpret_cast<float *>(sqd + n1);
   const double *dd = S.bdws, *ee = S.bdws + n;
   double hl = 0.0;
   for (int j = threadIdx.x; j < n; j += blockDim.x)
@@ -925,7 +963,10 @@ __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const i
   for (int j = threadIdx.x; j < n1; j += blockDim.x) {
     const double o = (j & 1) ? ee[j >> 1] : dd[j >> 1];
     sq[j] = o * o;
-    sqf[j] = (float)((o * inv_hi) * (o * inv_hi));
+    const double os = (o * inv_hi) * (o * inv_hi);
+    const float oh = (float)os;
+    sqd[j] = make_float2(oh, (float)(os - (double)oh));
+    sqf[j] = oh;
   }
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -941,8 +982,18 @@ __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const i
     else
       hf = mid;
   }
-  double lo = fmax(0.0, ((double)lf - 3.814697265625e-06) * hi);  // widened by 2^-18
-  double h = fmin(1.0, (double)hf + 3.814697265625e-06) * hi;
+  // 2. double-float bisection on the scaled problem from the FP32 bracket widened by 2^-18
+  double ls = fmax(0.0, (double)lf - 3.814697265625e-06), hs = fmin(1.0, (double)hf + 3.814697265625e-06);
+  for (int it = 0; it < 64 && hs - ls > 2.2737367544323206e-13; ++it) {
+    const double mid = 0.5 * (ls + hs);
+    const float mh = (float)mid;
+    if (gk_count_df(sqd, n1, mh, (float)(mid - (double)mh)) <= target)
+      ls = mid;
+    else
+      hs = mid;
+  }
+  double lo = fmax(0.0, ls - 9.094947017729282e-13) * hi;  // widened by 2^-40
+  double h = fmin(1.0, hs + 9.094947017729282e-13) * hi;
   {
     int c0, c1;
     gk_count2(sq, n1, lo, h, pivmin, c0, c1);
@@ -951,7 +1002,7 @@ __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const i
       h = hi;
     }
   }
-  // 2. FP64 bisection
+  // 3. FP64 bisection
   for (int it = 0; it < 160; ++it) {
     if (h - lo <= 4.440892098500626e-16 * h + 2.220446049250313e-16 * hi || h < 1e-30 * hi) break;
     const double mid = 0.5 * (lo + h);
@@ -1537,7 +1588,7 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     ++h->stats.gebrd_launches;
   }
   {
-    const size_t smem = (sizeof(double) + sizeof(float)) * (size_t)(2 * nmax);
+    const size_t smem = (sizeof(double) + sizeof(float2) + sizeof(float)) * (size_t)(2 * nmax);
     if ((rc = check_cuda(h, cudaFuncSetAttribute(k_bd_sigma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)smem),
                          "bisection shared memory")))
