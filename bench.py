@@ -157,9 +157,11 @@ def run_reference(args):
     import multiprocessing as mp
 
     jobs = [(k, gam[k - 1], gam[k], lam[k - 1], lam[k], lam[k + 1], Udt[k - 1]) for k in links]
-    # The reference's update costs the same at every step (ZGESVD('A','A') on the full
-    # 640 x 640 Theta whatever the rank), so a bounded number of rounds measures its
-    # rate: the warm-up rounds size the timed ones to ~90 s.
+    # A bounded number of rounds (sized from the warm-up to ~90 s) of the first odd
+    # sweep's bonds of the initial state.  ZGESVD('A','A') always runs on the full
+    # 640 x 640 Theta, but its iterations converge fastest on this nearly product
+    # state, so this rate overstates the reference's average over the run (the
+    # default GPU run's cpu_baseline times two saturated bonds of the final state).
     with mp.get_context("spawn").Pool(len(links)) as pool:
         tw = time.perf_counter()
         for _ in range(max(1, args.warmup)):
@@ -172,8 +174,8 @@ def run_reference(args):
         wall = time.perf_counter() - t0
     value = len(links) * rounds / wall
     sample = ("%d rounds of %d concurrent bond updates (links %s of the first odd sweep, d=5, chi=128, "
-              "one process per core, OpenBLAS 1 thread each); the reference's cost per update does not "
-              "depend on the step" % (rounds, len(links), ",".join(map(str, links[:4])) + ",..."))
+              "one process per core, OpenBLAS 1 thread each) on the initial state, where ZGESVD "
+              "converges fastest" % (rounds, len(links), ",".join(map(str, links[:4])) + ",..."))
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": args.gpus,
         "steps": args.steps, "timed_rounds": rounds, "warmup": args.warmup, "ms_per_step": wall / rounds * 1e3,
