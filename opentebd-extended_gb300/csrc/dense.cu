@@ -18,6 +18,7 @@
 // factors do not depend on it and the singular values are divided by the norm.
 #include <math.h>
 
+#include "df.cuh"
 #include "tebd_internal.cuh"
 
 namespace tebd {
@@ -154,6 +155,88 @@ __global__ void __launch_bounds__(256) k_theta_form(const double2 *__restrict__ 
       if (c >= n) continue;
       const int lphys = c % d, bp = c / d;
       X[r + (size_t)m * ((size_t)lphys * r2 + bp)] = acc[p][q];
+    }
+  }
+}
+
+// Precision form (TEBD_SVD_DF): the same contraction accumulated in double-float
+// on the FP32 pipe, tiles staged as double-float, the result stored in FP64.
+__global__ void __launch_bounds__(256) k_theta_form_df(const double2 *__restrict__ gam,
+                                                    const double *__restrict__ lam,
+                                                    const int *__restrict__ links, Slot *slots,
+                                                    int chi, int d) {
+  const int s = blockIdx.z;
+  const Compact cp = *slots[s].cp;
+  const int r0b = blockIdx.x * TT_M, c0b = blockIdx.y * TT_N;
+  if (r0b >= cp.m || c0b >= cp.n) return;  // uniform per CTA
+  const int link = links[s];
+  const size_t csz = (size_t)chi * d * chi;
+  const double2 *G1 = gam + (size_t)(link - 1) * csz;
+  const double2 *G2 = gam + (size_t)link * csz;
+  const double *l0 = lam + (size_t)(link - 1) * chi;
+  const double *l1 = lam + (size_t)link * chi;
+  const double *l2 = lam + (size_t)(link + 1) * chi;
+  const int *idx0 = slots[s].idx0, *idx1 = slots[s].idx1, *idx2 = slots[s].idx2;
+  double2 *X = slots[s].X;
+  const int m = cp.m, n = cp.n, r0 = cp.r0, r1 = cp.r1, r2 = cp.r2;
+
+  __shared__ float4 As[TT_K][TT_M + 1];
+  __shared__ float4 Bs[TT_K][TT_N + 1];
+  const int tid = threadIdx.x;
+  const int tr = tid % 16, tc = tid / 16;
+  float4 acc[4][4];  // double-float (re_hi, re_lo, im_hi, im_lo)
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = make_float4(0.f, 0.f, 0.f, 0.f);
+
+  for (int k0 = 0; k0 < r1; k0 += TT_K) {
+    for (int e = tid; e < TT_M * TT_K; e += 256) {
+      const int rr = e % TT_M, kk = e / TT_M;
+      const int r = r0b + rr, gk = k0 + kk;
+      double2 v = make_double2(0.0, 0.0);
+      if (r < m && gk < r1) {
+        const int i = r / r0, a = idx0[r - i * r0], g = idx1[gk];
+        v = cscale(G1[a + (size_t)chi * i + csz / chi * g], l0[a]);
+      }
+      As[kk][rr] = dfs(v);
+    }
+    for (int e = tid; e < TT_K * TT_N; e += 256) {
+      const int kk = e % TT_K, cc = e / TT_K;
+      const int gk = k0 + kk, c = c0b + cc;
+      double2 v = make_double2(0.0, 0.0);
+      if (gk < r1 && c < n) {
+        const int lphys = c % d, b = idx2[c / d], g = idx1[gk];
+        v = cscale(G2[g + (size_t)chi * lphys + (size_t)chi * d * b], l1[g] * l2[b]);
+      }
+      Bs[kk][cc] = dfs(v);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TT_K; ++kk) {
+      float4 a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a[q] = As[kk][tr + 16 * q];
+        b[q] = Bs[kk][tc + 16 * q];
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) df_cmac(acc[p][q].x, acc[p][q].y, acc[p][q].z, acc[p][q].w, a[p], b[q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const int r = r0b + tr + 16 * p;
+    if (r >= m) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = c0b + tc + 16 * q;
+      if (c >= n) continue;
+      const int lphys = c % d, bp = c / d;
+      X[r + (size_t)m * ((size_t)lphys * r2 + bp)] = dfd(acc[p][q]);
     }
   }
 }
@@ -396,8 +479,12 @@ int launch_dense_prepare(tebd_handle *h, int nb, bool /*real_gate: converted on 
   JacobiProblem<double> *jp = reinterpret_cast<JacobiProblem<double> *>(h->jprob_d);
   k_compact<<<nb, 96, 0, st>>>(h->lam, h->links_d, h->slots_d, jp, chi, d);
   TEBD_LAUNCHED(h);
-  k_theta_form<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
-                                                                       h->slots_d, chi, d);
+  if (h->opts.svd_mode == TEBD_SVD_DF)
+    k_theta_form_df<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
+                                                                            h->slots_d, chi, d);
+  else
+    k_theta_form<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
+                                                                         h->slots_d, chi, d);
   TEBD_LAUNCHED(h);
   const size_t gsm = sizeof(double2) * (size_t)d * d * d * d;
   k_gate_apply<<<dim3(cdiv((size_t)chi * chi, 128), nb), 128, gsm, st>>>(h->slots_d, chi, d);
