@@ -133,10 +133,16 @@ int tebd_trotter_step(tebd_handle *h, int order, int n_gates, const double *cons
  * unnormalised Theta, FormLambda1/FormGamma1/FormGamma2.  Dense mode. */
 int tebd_swapping(tebd_handle *h, int link, double *truncerr);
 
-/* TrotterStep2ndOrderPBC (propagation_module.f90:116-198), dense mode, order 2:
- * gates[g-1] = Udt(g), g = 1..L (n_gates >= L), Udt(L) the edge bond applied on
- * bond 1 after Swapping site L down to site 2 (and back).  The Forest-Ruth PBC
- * step (TrotterStep5thOrderPBC) is not provided (order != 2 -> TEBD_ERR_ARG). */
+/* Periodic-boundary Trotter step, dense mode; replaces TrotterStep with
+ * BoundaryCond='P' (propagation_module.f90:42-79).  The edge bond (L,1) is
+ * applied on bond 1 after Swapping site L down to site 2, and swapped back.
+ * gates[g-1] = Udt(g) in NEWConstructPropagators' periodic layout
+ * (TEBDtools_module.f90:1100-1190):
+ *   order 2 (TrotterStep2ndOrderPBC :116-198): g = 1..L, Udt(L) the edge
+ *     (n_gates >= L);
+ *   order 5 (TrotterStep5thOrderPBC :254-614), odd L: odd bond i Udt(3(i-1)+1..2),
+ *     even bond i Udt(2+3(i-2)+1..4), edge Udt(3(L-1)+1..3) (n_gates >= 3L);
+ *     even L: bond i Udt(2(i-1)+1..2), edge Udt(2(L-1)+1..2) (n_gates >= 2L). */
 int tebd_trotter_step_pbc(tebd_handle *h, int order, int n_gates, const double *const *gates,
                           double *total_truncerr);
 
@@ -148,9 +154,20 @@ int tebd_trotter_step_pbc(tebd_handle *h, int order, int n_gates, const double *
 int tebd_canonical_form(tebd_handle *h, int link);
 int tebd_canonical_form_all(tebd_handle *h);
 
-/* CanonicalFormAllNC (propagation_module.f90:1943-1983, no intDegFree): the
- * identity TwoSiteOpNC on links 1..L-1 then L-1..1.  NC mode. */
+/* CanonicalFormAllNC (propagation_module.f90:1943-1983): the identity
+ * TwoSiteOpNC on links 1..L-1 then L-1..1.  NC mode; follows tebd_set_conserv. */
 int tebd_canonical_form_all_nc(tebd_handle *h);
+
+/* Internal degrees of freedom for every NC routine of the handle: the reference
+ * passes the OPTIONAL argument intDegFree to TwoSiteOpNC, TrotterStepNC and
+ * CanonicalFormAllNC (local_operations_module.f90:748-1443, 1723-1964;
+ * propagation_module.f90:890-1018, 1943-1983) and then takes the particle number
+ * of local state i from the module global Conserv%vi(i) instead of i-1
+ * (set by the Hamiltonian builders, e.g. fermi_hubbard_module.f90:230-232).
+ * conserv: d numbers >= 0 (Conserv%vi), or NULL for the form without intDegFree.
+ * NC mode, d <= 8; at most 16 local pairs (i, j) may share one pair total
+ * n_i + n_j (TEBD_ERR_ARG otherwise). */
+int tebd_set_conserv(tebd_handle *h, const int *conserv);
 
 /* Singular values of the normalised Theta from the last update of `link`
  * (descending; NC mode: the flattened block values in the reference's order).

@@ -629,56 +629,110 @@ extern "C" int tebd_swapping(tebd_handle *h, int link, double *truncerr) {
   return rc;
 }
 
-// TrotterStep2ndOrderPBC (propagation_module.f90:116-198): gates[g-1] = Udt(g),
-// g = 1..L, Udt(L) the edge gate.  Site L is swapped down to position 2, the
-// edge gate acts on bond 1 and the swaps are undone; truncation errors of every
-// update and swap are summed in the reference's order.
+// TrotterStep2ndOrderPBC (propagation_module.f90:116-198) and
+// TrotterStep5thOrderPBC (:254-614).  gates[g-1] = Udt(g) in the periodic layout
+// of NEWConstructPropagators.  The edge gate acts on bond 1 between a swap of
+// site L down to position 2 and the swap back; same-parity bulk bonds are
+// batched; truncation errors of every update and swap are summed in the
+// reference's order.
 extern "C" int tebd_trotter_step_pbc(tebd_handle *h, int order, int n_gates, const double *const *gates,
                                      double *total_truncerr) {
   if (!h || !gates || !total_truncerr) return TEBD_ERR_ARG;
   if (h->mode != TEBD_MODE_DENSE) return set_error(h, TEBD_ERR_STATE, "the PBC Trotter step needs a dense handle");
-  if (order != 2) return set_error(h, TEBD_ERR_ARG, "periodic boundaries: only the 2nd-order step is provided");
+  if (order != 2 && order != 5) return set_error(h, TEBD_ERR_ARG, "periodic boundaries: order must be 2 or 5");
   const int L = h->L;
   if (L < 3) return set_error(h, TEBD_ERR_ARG, "periodic boundaries need L >= 3");
-  if (n_gates < L) return set_error(h, TEBD_ERR_ARG, "periodic boundaries need L gates (Udt(L) = edge)");
+  const int need = order == 2 ? L : (L % 2 == 1 ? 3 * L : 2 * L);
+  if (n_gates < need)
+    return set_error(h, TEBD_ERR_ARG, order == 2 ? "periodic 2nd order needs L gates (Udt(L) = edge)"
+                                                  : "periodic Forest-Ruth needs 3L gates (odd L) or 2L (even L)");
+  for (int g = 0; g < need; ++g)
+    if (!gates[g]) return set_error(h, TEBD_ERR_ARG, "NULL gate");
   double total = 0.0;
   std::vector<int> links;
   std::vector<const double *> gp;
   std::vector<double> te;
-  auto sweep = [&](int first) -> int {  // bonds first, first+2, ... with Udt(link)
+  // bonds first, first+2, ..., L-1 with Udt(base + step * (link - first0)) style indices
+  auto sweep = [&](int first, int (*gidx)(int, int, int), int v) -> int {
     links.clear();
     gp.clear();
     for (int link = first; link <= L - 1; link += 2) {
       links.push_back(link);
-      gp.push_back(gates[link - 1]);
+      gp.push_back(gates[gidx(link, L, v) - 1]);
     }
     te.assign(links.size(), 0.0);
     const int rc = apply_bonds_impl(h, (int)links.size(), links.data(), gp.data(), te.data());
-    for (double v : te) total = total + v;
+    for (double x : te) total = total + x;
     return rc;
   };
-  auto swap = [&](int link) -> int {
+  auto edge = [&](int g) -> int {
+    int rc;
+    for (int i = L - 1; i >= 2; --i) {
+      double t = 0.0;
+      if ((rc = tebd_swapping(h, i, &t))) return rc;
+      total = total + t;
+    }
     double t = 0.0;
-    const int rc = tebd_swapping(h, link, &t);
-    total = total + t;
-    return rc;
-  };
-  int rc;
-  if ((rc = sweep(1))) return rc;
-  if (L % 2 == 1 && (rc = sweep(2))) return rc;
-  for (int i = L - 1; i >= 2; --i)
-    if ((rc = swap(i))) return rc;
-  {
-    double t = 0.0;
-    const double *ge = gates[L - 1];
+    const double *ge = gates[g - 1];
     const int link = 1;
     if ((rc = apply_bonds_impl(h, 1, &link, &ge, &t))) return rc;
     total = total + t;
+    for (int i = 2; i <= L - 1; ++i) {
+      double t2 = 0.0;
+      if ((rc = tebd_swapping(h, i, &t2))) return rc;
+      total = total + t2;
+    }
+    return TEBD_OK;
+  };
+  int rc = TEBD_OK;
+#define PBC_DO(x) \
+  if ((rc = (x))) return rc
+  if (order == 2) {
+    auto same = [](int link, int, int) { return link; };
+    PBC_DO(sweep(1, same, 0));
+    if (L % 2 == 1) PBC_DO(sweep(2, same, 0));
+    PBC_DO(edge(L));
+    PBC_DO(sweep(2, same, 0));
+    PBC_DO(sweep(1, same, 0));
+  } else if (L % 2 == 1) {
+    // odd L: odd bonds Udt(3(i-1)+v), even bonds Udt(2+3(i-2)+v), edge Udt(3(L-1)+v)
+    auto odd = [](int i, int, int v) { return 3 * (i - 1) + v; };
+    auto even = [](int i, int, int v) { return 2 + 3 * (i - 2) + v; };
+    const int e0 = 3 * (L - 1);
+    // Forest-Ruth on the even bonds and the edge, nested in each even half-step
+    auto nested = [&](int a, int b, int ea, int eb) -> int {
+      int r;
+      if ((r = sweep(2, even, a))) return r;
+      if ((r = edge(e0 + ea))) return r;
+      if ((r = sweep(2, even, b))) return r;
+      if ((r = edge(e0 + eb))) return r;
+      if ((r = sweep(2, even, b))) return r;
+      if ((r = edge(e0 + ea))) return r;
+      return sweep(2, even, a);
+    };
+    PBC_DO(sweep(1, odd, 1));
+    PBC_DO(nested(1, 2, 1, 2));
+    PBC_DO(sweep(1, odd, 2));
+    PBC_DO(nested(3, 4, 2, 3));
+    PBC_DO(sweep(1, odd, 2));
+    PBC_DO(nested(1, 2, 1, 2));
+    PBC_DO(sweep(1, odd, 1));
+  } else {
+    // even L: bond i Udt(2(i-1)+v), edge Udt(2(L-1)+v); the edge commutes with the even bonds
+    auto both = [](int i, int, int v) { return 2 * (i - 1) + v; };
+    const int e0 = 2 * (L - 1);
+    PBC_DO(sweep(1, both, 1));
+    PBC_DO(edge(e0 + 1));
+    PBC_DO(sweep(2, both, 1));
+    PBC_DO(sweep(1, both, 2));
+    PBC_DO(edge(e0 + 2));
+    PBC_DO(sweep(2, both, 2));
+    PBC_DO(sweep(1, both, 2));
+    PBC_DO(edge(e0 + 1));
+    PBC_DO(sweep(2, both, 1));
+    PBC_DO(sweep(1, both, 1));
   }
-  for (int i = 2; i <= L - 1; ++i)
-    if ((rc = swap(i))) return rc;
-  if ((rc = sweep(2))) return rc;
-  if ((rc = sweep(1))) return rc;
+#undef PBC_DO
   *total_truncerr = total;
   return TEBD_OK;
 }

@@ -1,7 +1,7 @@
 // nc.cu -- number-conserving (U(1) block-sparse) two-site update on the GPU.
 //
-// Replaces TwoSiteOpNC_c/_r without internal degrees of freedom
-// (VidalCore_v_2.0/local_operations_module.f90:1723-1964) for a batch of
+// Replaces TwoSiteOpNC_c/_r, with or without internal degrees of freedom
+// (VidalCore_v_2.0/local_operations_module.f90:748-1964) for a batch of
 // same-parity bonds:
 //   minmaxNLR :1201, SizeOfBlocks :1252, IndexLeft/Right :1339/:1393   -> k_nc_blocks
 //   FormThetaNC :748, ThetaOperationNC :853/:950, RenormThetaNC :1046,
@@ -24,6 +24,12 @@
 // an allowed entry, so no block needs clearing.  Blocks with fewer rows than
 // columns are stored conjugate-transposed so the one-sided Jacobi always works
 // on the narrow side.
+//
+// Internal degrees of freedom (intDegFree present, tebd_set_conserv): local state
+// i carries Conserv(i) particles instead of i-1, so several (i, j) pairs share one
+// pair total n_i + n_j.  The block bookkeeping reads the table; the Theta kernel
+// runs a second form that lists the allowed pairs of each (alpha, gamma) in the
+// reference's loop order (i outer, j inner) and mixes them with the gate.
 //
 // Guards and the sentinel are the reference's: labels >= 1000 are unused,
 // 10000 is written for unused indices, and `10.0**(-10)` (single precision)
@@ -59,6 +65,11 @@ struct NcSlot {
   double *part;                   // kNormParts partial sums of |Theta'|^2
 };
 
+// local particle numbers: Conserv(i) with intDegFree, i-1 (0-based i) without
+struct NcLocal {
+  int n[8];
+};
+
 struct NcWorkspace {
   int bmax;
   std::vector<NcSlot> slots;
@@ -76,7 +87,7 @@ struct NcWorkspace {
 // ---------------------------------------------------------------------------
 __global__ void k_nc_blocks(const int *__restrict__ lab_l, const int *__restrict__ lab_r,
                             const int *links, Slot *slots, NcSlot *nc, JacobiProblem<double> *probs,
-                            int chi, int d, int totNum, int maxFilling, int bmax) {
+                            int chi, int d, int totNum, int maxFilling, int bmax, NcLocal nl) {
   const int s = blockIdx.x;
   if (threadIdx.x != 0) return;
   const int link = links[s];
@@ -120,17 +131,17 @@ __global__ void k_nc_blocks(const int *__restrict__ lab_l, const int *__restrict
   }
   S.hdr[H_NB] = nb;
   for (int k = 0; k < nb; ++k) S.rows[k] = S.cols[k] = 0;
-  // SizeOfBlocks (:1305-1335)
+  // SizeOfBlocks (:1252-1336)
   for (int a = 0; a < chi; ++a)
     for (int i = 0; i < d; ++i)
       if (ll0[a] < 1000) {
-        const int NL = ll0[a] + i;
+        const int NL = ll0[a] + nl.n[i];
         if (mnl <= NL && NL <= mxl) S.rows[NL - mnl]++;
       }
   for (int g = 0; g < chi; ++g)
     for (int j = 0; j < d; ++j)
       if (lr2[g] < 1000) {
-        const int NR = lr2[g] + j;
+        const int NR = lr2[g] + nl.n[j];
         if (mnr <= NR && NR <= mxr) {
           const int k = totNum - NR - mnl;
           if (k < 0 || k >= nb) {
@@ -154,13 +165,13 @@ __global__ void k_nc_blocks(const int *__restrict__ lab_l, const int *__restrict
   }
   S.hdr[H_SZ] = S.soff[nb];
   S.hdr[H_MAXDIM] = maxdim;
-  // IndexLeft (:1379-1391) and IndexRight (:1431-1443)
+  // IndexLeft (:1339-1391) and IndexRight (:1393-1443)
   for (int e = 0; e < chi * d; ++e) S.rowpos[e] = S.colpos[e] = -1;
   for (int k = 0; k < nb; ++k) S.rows[k] = 0;  // reused as fill counters
   for (int a = 0; a < chi; ++a)
     for (int i = 0; i < d; ++i)
-      if (ll0[a] < 1000 && mnl <= ll0[a] + i && ll0[a] + i <= mxl) {
-        const int k = ll0[a] + i - mnl;
+      if (ll0[a] < 1000 && mnl <= ll0[a] + nl.n[i] && ll0[a] + nl.n[i] <= mxl) {
+        const int k = ll0[a] + nl.n[i] - mnl;
         const int p = S.roff[k] + S.rows[k]++;
         S.l_alpha[p] = a;
         S.l_i[p] = i;
@@ -169,8 +180,8 @@ __global__ void k_nc_blocks(const int *__restrict__ lab_l, const int *__restrict
   for (int k = 0; k < nb; ++k) S.cols[k] = 0;
   for (int g = 0; g < chi; ++g)
     for (int j = 0; j < d; ++j)
-      if (lr2[g] < 1000 && mnr <= lr2[g] + j && lr2[g] + j <= mxr) {
-        const int k = totNum - (lr2[g] + j) - mnl;
+      if (lr2[g] < 1000 && mnr <= lr2[g] + nl.n[j] && lr2[g] + nl.n[j] <= mxr) {
+        const int k = totNum - (lr2[g] + nl.n[j]) - mnl;
         const int p = S.coff[k] + S.cols[k]++;
         S.r_gamma[p] = g;
         S.r_j[p] = j;
@@ -212,13 +223,16 @@ __global__ void k_nc_blocks(const int *__restrict__ lab_l, const int *__restrict
 // each, so the norm's summation order is fixed.
 // ---------------------------------------------------------------------------
 constexpr int kMaxDnc = 8;
+constexpr int kMaxPairs = 16;  // allowed (i, j) pairs of one pair total, intDegFree form
+static_assert(kMaxDnc <= 8, "NcLocal and the handle's table hold 8 local numbers");
 
+template <bool kIdf>
 __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ gam,
                                                   const double *__restrict__ lam,
                                                   const int *__restrict__ lab_l,
                                                   const int *__restrict__ lab_r, const int *links,
                                                   Slot *slots, NcSlot *nc, int chi, int d,
-                                                  int totNum, int maxFilling) {
+                                                  int totNum, int maxFilling, NcLocal nl) {
   const int s = blockIdx.y;
   const NcSlot S = nc[s];
   __shared__ double red[256];
@@ -245,6 +259,61 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
     const int lftN = ll0[a], rgtN = lr2[g];
     if (max(lftN, rgtN) >= 1000) continue;
     const int ntot = totNum - lftN - rgtN;
+    if (kIdf) {
+      // intDegFree form.  Pairs (i, l) with 0 <= ntot - n_i <= maxFilling and
+      // n_l = ntot - n_i, i outer and l inner: the entries ThetaOperationNC reads
+      // and writes (:970-1010) and RenormThetaNC sums (:1062-1102).
+      double2 th[kMaxPairs];
+      int pi[kMaxPairs], pl[kMaxPairs];
+      int np = 0;
+      for (int i = 0; i < d; ++i) {
+        const int r = ntot - nl.n[i];
+        if (r < 0 || r > maxFilling) continue;
+        for (int l = 0; l < d && np < kMaxPairs; ++l) {
+          if (nl.n[l] != r) continue;
+          // FormThetaNC (:772-818): betas with LabelLeft(link+1) = lftN + n_i and
+          // LabelRight(link+1) = rgtN + n_l, both differences within [0, maxFilling]
+          double2 sacc = make_double2(0.0, 0.0);
+          const int q = lftN + nl.n[i];
+          if (nl.n[i] <= maxFilling && q >= 0 && q <= totNum) {
+            for (int p = S.cls_off[q]; p < S.cls_off[q + 1]; ++p) {
+              const int b = S.cls_beta[p];
+              const int rgtN2 = lr1[b];
+              if (rgtN2 >= 1000 || rgtN2 - rgtN != r) continue;
+              const double2 x = G1[a + (size_t)chi * i + (size_t)chi * d * b];
+              const double2 y = G2[b + (size_t)chi * l + (size_t)chi * d * g];
+              const double w = l0[a] * l1[b] * l2[g];
+              sacc.x += w * (x.x * y.x - x.y * y.y);
+              sacc.y += w * (x.x * y.y + x.y * y.x);
+            }
+          }
+          th[np] = sacc;
+          pi[np] = i;
+          pl[np] = l;
+          ++np;
+        }
+      }
+      for (int o = 0; o < np; ++o) {
+        const int k = pi[o], jj = pl[o];
+        double2 v = make_double2(0.0, 0.0);
+        for (int p = 0; p < np; ++p) {
+          const double2 gv = op[(size_t)(k * d + jj) + (size_t)d2 * (pi[p] * d + pl[p])];
+          v.x += gv.x * th[p].x - gv.y * th[p].y;
+          v.y += gv.x * th[p].y + gv.y * th[p].x;
+        }
+        acc += v.x * v.x + v.y * v.y;
+        const int rp = S.rowpos[a * d + k], cpn = S.colpos[g * d + jj];
+        if (nb == 0 || rp < 0 || cpn < 0) continue;
+        const int blk = lftN + nl.n[k] - mnl;
+        const int m = S.rows[blk], n = S.cols[blk];
+        double2 *Xk = slots[s].X + S.boffx[blk];
+        if (m >= n)
+          Xk[rp + (size_t)m * cpn] = v;
+        else
+          Xk[cpn + (size_t)n * rp] = make_double2(v.x, -v.y);
+      }
+      continue;
+    }
     // FormThetaNC restricted to the entries ThetaOperationNC reads: (i, ll = ntot - i)
     double2 th[kMaxDnc];
     for (int i = 0; i < d; ++i) {
@@ -581,12 +650,22 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
   const int chi = h->chi, d = h->d, bmax = w->bmax;
   const int N = h->opts.tot_num, mf = h->opts.max_filling;
   if (d > kMaxDnc) return set_error(h, TEBD_ERR_ARG, "NC mode supports d <= 8");
+  // Without intDegFree the second physical index is a particle number (up to
+  // maxFilling), so it must stay below d.
+  if (!h->nc_idf && mf > d - 1)
+    return set_error(h, TEBD_ERR_ARG, "NC mode without internal degrees of freedom needs max_filling <= d-1");
+  NcLocal nl;
+  for (int i = 0; i < 8; ++i) nl.n[i] = (h->nc_idf && i < d) ? h->nc_conserv[i] : i;
   cudaStream_t st = h->stream;
   k_nc_blocks<<<nb, 32, 0, st>>>(h->lab_l, h->lab_r, h->links_d, h->slots_d, w->slots_d, w->probs_d,
-                                 chi, d, N, mf, bmax);
+                                 chi, d, N, mf, bmax, nl);
   TEBD_LAUNCHED(h);
-  k_nc_theta<<<dim3(kNormParts, nb), 256, 0, st>>>(h->gam, h->lam, h->lab_l, h->lab_r, h->links_d,
-                                                   h->slots_d, w->slots_d, chi, d, N, mf);
+  if (h->nc_idf)
+    k_nc_theta<true><<<dim3(kNormParts, nb), 256, 0, st>>>(h->gam, h->lam, h->lab_l, h->lab_r, h->links_d,
+                                                           h->slots_d, w->slots_d, chi, d, N, mf, nl);
+  else
+    k_nc_theta<false><<<dim3(kNormParts, nb), 256, 0, st>>>(h->gam, h->lam, h->lab_l, h->lab_r, h->links_d,
+                                                            h->slots_d, w->slots_d, chi, d, N, mf, nl);
   TEBD_LAUNCHED(h);
   k_nc_prepare_svd<<<dim3(32, nb), 256, 0, st>>>(w->slots_d, w->probs_d, h->nrm, bmax, h->status_d);
   TEBD_LAUNCHED(h);
@@ -622,3 +701,31 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
 }
 
 }  // namespace tebd
+
+// Internal degrees of freedom (intDegFree + Conserv%vi) for the handle's NC routines.
+extern "C" int tebd_set_conserv(tebd_handle *h, const int *conserv) {
+  using namespace tebd;
+  if (!h) return TEBD_ERR_ARG;
+  if (h->mode != TEBD_MODE_NC) return set_error(h, TEBD_ERR_STATE, "tebd_set_conserv needs a TEBD_MODE_NC handle");
+  if (!conserv) {
+    h->nc_idf = 0;
+    return TEBD_OK;
+  }
+  const int d = h->d;
+  if (d > kMaxDnc) return set_error(h, TEBD_ERR_ARG, "intDegFree: d <= 8");
+  int mx = 0;
+  for (int i = 0; i < d; ++i) {
+    if (conserv[i] < 0 || conserv[i] >= 1000) return set_error(h, TEBD_ERR_ARG, "intDegFree: Conserv values in [0, 1000)");
+    mx = std::max(mx, conserv[i]);
+  }
+  // pairs (i, j) per pair total, as the Theta kernel lists them
+  for (int t = 0; t <= 2 * mx; ++t) {
+    int np = 0;
+    for (int i = 0; i < d; ++i)
+      for (int j = 0; j < d; ++j) np += (conserv[i] + conserv[j] == t);
+    if (np > kMaxPairs) return set_error(h, TEBD_ERR_ARG, "intDegFree: more than 16 local pairs share one pair total");
+  }
+  for (int i = 0; i < 8; ++i) h->nc_conserv[i] = i < d ? conserv[i] : 0;
+  h->nc_idf = 1;
+  return TEBD_OK;
+}

@@ -155,6 +155,9 @@ struct tebd_handle {
   void *nc_ws;
   size_t nc_ws_bytes;
   void *nc_meta;  // host-side NC slot table (nc.cu)
+  // internal degrees of freedom (tebd_set_conserv): local particle numbers
+  int nc_idf;                    // 1: the intDegFree branches, 0: local number i-1
+  int nc_conserv[8];             // Conserv%vi(1..d)
   // last spectrum per link (tebd_get_singular_values / tebd_get_sweeps)
   double *sig_link_d;            // (L-1) * n
   int *sig_count_d;              // L-1

@@ -124,9 +124,14 @@ def forest_ruth_theta():
     return 1.0 / (2.0 - 2.0 ** float(np.float32(1.0) / np.float32(3.0)))
 
 
-def construct_propagators(H, dt, order=2):
-    """NEWConstructPropagators (TEBDtools_module.f90:1079-1196), BoundaryCond='O'.
-    Returns Udt as a list indexed like the reference's Udt(1..)."""
+def construct_propagators(H, dt, order=2, boundary="O"):
+    """NEWConstructPropagators (TEBDtools_module.f90:1079-1196).  Returns Udt as a
+    list indexed like the reference's Udt(1..).  BoundaryCond='O': H holds the L-1
+    bond terms; 'P': L terms, H(L) the edge bond (site 1 left, site L right)."""
+    if boundary == "P":
+        return _construct_propagators_pbc(H, dt, order)
+    if boundary != "O":
+        raise ValueError("boundary must be 'O' or 'P'")
     L1 = len(H)  # L - 1 bonds
     if order == 2:
         return [matrix_exponential(H[i], (0.5 if (i + 1) % 2 == 1 else 1.0) * dt) for i in range(L1)]
@@ -144,6 +149,44 @@ def construct_propagators(H, dt, order=2):
     return U
 
 
+def _construct_propagators_pbc(H, dt, order):
+    """BoundaryCond='P' branches of NEWConstructPropagators (TEBDtools_module.f90:
+    1100-1127 for order 2, 1149-1190 for order 5).  Even L: the edge term commutes
+    with the even bonds, so both take full steps; odd L: the even bonds take half
+    steps around the edge (order 2), or the nested Forest-Ruth fractions (order 5)."""
+    L = len(H)
+    ex = matrix_exponential
+    if order == 2:
+        even = 1.0 if L % 2 == 0 else 0.5
+        U = [ex(H[i - 1], (0.5 if i % 2 == 1 else even) * dt) for i in range(1, L)]
+        return U + [ex(H[L - 1], dt)]
+    if order != 5:
+        raise ValueError("order must be 2 or 5")
+    th = forest_ruth_theta()
+    if L % 2 == 0:
+        U = [None] * (2 * L)
+        for i in range(1, L):
+            f = (0.5 * th, 0.5 * (1.0 - th)) if i % 2 == 1 else (th, 1.0 - 2.0 * th)
+            U[2 * (i - 1)] = ex(H[i - 1], f[0] * dt)
+            U[2 * (i - 1) + 1] = ex(H[i - 1], f[1] * dt)
+        U[2 * (L - 1)] = ex(H[L - 1], th * dt)
+        U[2 * (L - 1) + 1] = ex(H[L - 1], (1.0 - 2.0 * th) * dt)
+        return U
+    U = [None] * (3 * L)
+    for i in range(1, L, 2):
+        U[3 * (i - 1)] = ex(H[i - 1], 0.5 * th * dt)
+        U[3 * (i - 1) + 1] = ex(H[i - 1], 0.5 * (1.0 - th) * dt)
+    for i in range(2, L, 2):
+        fr = (0.5 * th * th, 0.5 * (1.0 - th) * th, 0.5 * (1.0 - 2.0 * th) * th,
+              0.5 * (1.0 - th) * (1.0 - 2.0 * th))
+        for v in range(4):
+            U[2 + 3 * (i - 2) + v] = ex(H[i - 1], fr[v] * dt)
+    U[3 * (L - 1)] = ex(H[L - 1], th * th * dt)
+    U[3 * (L - 1) + 1] = ex(H[L - 1], (1.0 - 2.0 * th) * th * dt)
+    U[3 * (L - 1) + 2] = ex(H[L - 1], (1.0 - 2.0 * th) * (1.0 - 2.0 * th) * dt)
+    return U
+
+
 # ---------------------------------------------------------------------------
 # initial states
 # ---------------------------------------------------------------------------
@@ -157,6 +200,27 @@ def product_state(carray, chi):
         lam[i][0] = 1.0
     lam[L][0] = 1.0
     return gam, lam
+
+
+def product_state_labels(carray, chi, tot_num, conserv=None):
+    """ProductStateLabels (Hamiltonian_tools_module.f90:124-178) for a product state
+    of definite total number.  Plain form: the number of site i is j-1 of the LAST
+    nonzero carray(j, i); with internal degrees of freedom (``conserv`` =
+    Conserv%vi) it is Conserv(j) of the FIRST nonzero component, as there.
+    Returns LabelLeft, LabelRight (10000 = unused)."""
+    d, L = carray.shape
+    ll = [np.full(chi, 10000, dtype=np.int32) for _ in range(L + 1)]
+    lr = [np.full(chi, 10000, dtype=np.int32) for _ in range(L + 1)]
+    ll[0][0] = 0
+    for i in range(L):
+        nz = [j for j in range(d) if abs(carray[j, i]) != 0.0]
+        if not nz:
+            raise ValueError("site %d has no nonzero component" % (i + 1))
+        n = conserv[nz[0]] if conserv is not None else nz[-1]
+        ll[i + 1][0] = ll[i][0] + n
+    for i in range(L + 1):
+        lr[i][0] = tot_num - ll[i][0]
+    return ll, lr
 
 
 def initial_set_nc(L, d, chi, tot_num):

@@ -68,7 +68,7 @@ EXPORTED_SYMBOLS = (
     "tebd_local_energy", "tebd_total_energy", "tebd_inner_product", "tebd_chain_entropy",
     "tebd_record_lambdas", "tebd_record_gammas", "tebd_record_labels", "tebd_read_gamma_lambda",
     "tebd_read_gamma_lambda_labels", "tebd_swapping", "tebd_trotter_step_pbc", "tebd_canonical_form_all_nc",
-    "tebd_canonical_form", "tebd_canonical_form_all",
+    "tebd_canonical_form", "tebd_canonical_form_all", "tebd_set_conserv",
 )
 
 
@@ -175,6 +175,7 @@ def load_library(path: str = LIB_PATH):
     L.tebd_swapping.argtypes = [vp, ctypes.c_int, dp]
     L.tebd_trotter_step_pbc.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(dp), dp]
     L.tebd_canonical_form_all_nc.argtypes = [vp]
+    L.tebd_set_conserv.argtypes = [vp, ip]
     L.tebd_canonical_form.argtypes = [vp, ctypes.c_int]
     L.tebd_canonical_form_all.argtypes = [vp]
     cp = ctypes.c_char_p
@@ -208,7 +209,8 @@ class Chain:
     and in number-conserving mode LabelLeft/LabelRight (L+1, chi)."""
 
     def __init__(self, L, d, chi, mode=MODE_DENSE, tot_num=0, max_filling=None,
-                 svd_mode=SVD_FP64, max_sweeps=0, max_batch=0, jacobi_tol=0.0, device=0):
+                 svd_mode=SVD_FP64, max_sweeps=0, max_batch=0, jacobi_tol=0.0, device=0,
+                 conserv=None):
         self._lib = load_library()
         o = Opts()
         self._lib.tebd_default_opts(ctypes.byref(o))
@@ -226,6 +228,23 @@ class Chain:
         self.h = h
         self.L, self.d, self.chi, self.mode = L, d, chi, mode
         self.tot_num, self.max_filling = o.tot_num, o.max_filling
+        self.conserv = None
+        if conserv is not None:
+            self.set_conserv(conserv)
+
+    def set_conserv(self, conserv):
+        """Internal degrees of freedom for the NC routines: ``conserv`` = Conserv%vi
+        (d particle numbers) stands for the reference's OPTIONAL intDegFree argument
+        plus its Conserv global; None restores the plain form (number i-1)."""
+        if conserv is None:
+            self._check(self._lib.tebd_set_conserv(self.h, None))
+            self.conserv = None
+            return
+        c = np.ascontiguousarray(conserv, dtype=np.int32)
+        if c.shape != (self.d,):
+            raise ValueError("conserv needs d = %d entries" % self.d)
+        self._check(self._lib.tebd_set_conserv(self.h, c.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        self.conserv = c.copy()
 
     # -- lifetime -------------------------------------------------------------
     def close(self):
@@ -347,12 +366,14 @@ class Chain:
         self._check(self._lib.tebd_swapping(self.h, link, _dp(te)))
         return float(te[0])
 
-    def trotter_step_pbc(self, Udt):
-        """TrotterStep2ndOrderPBC; Udt[g-1] = Udt(g), g = 1..L, Udt(L) the edge bond."""
+    def trotter_step_pbc(self, Udt, order=2):
+        """TrotterStep2ndOrderPBC / TrotterStep5thOrderPBC (BoundaryCond='P'); Udt in
+        NEWConstructPropagators' periodic layout: L gates for order 2 (Udt(L) the
+        edge bond), 3L (odd L) or 2L (even L) for order 5."""
         gs = [_as_gate(g, self.d) for g in Udt]
         arr = (ctypes.POINTER(ctypes.c_double) * len(gs))(*[_dp(g) for g in gs])
         te = np.zeros(1)
-        self._check(self._lib.tebd_trotter_step_pbc(self.h, 2, len(gs), arr, _dp(te)))
+        self._check(self._lib.tebd_trotter_step_pbc(self.h, order, len(gs), arr, _dp(te)))
         return float(te[0])
 
     def canonical_form(self, link):

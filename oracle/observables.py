@@ -8,6 +8,8 @@ numpy restatements of the reference's observables (VidalCore_v_2.0/observables_m
 * :func:`bond_energy`      -- the per-bond term of TotalEnergy (:1432-1466)
 * :func:`inner_product`    -- InnerProduct (:1031-1089)
 * :func:`chain_entropy`    -- entanglement entropy of each Lambda, base d (ChainEntropy, :1583)
+* :func:`state_vector`     -- the dense state of a small chain (no reference routine;
+  used for exact-evolution known answers)
 
 Gamma arrays are (chi, d, chi) complex, Lambdas (chi,) real, all 0-based lists.
 """
@@ -76,3 +78,15 @@ def chain_entropy(lambdas, d):
         p = l[l != 0] ** 2
         out.append(float(-(p * np.log(np.abs(p))).sum() / np.log(d)))
     return np.array(out)
+
+
+def state_vector(gammas, lambdas):
+    """Dense state of a small open chain in Vidal form (test helper): the sum over
+    Schmidt indices of Lambda(1) Gamma(1) Lambda(2) ... Gamma(L) Lambda(L+1),
+    closed on the first index of the edge Lambdas (e_1 there).  Local index of
+    site 1 is the slowest; d**L entries."""
+    chi = gammas[0].shape[0]
+    r = np.asarray(lambdas[0], dtype=complex)[None, :]
+    for s, g in enumerate(gammas):
+        r = np.einsum("pa,aib,b->pib", r, g, lambdas[s + 1]).reshape(-1, chi)
+    return r[:, 0].copy()

@@ -10,10 +10,13 @@ OpenTEBD-extended tree):
 
 * :func:`two_site_op`     -- ``TwoSiteOp_c``/``TwoSiteOp_r``
   (VidalCore_v_2.0/local_operations_module.f90:430-494)
-* :func:`two_site_op_nc`  -- ``TwoSiteOpNC_c``/``_r`` without internal degrees of
-  freedom (local_operations_module.f90:1723-1964)
+* :func:`two_site_op_nc`  -- ``TwoSiteOpNC_c``/``_r``, with or without internal
+  degrees of freedom (local_operations_module.f90:748-1964; ``conserv`` stands
+  for the optional ``intDegFree`` argument plus the global ``Conserv%vi``)
 * :func:`trotter_step`, :func:`trotter_step_nc` -- ``TrotterStep2ndOrder`` /
   ``TrotterStep5thOrder`` and NC twins (propagation_module.f90:82-252, 956-1018)
+* :func:`trotter_step_pbc` -- ``TrotterStep2ndOrderPBC`` / ``TrotterStep5thOrderPBC``
+  (propagation_module.f90:116-198, 254-614)
 
 Parity unpinned: the reference is Fortran, no Fortran compiler is available
 where this oracle is built, and the reference holds no tests or golden vectors.
@@ -75,6 +78,8 @@ def lib():
     L.oracle_swapping.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp]
     L.oracle_canonical_form.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp]
     L.oracle_trotter_step_pbc.argtypes = [ctypes.c_int] * 3 + [ctypes.POINTER(dp)] * 3 + [dp]
+    L.oracle_trotter_step_pbc5.argtypes = [ctypes.c_int] * 3 + [ctypes.POINTER(dp)] * 3 + [dp]
+    L.oracle_set_conserv.argtypes = [ctypes.c_int, ip]
     L.oracle_trotter_step_nc.argtypes = (
         [ctypes.c_int] * 6 + [ctypes.POINTER(dp)] * 2 + [ctypes.POINTER(ip)] * 2 + [ctypes.POINTER(dp), dp]
     )
@@ -127,10 +132,24 @@ def two_site_op(gamma1, gamma2, lam0, lam1, lam2, op2):
     return g1, g2, l1, float(te[0]), s
 
 
-def two_site_op_nc(gamma1, gamma2, lam0, lam1, lam2, op2, ll0, ll1, lr1, lr2, tot_num, max_filling):
-    """One number-conserving bond update (intDegFree absent).  Returns
+def _set_conserv(d, conserv):
+    """Select the intDegFree branches with local numbers ``conserv`` (Conserv%vi),
+    or the plain ones (local number i-1) for None."""
+    if conserv is None:
+        _check(lib().oracle_set_conserv(d, None), "oracle_set_conserv")
+        return
+    c = np.ascontiguousarray(conserv, dtype=np.int32)
+    assert c.shape == (d,)
+    _check(lib().oracle_set_conserv(d, _iptr(c)), "oracle_set_conserv")
+
+
+def two_site_op_nc(gamma1, gamma2, lam0, lam1, lam2, op2, ll0, ll1, lr1, lr2, tot_num, max_filling,
+                   conserv=None):
+    """One number-conserving bond update; ``conserv`` (d local particle numbers)
+    selects the intDegFree form.  Returns
     ``(gamma1', gamma2', lam1', ll1', lr1', truncerr, ssflat)``."""
     chi, d, _ = gamma1.shape
+    _set_conserv(d, conserv)
     g1 = _fcomplex(gamma1, (chi, d, chi)).copy(order="F")
     g2 = _fcomplex(gamma2, (chi, d, chi)).copy(order="F")
     l0 = np.ascontiguousarray(lam0, dtype=np.float64)
@@ -215,23 +234,31 @@ def canonical_form_all(gammas, lambdas):
                                                                gammas[k], lambdas[k + 1])
 
 
-def trotter_step_pbc(gammas, lambdas, gates):
-    """TrotterStep2ndOrderPBC in place; gates[g-1] = Udt(g), g = 1..L (Udt(L): bond L-1)."""
+def trotter_step_pbc(gammas, lambdas, gates, order=2):
+    """TrotterStep2ndOrderPBC / TrotterStep5thOrderPBC in place; gates[g-1] = Udt(g)
+    in NEWConstructPropagators' periodic layout (L gates for order 2, Udt(L) the
+    edge bond; 3L for order 5 and odd L, 2L for even L)."""
     L = len(gammas)
     chi, d, _ = gammas[0].shape
+    need = L if order == 2 else (3 * L if L % 2 == 1 else 2 * L)
+    if order not in (2, 5) or len(gates) < need:
+        raise ValueError("periodic step: order 2 or 5 with %d gates" % need)
     gts = [np.asfortranarray(g, dtype=np.complex128) for g in gates]
     te = np.zeros(1)
-    st = lib().oracle_trotter_step_pbc(L, chi, d, _ptr_array(gammas, ctypes.c_double),
-                                       _ptr_array(lambdas, ctypes.c_double),
-                                       _ptr_array(gts, ctypes.c_double), _dptr(te))
+    fn = lib().oracle_trotter_step_pbc if order == 2 else lib().oracle_trotter_step_pbc5
+    st = fn(L, chi, d, _ptr_array(gammas, ctypes.c_double), _ptr_array(lambdas, ctypes.c_double),
+            _ptr_array(gts, ctypes.c_double), _dptr(te))
     _check(st, "oracle_trotter_step_pbc")
     return float(te[0])
 
 
-def trotter_step_nc(gammas, lambdas, label_left, label_right, gates, tot_num, max_filling, order=2):
-    """Number-conserving Trotter step; all lists updated in place."""
+def trotter_step_nc(gammas, lambdas, label_left, label_right, gates, tot_num, max_filling, order=2,
+                    conserv=None):
+    """Number-conserving Trotter step; all lists updated in place.  ``conserv``
+    selects the intDegFree form."""
     L = len(gammas)
     chi, d, _ = gammas[0].shape
+    _set_conserv(d, conserv)
     gts = [np.asfortranarray(g, dtype=np.complex128) for g in gates]
     te = np.zeros(1)
     st = lib().oracle_trotter_step_nc(L, chi, d, tot_num, max_filling, order,

@@ -360,8 +360,31 @@ done:
 }
 
 /* ------------------------------------------------------------------------- */
-/* Number-conserving update (U(1) labels, no internal degrees of freedom)     */
+/* Number-conserving update (U(1) labels)                                     */
 /* ------------------------------------------------------------------------- */
+
+/* Internal degrees of freedom.  The reference passes the OPTIONAL argument
+ * intDegFree to every NC routine and reads the particle number of local state i
+ * from the module global Conserv%vi(i) (set by the Hamiltonian builders, e.g.
+ * fermi_hubbard_module.f90:230-232).  Here oracle_set_conserv(d, conserv) plays
+ * both parts: a non-NULL table selects the intDegFree branches, NULL the plain
+ * ones (local number i-1). */
+static int g_idf = 0;
+static int g_cons[64];
+
+int oracle_set_conserv(int d, const int *conserv) {
+  if (!conserv) {
+    g_idf = 0;
+    return OR_OK;
+  }
+  if (d < 1 || d > 64) return OR_ERR_ARG;
+  for (int i = 0; i < d; ++i) g_cons[i] = conserv[i];
+  g_idf = 1;
+  return OR_OK;
+}
+
+/* particle number of local state i (0-based) */
+static int nloc(int i) { return g_idf ? g_cons[i] : i; }
 
 typedef struct {
   int nb;              /* number of blocks maxNL-minNL+1                       */
@@ -382,13 +405,37 @@ static void nc_free(nc_blocks *b) {
   free(b->r_j);
 }
 
-/* FormThetaNC (:820-851, intDegFree absent).  ll0=LabelLeft(link), ll1=LabelLeft(link+1),
+/* FormThetaNC (:748-851).  ll0=LabelLeft(link), ll1=LabelLeft(link+1),
  * lr1=LabelRight(link+1), lr2=LabelRight(link+2). */
-static void form_theta_nc(int chi, int d, zc *theta, const double *l0, const zc *g1,
+static void form_theta_nc(int chi, int d, int maxFilling, zc *theta, const double *l0, const zc *g1,
                           const double *l1, const zc *g2, const double *l2, const int *ll0,
                           const int *ll1, const int *lr1, const int *lr2) {
   const size_t sg = (size_t)chi * d;
   memset(theta, 0, sizeof(zc) * (size_t)chi * d * d * chi);
+  if (g_idf) {
+    /* FormThetaNC (:772-818), intDegFree present: sum over the local states
+     * whose numbers close the label differences */
+    for (int a = 0; a < chi; ++a)
+      for (int g = 0; g < chi; ++g)
+        for (int b = 0; b < chi; ++b)
+          for (int i = 0; i < d; ++i)
+            for (int j = 0; j < d; ++j) {
+              const int ni = g_cons[i], nj = g_cons[j];
+              const int lftN1 = ll0[a], lftN2 = ll1[b], rgtN1 = lr2[g], rgtN2 = lr1[b];
+              int mx = lftN1;
+              if (lftN2 > mx) mx = lftN2;
+              if (rgtN1 > mx) mx = rgtN1;
+              if (rgtN2 > mx) mx = rgtN2;
+              if (mx < 1000 && lftN2 - lftN1 <= maxFilling && lftN2 - lftN1 >= 0 &&
+                  rgtN2 - rgtN1 <= maxFilling && rgtN2 - rgtN1 >= 0 && lftN1 + ni == lftN2 &&
+                  rgtN1 + nj == rgtN2) {
+                zc *t = &theta[a + (size_t)chi * (i + (size_t)d * (j + (size_t)d * g))];
+                *t = *t + l0[a] * g1[a + (size_t)chi * i + sg * b] * l1[b] *
+                              g2[b + (size_t)chi * j + sg * g] * l2[g];
+              }
+            }
+    return;
+  }
   for (int a = 0; a < chi; ++a)
     for (int g = 0; g < chi; ++g)
       for (int b = 0; b < chi; ++b) {
@@ -407,13 +454,42 @@ static void form_theta_nc(int chi, int d, zc *theta, const double *l0, const zc 
       }
 }
 
-/* ThetaOperationNC_c / _r (:1013-1040 / :916-943, intDegFree absent) */
+/* ThetaOperationNC_c / _r (:950-1044 / :853-948) */
 static void theta_operation_nc(int chi, int d, int totNum, int maxFilling, zc *theta,
                                const zc *op_c, const double *op_r, const int *ll0,
                                const int *lr2) {
   const size_t nt = (size_t)chi * d * d * chi;
   const int d2 = d * d;
   zc *tmp = (zc *)calloc(nt, sizeof(zc));
+  if (g_idf) {
+    /* intDegFree present (:970-1010): every (k, j) with n_k + n_j = totNum - lftN - rgtN */
+    for (int a = 0; a < chi; ++a)
+      for (int k = 0; k < d; ++k)
+        for (int j = 0; j < d; ++j)
+          for (int g = 0; g < chi; ++g) {
+            const int nk = g_cons[k], nj = g_cons[j];
+            const int lftN = ll0[a], rgtN = lr2[g];
+            const int mx = lftN > rgtN ? lftN : rgtN;
+            const int rest = totNum - lftN - rgtN - nk;
+            if (mx < 1000 && rest >= 0 && rest <= maxFilling && nj == rest) {
+              zc acc = 0.0;
+              for (int i = 0; i < d; ++i)
+                for (int l = 0; l < d; ++l) {
+                  const int ni = g_cons[i], nl = g_cons[l];
+                  const int ri = totNum - lftN - rgtN - ni;
+                  if (ri >= 0 && ri <= maxFilling && nl == ri) {
+                    const size_t oi = (size_t)(k * d + j) + (size_t)d2 * (i * d + l);
+                    const zc op = op_c ? op_c[oi] : (zc)op_r[oi];
+                    acc = acc + op * theta[a + (size_t)chi * (i + (size_t)d * (l + (size_t)d * g))];
+                  }
+                }
+              tmp[a + (size_t)chi * (k + (size_t)d * (j + (size_t)d * g))] = acc;
+            }
+          }
+    memcpy(theta, tmp, sizeof(zc) * nt);
+    free(tmp);
+    return;
+  }
   for (int a = 0; a < chi; ++a)
     for (int k = 1; k <= d; ++k)
       for (int g = 0; g < chi; ++g) {
@@ -439,10 +515,33 @@ static void theta_operation_nc(int chi, int d, int totNum, int maxFilling, zc *t
   free(tmp);
 }
 
-/* RenormThetaNC (:1105-1128, intDegFree absent) */
+/* RenormThetaNC (:1046-1129) */
 static void renorm_theta_nc(int chi, int d, int totNum, int maxFilling, zc *theta, const int *ll0,
                             const int *lr2) {
   zc nsq = 0.0;
+  if (g_idf) {
+    /* intDegFree present (:1062-1102) */
+    for (int pass = 0; pass < 2; ++pass) {
+      const double norm = sqrt(creal(nsq));
+      for (int a = 0; a < chi; ++a)
+        for (int g = 0; g < chi; ++g) {
+          const int lftN = ll0[a], rgtN = lr2[g];
+          for (int i = 0; i < d; ++i)
+            for (int j = 0; j < d; ++j) {
+              const int ni = g_cons[i], nj = g_cons[j];
+              const int r = totNum - lftN - rgtN - ni;
+              if ((lftN > rgtN ? lftN : rgtN) < 1000 && r >= 0 && r <= maxFilling && nj == r) {
+                zc *t = &theta[a + (size_t)chi * (i + (size_t)d * (j + (size_t)d * g))];
+                if (pass == 0)
+                  nsq = nsq + conj(*t) * *t;
+                else
+                  *t = *t / norm;
+              }
+            }
+        }
+    }
+    return;
+  }
   for (int a = 0; a < chi; ++a)
     for (int g = 0; g < chi; ++g) {
       const int lftN = ll0[a], rgtN = lr2[g];
@@ -498,9 +597,10 @@ static void minmax_nlr(int chi, int totNum, int maxFilling, const int *ll0, cons
   *maxNR = mxr;
 }
 
-/* SizeOfBlocks (:1305-1335) + IndexLeft (:1379-1391) + IndexRight (:1431-1443),
- * intDegFree absent.  Returns OR_ERR_ARG if a block index falls outside
- * [1, nb] (the reference would write out of bounds there). */
+/* SizeOfBlocks (:1252-1336) + IndexLeft (:1339-1391) + IndexRight (:1393-1443);
+ * the local number is i-1, or Conserv(i) with intDegFree.  Returns OR_ERR_ARG if
+ * a block index falls outside [1, nb] (the reference would write out of bounds
+ * there). */
 static int build_blocks(int chi, int d, int totNum, int minNL, int maxNL, int minNR, int maxNR,
                         const int *ll0, const int *lr2, nc_blocks *B) {
   memset(B, 0, sizeof(*B));
@@ -521,13 +621,13 @@ static int build_blocks(int chi, int d, int totNum, int minNL, int maxNL, int mi
   for (int a = 0; a < chi; ++a)
     for (int i = 1; i <= d; ++i)
       if (ll0[a] < 1000) {
-        const int NL = ll0[a] + i - 1;
+        const int NL = ll0[a] + nloc(i - 1);
         if (minNL <= NL && NL <= maxNL) B->rows[NL - minNL]++;
       }
   for (int g = 0; g < chi; ++g)
     for (int j = 1; j <= d; ++j)
       if (lr2[g] < 1000) {
-        const int NR = lr2[g] + j - 1;
+        const int NR = lr2[g] + nloc(j - 1);
         if (minNR <= NR && NR <= maxNR) {
           const int k = totNum - NR - minNL;
           if (k < 0 || k >= nb) return OR_ERR_ARG;
@@ -542,8 +642,8 @@ static int build_blocks(int chi, int d, int totNum, int minNL, int maxNL, int mi
   if (!turn) return OR_ERR_ALLOC;
   for (int a = 0; a < chi; ++a)
     for (int i = 1; i <= d; ++i)
-      if (ll0[a] < 1000 && minNL <= ll0[a] + i - 1 && ll0[a] + i - 1 <= maxNL) {
-        const int k = ll0[a] + i - 1 - minNL;
+      if (ll0[a] < 1000 && minNL <= ll0[a] + nloc(i - 1) && ll0[a] + nloc(i - 1) <= maxNL) {
+        const int k = ll0[a] + nloc(i - 1) - minNL;
         const int p = B->roff[k] + turn[k]++;
         B->l_alpha[p] = a;
         B->l_i[p] = i - 1;
@@ -551,8 +651,8 @@ static int build_blocks(int chi, int d, int totNum, int minNL, int maxNL, int mi
   memset(turn, 0, sizeof(int) * nb);
   for (int g = 0; g < chi; ++g)
     for (int j = 1; j <= d; ++j)
-      if (lr2[g] < 1000 && minNR <= lr2[g] + j - 1 && lr2[g] + j - 1 <= maxNR) {
-        const int k = totNum - (lr2[g] + j - 1) - minNL;
+      if (lr2[g] < 1000 && minNR <= lr2[g] + nloc(j - 1) && lr2[g] + nloc(j - 1) <= maxNR) {
+        const int k = totNum - (lr2[g] + nloc(j - 1)) - minNL;
         const int p = B->coff[k] + turn[k]++;
         B->r_gamma[p] = g;
         B->r_j[p] = j - 1;
@@ -582,7 +682,7 @@ static void ordering(int sz, const double *arr, int *order /* 1-based values */)
   free(def);
 }
 
-/* TwoSiteOpNC_c (:1845-1964, intDegFree absent).  Labels are updated in place
+/* TwoSiteOpNC_c (:1845-1964; intDegFree as set by oracle_set_conserv).  Labels are updated in place
  * for link+1.  Optional s_out receives the flattened block singular values
  * (ssflat) and *sz_out their count. */
 int oracle_two_site_op_nc(int chi, int d, int totNum, int maxFilling, double *g1_, double *g2_,
@@ -595,7 +695,7 @@ int oracle_two_site_op_nc(int chi, int d, int totNum, int maxFilling, double *g1
   const size_t nt = (size_t)chi * d * d * chi;
   zc *theta = (zc *)malloc(sizeof(zc) * nt);
   if (!theta) return OR_ERR_ALLOC;
-  form_theta_nc(chi, d, theta, l0, g1, l1, g2, l2, ll0, ll1, lr1, lr2);
+  form_theta_nc(chi, d, maxFilling, theta, l0, g1, l1, g2, l2, ll0, ll1, lr1, lr2);
   theta_operation_nc(chi, d, totNum, maxFilling, theta, op_c, op_r, ll0, lr2);
   renorm_theta_nc(chi, d, totNum, maxFilling, theta, ll0, lr2);
   int minNL, maxNL, minNR, maxNR;
@@ -790,6 +890,69 @@ int oracle_trotter_step_pbc(int L, int chi, int d, double **gammas, double **lam
   for (int i = 1; i <= L - 1; i += 2) OP(i, i);
 #undef OP
 #undef SW
+  *total_truncerr = tot;
+  return OR_OK;
+}
+
+/* TrotterStep5thOrderPBC (propagation_module.f90:254-614): the Forest-Ruth
+ * sequence with the edge bond (L,1) applied on bond 1 between a swap of site L
+ * down to site 2 and the swap back.  Gate layout (NEWConstructPropagators,
+ * TEBDtools_module.f90:1149-1190): odd L -- odd bond i: Udt(3(i-1)+1..2), even
+ * bond i: Udt(2+3(i-2)+1..4), edge: Udt(3(L-1)+1..3); even L -- bond i:
+ * Udt(2(i-1)+1..2), edge Udt(2(L-1)+1..2).  gates[g-1] = Udt(g). */
+int oracle_trotter_step_pbc5(int L, int chi, int d, double **gammas, double **lambdas,
+                             const double *const *gates, double *total_truncerr) {
+  double tot = 0.0, te = 0.0;
+  int st;
+#define OP(link, g)                                                                              \
+  do {                                                                                           \
+    st = oracle_two_site_op(chi, d, gammas[(link)-1], gammas[(link)], lambdas[(link)-1],         \
+                            lambdas[(link)], lambdas[(link) + 1], gates[(g)-1], 0, &te, 0);      \
+    if (st != OR_OK) return st;                                                                  \
+    tot += te;                                                                                   \
+  } while (0)
+#define SW(link)                                                                                 \
+  do {                                                                                           \
+    st = oracle_swapping(chi, d, gammas[(link)-1], gammas[(link)], lambdas[(link)-1],            \
+                         lambdas[(link)], lambdas[(link) + 1], &te);                             \
+    if (st != OR_OK) return st;                                                                  \
+    tot += te;                                                                                   \
+  } while (0)
+#define EDGE(g)                                   \
+  do {                                            \
+    for (int i = L - 1; i >= 2; --i) SW(i);       \
+    OP(1, g);                                     \
+    for (int i = 2; i <= L - 1; ++i) SW(i);       \
+  } while (0)
+  if (L % 2 == 1) {
+#define ODD3(v) for (int i = 1; i <= L - 1; i += 2) OP(i, 3 * (i - 1) + (v))
+#define EVEN3(v) for (int i = 2; i <= L - 1; i += 2) OP(i, 2 + 3 * (i - 2) + (v))
+#define EDGE3(v) EDGE(3 * (L - 1) + (v))
+    ODD3(1);
+    EVEN3(1); EDGE3(1); EVEN3(2); EDGE3(2); EVEN3(2); EDGE3(1); EVEN3(1);
+    ODD3(2);
+    EVEN3(3); EDGE3(2); EVEN3(4); EDGE3(3); EVEN3(4); EDGE3(2); EVEN3(3);
+    ODD3(2);
+    EVEN3(1); EDGE3(1); EVEN3(2); EDGE3(2); EVEN3(2); EDGE3(1); EVEN3(1);
+    ODD3(1);
+#undef ODD3
+#undef EVEN3
+#undef EDGE3
+  } else {
+#define ODD2(v) for (int i = 1; i <= L - 1; i += 2) OP(i, 2 * (i - 1) + (v))
+#define EVEN2(v) for (int i = 2; i <= L - 1; i += 2) OP(i, 2 * (i - 1) + (v))
+#define EDGE2(v) EDGE(2 * (L - 1) + (v))
+    ODD2(1); EDGE2(1); EVEN2(1);
+    ODD2(2); EDGE2(2); EVEN2(2);
+    ODD2(2); EDGE2(1); EVEN2(1);
+    ODD2(1);
+#undef ODD2
+#undef EVEN2
+#undef EDGE2
+  }
+#undef OP
+#undef SW
+#undef EDGE
   *total_truncerr = tot;
   return OR_OK;
 }

@@ -84,6 +84,33 @@ def test_trotter_step_pbc_matches_oracle(pkg, oracle, L):
     assert abs(abs(obs.inner_product(gam, lam, g_gpu, l_gpu)) - 1.0) < 1e-10
 
 
+@pytest.mark.parametrize("L,chi", [(6, 8), (7, 8), (7, 4)])
+def test_trotter_step_pbc_forest_ruth_matches_oracle(pkg, oracle, L, chi):
+    """TrotterStep5thOrderPBC in both gate layouts (even L: 2L gates, odd L: 3L),
+    exact (chi = 8) and truncated (chi = 4)."""
+    H = pkg.hamiltonians
+    d, dt = 2, 0.05
+    rng = np.random.default_rng(100 + L)
+    c0 = rng.standard_normal((d, L)) + 1j * rng.standard_normal((d, L))
+    c0 /= np.linalg.norm(c0, axis=0)
+    gam, lam = H.product_state(c0, chi)
+    hb = H.heisenberg(L, 1.0, 1.0, 0.5)[0]
+    U = H.construct_propagators([hb] * L, dt, 5, boundary="P")
+    with pkg.Chain(L, d, chi) as c:
+        c.set_state(gam, lam)
+        te = [c.trotter_step_pbc(U, 5) for _ in range(2)]
+        g_gpu, l_gpu = c.get_state()
+        with pytest.raises(pkg.TebdError):
+            c.trotter_step_pbc(U[: len(U) - 1], 5)
+    rte = [oracle.trotter_step_pbc(gam, lam, U, 5) for _ in range(2)]
+    assert np.allclose(te, rte, atol=1e-10)
+    for a, b in zip(l_gpu, lam):
+        assert np.allclose(a, b, atol=1e-10)
+    sz = np.diag([0.5, -0.5])
+    assert np.allclose(obs.one_site_expval(g_gpu, l_gpu, sz), obs.one_site_expval(gam, lam, sz), atol=1e-10)
+    assert abs(abs(obs.inner_product(gam, lam, g_gpu, l_gpu)) - 1.0) < 1e-10
+
+
 def test_canonical_form_all_nc_matches_oracle(pkg, oracle):
     H = pkg.hamiltonians
     L, d, chi, N = 8, 3, 12, 8

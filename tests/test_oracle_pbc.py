@@ -91,3 +91,48 @@ def test_canonical_form_all_makes_a_random_chain_canonical(oracle):
         keep = lam[s + 1] > 1e-6
         Mx = A.conj().T @ A
         assert np.allclose(Mx[np.ix_(keep, keep)], np.eye(keep.sum()), atol=1e-8)
+
+
+def _ring_hamiltonian(L, hb, d):
+    """Dense H of a ring: hb on bonds (s, s+1) and on the edge (site 1 left, site L right)."""
+    N = d ** L
+    Hf = np.zeros((N, N), complex)
+    for b in range(L - 1):
+        Hf += np.kron(np.kron(np.eye(d ** b), hb), np.eye(d ** (L - b - 2)))
+    h4 = hb.reshape(d, d, d, d)
+    shape = (d,) * L
+    for idx in range(N):
+        digs = np.unravel_index(idx, shape)
+        for i1 in range(d):
+            for iL in range(d):
+                v = h4[i1, iL, digs[0], digs[-1]]
+                if v != 0:
+                    Hf[np.ravel_multi_index((i1,) + digs[1:-1] + (iL,), shape), idx] += v
+    return Hf
+
+
+@pytest.mark.parametrize("L", [5, 6])
+@pytest.mark.parametrize("order,dt,bound", [(2, 0.1, 2e-7), (5, 0.1, 2e-11), (5, 0.05, 1e-13)])
+def test_pbc_steps_follow_the_exact_ring_evolution(oracle, H, L, order, dt, bound):
+    """TrotterStep2ndOrderPBC / 5thOrderPBC with NEWConstructPropagators' periodic
+    gates against exp(-iHt) of the ring (exact chi, no truncation): the infidelity
+    after t = 0.4 falls like dt^4 (order 2) and dt^8 (Forest-Ruth), which a wrong
+    gate index, fraction or sweep would break by orders of magnitude."""
+    from oracle import observables as obs
+    d, chi = 2, 2 ** (L // 2)
+    hb = H.heisenberg(L, 1.0, 1.0, 0.7)[0]
+    rng = np.random.default_rng(L)
+    c0 = rng.standard_normal((d, L)) + 1j * rng.standard_normal((d, L))
+    c0 /= np.linalg.norm(c0, axis=0)
+    psi0 = c0[:, 0]
+    for s in range(1, L):
+        psi0 = np.kron(psi0, c0[:, s])
+    steps = int(round(0.4 / dt))
+    gam, lam = H.product_state(c0, chi)
+    U = H.construct_propagators([hb] * L, dt, order, boundary="P")
+    assert len(U) == (L if order == 2 else (3 * L if L % 2 else 2 * L))
+    te = sum(oracle.trotter_step_pbc(gam, lam, U, order) for _ in range(steps))
+    assert te < 1e-11
+    w, v = np.linalg.eigh(_ring_hamiltonian(L, hb, d))
+    exact = v @ (np.exp(-1j * w * dt * steps) * (v.conj().T @ psi0))
+    assert 1.0 - abs(np.vdot(exact, obs.state_vector(gam, lam))) < bound
