@@ -130,11 +130,15 @@ int tebd_trotter_step(tebd_handle *h, int order, int n_gates, const double *cons
 
 /* Swapping(link, truncerr, Gammas, Lambdas) (local_operations_module.f90:651-689):
  * exchange the physical indices of sites link and link+1 (SwapTheta), SVD of the
- * unnormalised Theta, FormLambda1/FormGamma1/FormGamma2.  Dense mode. */
+ * unnormalised Theta, FormLambda1/FormGamma1/FormGamma2.  In NC mode
+ * SwappingNC(link, Gammas, Lambdas, LabelLeft, LabelRight, truncerr[, intDegFree])
+ * (:1966-2095): SwapThetaNC and the block decomposition without RenormThetaNC. */
 int tebd_swapping(tebd_handle *h, int link, double *truncerr);
 
-/* Periodic-boundary Trotter step, dense mode; replaces TrotterStep with
- * BoundaryCond='P' (propagation_module.f90:42-79).  The edge bond (L,1) is
+/* Periodic-boundary Trotter step; replaces TrotterStep with BoundaryCond='P'
+ * (propagation_module.f90:42-79) in dense mode and TrotterStep2ndOrderPBCNC /
+ * TrotterStep5thOrderPBCNC (:1019-1940, same sequences with TwoSiteOpNC and
+ * SwappingNC) in NC mode.  The edge bond (L,1) is
  * applied on bond 1 after Swapping site L down to site 2, and swapped back.
  * gates[g-1] = Udt(g) in NEWConstructPropagators' periodic layout
  * (TEBDtools_module.f90:1100-1190):
@@ -164,7 +168,8 @@ int tebd_canonical_form_all_nc(tebd_handle *h);
  * propagation_module.f90:890-1018, 1943-1983) and then takes the particle number
  * of local state i from the module global Conserv%vi(i) instead of i-1
  * (set by the Hamiltonian builders, e.g. fermi_hubbard_module.f90:230-232).
- * conserv: d numbers >= 0 (Conserv%vi), or NULL for the form without intDegFree.
+ * conserv: d numbers in [0, max_filling] (Conserv%vi), or NULL for the form
+ * without intDegFree (which needs max_filling = d-1).
  * NC mode, d <= 8; at most 16 local pairs (i, j) may share one pair total
  * n_i + n_j (TEBD_ERR_ARG otherwise). */
 int tebd_set_conserv(tebd_handle *h, const int *conserv);

@@ -618,9 +618,12 @@ static std::vector<double> swap_gate(int d) {
 // physical indices of the unnormalised Theta, which equals applying SWAP as the
 // gate; the SVD then runs without ReshapeTheta's 1/||Theta||, as Swapping calls
 // SVDTruncation directly (truncerr = |1 - sum of kept S^2| of the raw Theta).
+// NC mode: SwappingNC (:1966-2095) -- SwapThetaNC moves the allowed entries
+// (i, j) to (j, i), which is SWAP through ThetaOperationNC when every local
+// number lies in [0, maxFilling] (enforced for both NC forms), and RenormThetaNC
+// is skipped the same way.
 extern "C" int tebd_swapping(tebd_handle *h, int link, double *truncerr) {
   if (!h || !truncerr) return TEBD_ERR_ARG;
-  if (h->mode != TEBD_MODE_DENSE) return set_error(h, TEBD_ERR_STATE, "Swapping needs a TEBD_MODE_DENSE handle");
   const std::vector<double> g = swap_gate(h->d);
   const double *gp = g.data();
   h->unnormalized = 1;
@@ -630,7 +633,9 @@ extern "C" int tebd_swapping(tebd_handle *h, int link, double *truncerr) {
 }
 
 // TrotterStep2ndOrderPBC (propagation_module.f90:116-198) and
-// TrotterStep5thOrderPBC (:254-614).  gates[g-1] = Udt(g) in the periodic layout
+// TrotterStep5thOrderPBC (:254-614); in NC mode TrotterStep2ndOrderPBCNC
+// (:1019-1186) and TrotterStep5thOrderPBCNC (:1244-1940), the same sequences with
+// TwoSiteOpNC and SwappingNC.  gates[g-1] = Udt(g) in the periodic layout
 // of NEWConstructPropagators.  The edge gate acts on bond 1 between a swap of
 // site L down to position 2 and the swap back; same-parity bulk bonds are
 // batched; truncation errors of every update and swap are summed in the
@@ -638,7 +643,6 @@ extern "C" int tebd_swapping(tebd_handle *h, int link, double *truncerr) {
 extern "C" int tebd_trotter_step_pbc(tebd_handle *h, int order, int n_gates, const double *const *gates,
                                      double *total_truncerr) {
   if (!h || !gates || !total_truncerr) return TEBD_ERR_ARG;
-  if (h->mode != TEBD_MODE_DENSE) return set_error(h, TEBD_ERR_STATE, "the PBC Trotter step needs a dense handle");
   if (order != 2 && order != 5) return set_error(h, TEBD_ERR_ARG, "periodic boundaries: order must be 2 or 5");
   const int L = h->L;
   if (L < 3) return set_error(h, TEBD_ERR_ARG, "periodic boundaries need L >= 3");

@@ -371,15 +371,17 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
 }
 
 // V = identity for every block problem; norm from the fixed-order partials
+// unnormalized = 1 for SwappingNC, which skips RenormThetaNC: the block singular
+// values are taken as they are (norm 1 in the flattening).
 __global__ void k_nc_prepare_svd(NcSlot *nc, JacobiProblem<double> *probs, double *nrm, int bmax,
-                                 int *status) {
+                                 int *status, int unnormalized) {
   const int s = blockIdx.y;
   const NcSlot S = nc[s];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     double acc = 0.0;
     for (int j = 0; j < kNormParts; ++j) acc += S.part[j];
     const double v = sqrt(acc);
-    nrm[s] = v;
+    nrm[s] = unnormalized ? 1.0 : v;
     if (!isfinite(v) || v == 0.0) atomicOr(&status[0], 1);
     if (S.hdr[H_ERR]) atomicOr(&status[1], 1);
   }
@@ -650,10 +652,12 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
   const int chi = h->chi, d = h->d, bmax = w->bmax;
   const int N = h->opts.tot_num, mf = h->opts.max_filling;
   if (d > kMaxDnc) return set_error(h, TEBD_ERR_ARG, "NC mode supports d <= 8");
-  // Without intDegFree the second physical index is a particle number (up to
-  // maxFilling), so it must stay below d.
-  if (!h->nc_idf && mf > d - 1)
-    return set_error(h, TEBD_ERR_ARG, "NC mode without internal degrees of freedom needs max_filling <= d-1");
+  // Without intDegFree the physical index is the particle number: local states
+  // 0..d-1 and at most maxFilling particles must be the same range (the reference
+  // indexes past Gamma for maxFilling > d-1, and for maxFilling < d-1 its
+  // SwapThetaNC keeps entries that ThetaOperationNC would drop).
+  if (!h->nc_idf && mf != d - 1)
+    return set_error(h, TEBD_ERR_ARG, "NC mode without internal degrees of freedom needs max_filling = d-1");
   NcLocal nl;
   for (int i = 0; i < 8; ++i) nl.n[i] = (h->nc_idf && i < d) ? h->nc_conserv[i] : i;
   cudaStream_t st = h->stream;
@@ -667,7 +671,8 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
     k_nc_theta<false><<<dim3(kNormParts, nb), 256, 0, st>>>(h->gam, h->lam, h->lab_l, h->lab_r, h->links_d,
                                                             h->slots_d, w->slots_d, chi, d, N, mf, nl);
   TEBD_LAUNCHED(h);
-  k_nc_prepare_svd<<<dim3(32, nb), 256, 0, st>>>(w->slots_d, w->probs_d, h->nrm, bmax, h->status_d);
+  k_nc_prepare_svd<<<dim3(32, nb), 256, 0, st>>>(w->slots_d, w->probs_d, h->nrm, bmax, h->status_d,
+                                                 h->unnormalized);
   TEBD_LAUNCHED(h);
   // sizes for the launch configuration
   std::vector<int> hdr((size_t)nb * H_COUNT);
@@ -713,9 +718,12 @@ extern "C" int tebd_set_conserv(tebd_handle *h, const int *conserv) {
   }
   const int d = h->d;
   if (d > kMaxDnc) return set_error(h, TEBD_ERR_ARG, "intDegFree: d <= 8");
+  // Local numbers above maxFilling are dropped by FormThetaNC but can be filled by
+  // ThetaOperationNC, a state the reference never builds; they are refused.
   int mx = 0;
   for (int i = 0; i < d; ++i) {
-    if (conserv[i] < 0 || conserv[i] >= 1000) return set_error(h, TEBD_ERR_ARG, "intDegFree: Conserv values in [0, 1000)");
+    if (conserv[i] < 0 || conserv[i] > h->opts.max_filling)
+      return set_error(h, TEBD_ERR_ARG, "intDegFree: Conserv values must lie in [0, max_filling]");
     mx = std::max(mx, conserv[i]);
   }
   // pairs (i, j) per pair total, as the Theta kernel lists them

@@ -80,6 +80,10 @@ def lib():
     L.oracle_trotter_step_pbc.argtypes = [ctypes.c_int] * 3 + [ctypes.POINTER(dp)] * 3 + [dp]
     L.oracle_trotter_step_pbc5.argtypes = [ctypes.c_int] * 3 + [ctypes.POINTER(dp)] * 3 + [dp]
     L.oracle_set_conserv.argtypes = [ctypes.c_int, ip]
+    L.oracle_swapping_nc.argtypes = [ctypes.c_int] * 4 + [dp] * 5 + [ip] * 4 + [dp]
+    L.oracle_trotter_step_pbc_nc.argtypes = (
+        [ctypes.c_int] * 6 + [ctypes.POINTER(dp)] * 2 + [ctypes.POINTER(ip)] * 2 + [ctypes.POINTER(dp), dp]
+    )
     L.oracle_trotter_step_nc.argtypes = (
         [ctypes.c_int] * 6 + [ctypes.POINTER(dp)] * 2 + [ctypes.POINTER(ip)] * 2 + [ctypes.POINTER(dp), dp]
     )
@@ -249,6 +253,48 @@ def trotter_step_pbc(gammas, lambdas, gates, order=2):
     st = fn(L, chi, d, _ptr_array(gammas, ctypes.c_double), _ptr_array(lambdas, ctypes.c_double),
             _ptr_array(gts, ctypes.c_double), _dptr(te))
     _check(st, "oracle_trotter_step_pbc")
+    return float(te[0])
+
+
+def swapping_nc(gamma1, gamma2, lam0, lam1, lam2, ll0, ll1, lr1, lr2, tot_num, max_filling, conserv=None):
+    """SwappingNC on one bond.  Returns ``(gamma1', gamma2', lam1', ll1', lr1', truncerr)``."""
+    chi, d, _ = gamma1.shape
+    _set_conserv(d, conserv)
+    g1 = _fcomplex(gamma1, (chi, d, chi)).copy(order="F")
+    g2 = _fcomplex(gamma2, (chi, d, chi)).copy(order="F")
+    l0 = np.ascontiguousarray(lam0, dtype=np.float64)
+    l1 = np.array(lam1, dtype=np.float64)
+    l2 = np.ascontiguousarray(lam2, dtype=np.float64)
+    a_ll0 = np.ascontiguousarray(ll0, dtype=np.int32)
+    a_ll1 = np.array(ll1, dtype=np.int32)
+    a_lr1 = np.array(lr1, dtype=np.int32)
+    a_lr2 = np.ascontiguousarray(lr2, dtype=np.int32)
+    te = np.zeros(1)
+    st = lib().oracle_swapping_nc(chi, d, tot_num, max_filling, _dptr(g1), _dptr(g2), _dptr(l0), _dptr(l1),
+                                  _dptr(l2), _iptr(a_ll0), _iptr(a_ll1), _iptr(a_lr1), _iptr(a_lr2), _dptr(te))
+    _check(st, "oracle_swapping_nc")
+    return g1, g2, l1, a_ll1, a_lr1, float(te[0])
+
+
+def trotter_step_pbc_nc(gammas, lambdas, label_left, label_right, gates, tot_num, max_filling, order=2,
+                        conserv=None):
+    """TrotterStep2ndOrderPBCNC / 5thOrderPBCNC in place (gate layout as
+    :func:`trotter_step_pbc`)."""
+    L = len(gammas)
+    chi, d, _ = gammas[0].shape
+    need = L if order == 2 else (3 * L if L % 2 == 1 else 2 * L)
+    if order not in (2, 5) or len(gates) < need:
+        raise ValueError("periodic step: order 2 or 5 with %d gates" % need)
+    _set_conserv(d, conserv)
+    gts = [np.asfortranarray(g, dtype=np.complex128) for g in gates]
+    te = np.zeros(1)
+    st = lib().oracle_trotter_step_pbc_nc(L, chi, d, tot_num, max_filling, order,
+                                          _ptr_array(gammas, ctypes.c_double),
+                                          _ptr_array(lambdas, ctypes.c_double),
+                                          _ptr_array(label_left, ctypes.c_int),
+                                          _ptr_array(label_right, ctypes.c_int),
+                                          _ptr_array(gts, ctypes.c_double), _dptr(te))
+    _check(st, "oracle_trotter_step_pbc_nc")
     return float(te[0])
 
 

@@ -682,6 +682,46 @@ static void ordering(int sz, const double *arr, int *order /* 1-based values */)
   free(def);
 }
 
+/* SwapThetaNC (:1144-1250): exchange the two physical indices on the allowed
+ * entries (i, j) of each (alpha, gamma).  Without intDegFree the swapped array
+ * starts from zero; with it the reference leaves the other entries unset, and
+ * none of them is read afterwards when Conserv lies in [0, maxFilling]. */
+static void swap_theta_nc(int chi, int d, int totNum, int maxFilling, zc *theta, const int *ll0,
+                          const int *lr2) {
+  const size_t nt = (size_t)chi * d * d * chi;
+  zc *sw = (zc *)calloc(nt, sizeof(zc));
+  for (int a = 0; a < chi; ++a)
+    for (int g = 0; g < chi; ++g) {
+      const int lftN = ll0[a], rgtN = lr2[g];
+      if ((lftN > rgtN ? lftN : rgtN) >= 1000) continue;
+      if (g_idf) {
+        for (int i = 0; i < d; ++i)
+          for (int j = 0; j < d; ++j) {
+            const int r = totNum - lftN - rgtN - g_cons[i];
+            if (r >= 0 && r <= maxFilling && g_cons[j] == r)
+              sw[a + (size_t)chi * (j + (size_t)d * (i + (size_t)d * g))] =
+                  theta[a + (size_t)chi * (i + (size_t)d * (j + (size_t)d * g))];
+          }
+      } else {
+        for (int i = 1; i <= d; ++i) {
+          const int r = totNum - lftN - rgtN - i + 1;
+          if (r >= 0 && r <= maxFilling) {
+            const int j = totNum - lftN - rgtN - i + 2; /* 1-based */
+            sw[a + (size_t)chi * ((j - 1) + (size_t)d * ((i - 1) + (size_t)d * g))] =
+                theta[a + (size_t)chi * ((i - 1) + (size_t)d * ((j - 1) + (size_t)d * g))];
+          }
+        }
+      }
+    }
+  memcpy(theta, sw, sizeof(zc) * nt);
+  free(sw);
+}
+
+static int nc_core(int chi, int d, int totNum, int maxFilling, double *g1_, double *g2_,
+                   const double *l0, double *l1, const double *l2, const double *op_c_,
+                   const double *op_r, const int *ll0, int *ll1, int *lr1, const int *lr2,
+                   double *truncerr, double *s_out, int *sz_out, int swap);
+
 /* TwoSiteOpNC_c (:1845-1964; intDegFree as set by oracle_set_conserv).  Labels are updated in place
  * for link+1.  Optional s_out receives the flattened block singular values
  * (ssflat) and *sz_out their count. */
@@ -689,15 +729,37 @@ int oracle_two_site_op_nc(int chi, int d, int totNum, int maxFilling, double *g1
                           const double *l0, double *l1, const double *l2, const double *op_c_,
                           const double *op_r, const int *ll0, int *ll1, int *lr1, const int *lr2,
                           double *truncerr, double *s_out, int *sz_out) {
-  if (chi < 1 || d < 1 || (!op_c_ && !op_r)) return OR_ERR_ARG;
+  if (!op_c_ && !op_r) return OR_ERR_ARG;
+  return nc_core(chi, d, totNum, maxFilling, g1_, g2_, l0, l1, l2, op_c_, op_r, ll0, ll1, lr1, lr2,
+                 truncerr, s_out, sz_out, 0);
+}
+
+/* SwappingNC (:1966-2095): FormThetaNC, SwapThetaNC, then the block SVD and the
+ * label / Lambda / Gamma updates of TwoSiteOpNC, without RenormThetaNC. */
+int oracle_swapping_nc(int chi, int d, int totNum, int maxFilling, double *g1_, double *g2_,
+                       const double *l0, double *l1, const double *l2, const int *ll0, int *ll1,
+                       int *lr1, const int *lr2, double *truncerr) {
+  return nc_core(chi, d, totNum, maxFilling, g1_, g2_, l0, l1, l2, 0, 0, ll0, ll1, lr1, lr2, truncerr,
+                 0, 0, 1);
+}
+
+static int nc_core(int chi, int d, int totNum, int maxFilling, double *g1_, double *g2_,
+                   const double *l0, double *l1, const double *l2, const double *op_c_,
+                   const double *op_r, const int *ll0, int *ll1, int *lr1, const int *lr2,
+                   double *truncerr, double *s_out, int *sz_out, int swap) {
+  if (chi < 1 || d < 1) return OR_ERR_ARG;
   zc *g1 = (zc *)g1_, *g2 = (zc *)g2_;
   const zc *op_c = (const zc *)op_c_;
   const size_t nt = (size_t)chi * d * d * chi;
   zc *theta = (zc *)malloc(sizeof(zc) * nt);
   if (!theta) return OR_ERR_ALLOC;
   form_theta_nc(chi, d, maxFilling, theta, l0, g1, l1, g2, l2, ll0, ll1, lr1, lr2);
-  theta_operation_nc(chi, d, totNum, maxFilling, theta, op_c, op_r, ll0, lr2);
-  renorm_theta_nc(chi, d, totNum, maxFilling, theta, ll0, lr2);
+  if (swap) {
+    swap_theta_nc(chi, d, totNum, maxFilling, theta, ll0, lr2);
+  } else {
+    theta_operation_nc(chi, d, totNum, maxFilling, theta, op_c, op_r, ll0, lr2);
+    renorm_theta_nc(chi, d, totNum, maxFilling, theta, ll0, lr2);
+  }
   int minNL, maxNL, minNR, maxNR;
   minmax_nlr(chi, totNum, maxFilling, ll0, lr2, &minNL, &maxNL, &minNR, &maxNR);
   nc_blocks B;
@@ -859,64 +921,57 @@ int oracle_trotter_step_nc(int L, int chi, int d, int totNum, int maxFilling, in
   return OR_OK;
 }
 
-/* TrotterStep2ndOrderPBC (propagation_module.f90:116-198): gates[g-1] = Udt(g),
- * g = 1..L, Udt(L) the edge bond (L,1) applied on bond 1 after swapping site L
- * down to site 2. */
-int oracle_trotter_step_pbc(int L, int chi, int d, double **gammas, double **lambdas,
-                            const double *const *gates, double *total_truncerr) {
-  double tot = 0.0, te = 0.0;
+/* Periodic-boundary steps.  One context carries the chain for the dense
+ * routines (TwoSiteOp, Swapping) or the number-conserving ones (TwoSiteOpNC,
+ * SwappingNC with the labels); the sequences are the reference's, which are the
+ * same for both (propagation_module.f90:116-614 and 1019-1940).  The edge bond
+ * (L,1) is applied on bond 1 after swapping site L down to site 2: the edge calls
+ * in the NC drivers pass the loop variable after `DO i=systemSize-1,2,(-1)`,
+ * which is 1 there. */
+typedef struct {
+  int nc, chi, d, totNum, maxFilling;
+  double **gammas, **lambdas;
+  int **ll, **lr;
+  const double *const *gates;
+  double tot;
+} pbc_ctx;
+
+static int pbc_op(pbc_ctx *C, int link, int g) {
+  double te = 0.0;
   int st;
-#define OP(link, g)                                                                              \
-  do {                                                                                           \
-    st = oracle_two_site_op(chi, d, gammas[(link)-1], gammas[(link)], lambdas[(link)-1],         \
-                            lambdas[(link)], lambdas[(link) + 1], gates[(g)-1], 0, &te, 0);      \
-    if (st != OR_OK) return st;                                                                  \
-    tot += te;                                                                                   \
-  } while (0)
-#define SW(link)                                                                                 \
-  do {                                                                                           \
-    st = oracle_swapping(chi, d, gammas[(link)-1], gammas[(link)], lambdas[(link)-1],            \
-                         lambdas[(link)], lambdas[(link) + 1], &te);                             \
-    if (st != OR_OK) return st;                                                                  \
-    tot += te;                                                                                   \
-  } while (0)
-  for (int i = 1; i <= L - 1; i += 2) OP(i, i);
-  if (L % 2 == 1)
-    for (int i = 2; i <= L - 1; i += 2) OP(i, i);
-  for (int i = L - 1; i >= 2; --i) SW(i);
-  OP(1, L);
-  for (int i = 2; i <= L - 1; ++i) SW(i);
-  for (int i = 2; i <= L - 1; i += 2) OP(i, i);
-  for (int i = 1; i <= L - 1; i += 2) OP(i, i);
-#undef OP
-#undef SW
-  *total_truncerr = tot;
-  return OR_OK;
+  if (C->nc)
+    st = oracle_two_site_op_nc(C->chi, C->d, C->totNum, C->maxFilling, C->gammas[link - 1],
+                               C->gammas[link], C->lambdas[link - 1], C->lambdas[link],
+                               C->lambdas[link + 1], C->gates[g - 1], 0, C->ll[link - 1], C->ll[link],
+                               C->lr[link], C->lr[link + 1], &te, 0, 0);
+  else
+    st = oracle_two_site_op(C->chi, C->d, C->gammas[link - 1], C->gammas[link], C->lambdas[link - 1],
+                            C->lambdas[link], C->lambdas[link + 1], C->gates[g - 1], 0, &te, 0);
+  C->tot += te;
+  return st;
 }
 
-/* TrotterStep5thOrderPBC (propagation_module.f90:254-614): the Forest-Ruth
- * sequence with the edge bond (L,1) applied on bond 1 between a swap of site L
- * down to site 2 and the swap back.  Gate layout (NEWConstructPropagators,
- * TEBDtools_module.f90:1149-1190): odd L -- odd bond i: Udt(3(i-1)+1..2), even
- * bond i: Udt(2+3(i-2)+1..4), edge: Udt(3(L-1)+1..3); even L -- bond i:
- * Udt(2(i-1)+1..2), edge Udt(2(L-1)+1..2).  gates[g-1] = Udt(g). */
-int oracle_trotter_step_pbc5(int L, int chi, int d, double **gammas, double **lambdas,
-                             const double *const *gates, double *total_truncerr) {
-  double tot = 0.0, te = 0.0;
+static int pbc_sw(pbc_ctx *C, int link) {
+  double te = 0.0;
   int st;
-#define OP(link, g)                                                                              \
-  do {                                                                                           \
-    st = oracle_two_site_op(chi, d, gammas[(link)-1], gammas[(link)], lambdas[(link)-1],         \
-                            lambdas[(link)], lambdas[(link) + 1], gates[(g)-1], 0, &te, 0);      \
-    if (st != OR_OK) return st;                                                                  \
-    tot += te;                                                                                   \
+  if (C->nc)
+    st = oracle_swapping_nc(C->chi, C->d, C->totNum, C->maxFilling, C->gammas[link - 1], C->gammas[link],
+                            C->lambdas[link - 1], C->lambdas[link], C->lambdas[link + 1],
+                            C->ll[link - 1], C->ll[link], C->lr[link], C->lr[link + 1], &te);
+  else
+    st = oracle_swapping(C->chi, C->d, C->gammas[link - 1], C->gammas[link], C->lambdas[link - 1],
+                         C->lambdas[link], C->lambdas[link + 1], &te);
+  C->tot += te;
+  return st;
+}
+
+#define OP(link, g)                                 \
+  do {                                              \
+    if ((st = pbc_op(C, (link), (g))) != OR_OK) return st; \
   } while (0)
-#define SW(link)                                                                                 \
-  do {                                                                                           \
-    st = oracle_swapping(chi, d, gammas[(link)-1], gammas[(link)], lambdas[(link)-1],            \
-                         lambdas[(link)], lambdas[(link) + 1], &te);                             \
-    if (st != OR_OK) return st;                                                                  \
-    tot += te;                                                                                   \
+#define SW(link)                                    \
+  do {                                              \
+    if ((st = pbc_sw(C, (link))) != OR_OK) return st; \
   } while (0)
 #define EDGE(g)                                   \
   do {                                            \
@@ -924,6 +979,27 @@ int oracle_trotter_step_pbc5(int L, int chi, int d, double **gammas, double **la
     OP(1, g);                                     \
     for (int i = 2; i <= L - 1; ++i) SW(i);       \
   } while (0)
+
+/* TrotterStep2ndOrderPBC (:116-198) / TrotterStep2ndOrderPBCNC (:1019-1186):
+ * gates[g-1] = Udt(g), g = 1..L, Udt(L) the edge. */
+static int pbc2_run(pbc_ctx *C, int L) {
+  int st;
+  for (int i = 1; i <= L - 1; i += 2) OP(i, i);
+  if (L % 2 == 1)
+    for (int i = 2; i <= L - 1; i += 2) OP(i, i);
+  EDGE(L);
+  for (int i = 2; i <= L - 1; i += 2) OP(i, i);
+  for (int i = 1; i <= L - 1; i += 2) OP(i, i);
+  return OR_OK;
+}
+
+/* TrotterStep5thOrderPBC (:254-614) / TrotterStep5thOrderPBCNC (:1244-1940): the
+ * Forest-Ruth sequence.  Gate layout (NEWConstructPropagators,
+ * TEBDtools_module.f90:1149-1190): odd L -- odd bond i: Udt(3(i-1)+1..2), even
+ * bond i: Udt(2+3(i-2)+1..4), edge: Udt(3(L-1)+1..3); even L -- bond i:
+ * Udt(2(i-1)+1..2), edge Udt(2(L-1)+1..2).  gates[g-1] = Udt(g). */
+static int pbc5_run(pbc_ctx *C, int L) {
+  int st;
   if (L % 2 == 1) {
 #define ODD3(v) for (int i = 1; i <= L - 1; i += 2) OP(i, 3 * (i - 1) + (v))
 #define EVEN3(v) for (int i = 2; i <= L - 1; i += 2) OP(i, 2 + 3 * (i - 2) + (v))
@@ -950,9 +1026,35 @@ int oracle_trotter_step_pbc5(int L, int chi, int d, double **gammas, double **la
 #undef EVEN2
 #undef EDGE2
   }
+  return OR_OK;
+}
 #undef OP
 #undef SW
 #undef EDGE
-  *total_truncerr = tot;
-  return OR_OK;
+
+int oracle_trotter_step_pbc(int L, int chi, int d, double **gammas, double **lambdas,
+                            const double *const *gates, double *total_truncerr) {
+  pbc_ctx C = {0, chi, d, 0, 0, gammas, lambdas, 0, 0, gates, 0.0};
+  const int st = pbc2_run(&C, L);
+  *total_truncerr = C.tot;
+  return st;
+}
+
+int oracle_trotter_step_pbc5(int L, int chi, int d, double **gammas, double **lambdas,
+                             const double *const *gates, double *total_truncerr) {
+  pbc_ctx C = {0, chi, d, 0, 0, gammas, lambdas, 0, 0, gates, 0.0};
+  const int st = pbc5_run(&C, L);
+  *total_truncerr = C.tot;
+  return st;
+}
+
+/* Number-conserving periodic steps (intDegFree as set by oracle_set_conserv). */
+int oracle_trotter_step_pbc_nc(int L, int chi, int d, int totNum, int maxFilling, int order,
+                               double **gammas, double **lambdas, int **label_left, int **label_right,
+                               const double *const *gates, double *total_truncerr) {
+  if (order != 2 && order != 5) return OR_ERR_ARG;
+  pbc_ctx C = {1, chi, d, totNum, maxFilling, gammas, lambdas, label_left, label_right, gates, 0.0};
+  const int st = order == 2 ? pbc2_run(&C, L) : pbc5_run(&C, L);
+  *total_truncerr = C.tot;
+  return st;
 }

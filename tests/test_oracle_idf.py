@@ -1,6 +1,6 @@
-"""Known answers for the oracle's number-conserving update with internal degrees
-of freedom (the intDegFree branches of FormThetaNC, ThetaOperationNC,
-RenormThetaNC, SizeOfBlocks and IndexLeft/Right)."""
+"""Known answers for the oracle's number-conserving routines: the intDegFree
+branches of FormThetaNC, ThetaOperationNC, RenormThetaNC, SizeOfBlocks and
+IndexLeft/Right, SwappingNC, and the number-conserving periodic steps."""
 import numpy as np
 import pytest
 
@@ -92,3 +92,52 @@ def test_product_state_labels_take_the_first_component_with_conserv(H):
     assert [int(x[0]) for x in ll] == [0, 1, 3] and [int(x[0]) for x in lr] == [3, 2, 0]
     ll, lr = H.product_state_labels(c0, 4, 5, None)
     assert [int(x[0]) for x in ll] == [0, 2, 5]
+
+
+@pytest.mark.parametrize("L", [4, 5])
+@pytest.mark.parametrize("order", [2, 5])
+@pytest.mark.parametrize("idf", [False, True])
+def test_nc_periodic_steps_follow_the_dense_ones(oracle, H, L, order, idf):
+    """TrotterStep2ndOrderPBCNC / 5thOrderPBCNC (with SwappingNC) at exact chi give
+    the state of the dense periodic steps, which the exact ring evolution pins."""
+    if idf:
+        d, chi, mf = 4, 16, 2
+        c0, N = sector_product_state(L, 11)
+        hb = two_species_bond()
+        gam, lam = H.product_state(c0, chi)
+        ll, lr = H.product_state_labels(c0, chi, N, CONSERV)
+        cons = CONSERV
+    else:
+        d, N, mf = 3, L, 2
+        chi = d ** (L // 2)
+        hb = H.bose_hubbard(L, d, 1.0, 2.0)[1]
+        gam, lam, ll, lr = H.initial_set_nc(L, d, chi, N)
+        cons = None
+    U = H.construct_propagators([hb] * L, 0.05, order, boundary="P")
+    gd = [g.copy(order="F") for g in gam]
+    ld = [x.copy() for x in lam]
+    for _ in range(3):
+        te = oracle.trotter_step_pbc_nc(gam, lam, ll, lr, U, N, mf, order, conserv=cons)
+        oracle.trotter_step_pbc(gd, ld, U, order)
+        assert te < 1e-11
+    assert 1.0 - abs(np.vdot(obs.state_vector(gd, ld), obs.state_vector(gam, lam))) < 1e-12
+    for link in range(1, L):
+        used = ll[link] < 1000
+        assert np.all(lr[link][used] == N - ll[link][used])
+
+
+def test_swapping_nc_is_the_dense_swap(oracle, H):
+    """SwappingNC on a number-conserving bond: same Lambda (as a multiset) and
+    two-site density as the dense Swapping of the same chain."""
+    L, d, chi, N = 6, 3, 9, 6
+    gam, lam, ll, lr = H.initial_set_nc(L, d, chi, N)
+    U = H.construct_propagators(H.bose_hubbard(L, d, 1.0, np.linspace(1.0, 3.0, L)), 0.1, 2)
+    for _ in range(2):
+        oracle.trotter_step_nc(gam, lam, ll, lr, U, N, d - 1, 2)
+    a = oracle.swapping_nc(gam[2], gam[3], lam[2], lam[3], lam[4], ll[2], ll[3], lr[3], lr[4], N, d - 1)
+    b = oracle.swapping(gam[2], gam[3], lam[2], lam[3], lam[4])
+    assert abs(a[5] - b[3]) < 1e-13
+    assert np.allclose(np.sort(a[2]), np.sort(b[2]), atol=1e-13)
+    ra = obs.two_site_rho(lam[2], a[0], a[2], a[1], lam[4])
+    rb = obs.two_site_rho(lam[2], b[0], b[2], b[1], lam[4])
+    assert np.allclose(ra, rb, atol=1e-13)
