@@ -162,6 +162,15 @@ int tebd_canonical_form_all(tebd_handle *h);
  * TwoSiteOpNC on links 1..L-1 then L-1..1.  NC mode; follows tebd_set_conserv. */
 int tebd_canonical_form_all_nc(tebd_handle *h);
 
+/* Kept-rank form (no reference counterpart; the reference keeps chi values):
+ * after each update keep the fewest leading singular values whose discarded
+ * weight -- everything beyond them, relative to ||Theta||^2 = 1 -- is at most
+ * `bound`; the remaining Lambda entries become exact zeros (NC: label 10000), so
+ * the neighbouring updates compact them away.  truncerr reports the full
+ * discarded weight.  bound = 0 restores the reference's rule.  Swapping keeps
+ * the reference's rule. */
+int tebd_set_rank_bound(tebd_handle *h, double bound);
+
 /* Internal degrees of freedom for every NC routine of the handle: the reference
  * passes the OPTIONAL argument intDegFree to TwoSiteOpNC, TrotterStepNC and
  * CanonicalFormAllNC (local_operations_module.f90:748-1443, 1723-1964;

@@ -632,6 +632,15 @@ extern "C" int tebd_swapping(tebd_handle *h, int link, double *truncerr) {
   return rc;
 }
 
+// Kept-rank form: discarded-weight bound per bond update (0 = the reference's
+// rule, keep chi values above the 1e-15 guard).
+extern "C" int tebd_set_rank_bound(tebd_handle *h, double bound) {
+  if (!h) return TEBD_ERR_ARG;
+  if (!(bound >= 0.0 && bound < 1.0)) return set_error(h, TEBD_ERR_ARG, "rank bound must lie in [0, 1)");
+  h->rank_bound = bound;
+  return TEBD_OK;
+}
+
 // TrotterStep2ndOrderPBC (propagation_module.f90:116-198) and
 // TrotterStep5thOrderPBC (:254-614); in NC mode TrotterStep2ndOrderPBCNC
 // (:1019-1186) and TrotterStep5thOrderPBCNC (:1244-1940), the same sequences with

@@ -372,18 +372,37 @@ __global__ void __launch_bounds__(1024) k_sigma_sort(Slot *slots, const double *
 }
 
 // FormLambda1 (:347-379): sequential in the reference's order, one thread per slot.
+// Kept-rank form (rank_bound > 0, no reference counterpart): keep the fewest
+// leading values whose discarded weight -- the weight beyond chi, 1 - sum of the
+// chi values, plus the dropped kept values summed from the smallest up -- stays
+// within rank_bound; the rest of Lambda1 is set to exactly zero, so that the
+// neighbouring updates compact those Schmidt indices away.
 __global__ void k_lambda(Slot *slots, const int *links, double *lam, double *truncerr, int chi,
-                         int nb) {
+                         int nb, double rank_bound) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nb) return;
   const double *S = slots[s].S;
+  int keep = chi;
+  if (rank_bound > 0.0) {
+    double all = 0.0;
+    for (int a = 0; a < chi; ++a)
+      if (fabs(S[a]) > kGuardDense) all = all + S[a] * S[a];
+    double w = fmax(1.0 - all, 0.0);  // weight beyond chi
+    keep = chi;
+    while (keep > 1) {
+      const double v = fabs(S[keep - 1]) > kGuardDense ? S[keep - 1] * S[keep - 1] : 0.0;
+      if (w + v > rank_bound) break;
+      w += v;
+      --keep;
+    }
+  }
   double norm = 0.0;
-  for (int a = 0; a < chi; ++a)
+  for (int a = 0; a < keep; ++a)
     if (fabs(S[a]) > kGuardDense) norm = norm + S[a] * S[a];
   truncerr[s] = fabs(1.0 - norm);
   double *l1 = lam + (size_t)links[s] * chi;
   const double rs = sqrt(norm);
-  for (int a = 0; a < chi; ++a) l1[a] = (fabs(S[a]) > kGuardDense) ? S[a] / rs : 0.0;
+  for (int a = 0; a < chi; ++a) l1[a] = (a < keep && fabs(S[a]) > kGuardDense) ? S[a] / rs : 0.0;
 }
 
 // Keep the last spectrum and sweep count of every link for tebd_get_singular_values.
@@ -524,7 +543,8 @@ int launch_dense_finish(tebd_handle *h, int nb) {
   cudaStream_t st = h->stream;
   k_sigma_sort<<<nb, 1024, sizeof(double) * n, st>>>(h->slots_d, h->nrm, n, h->status_d);
   TEBD_LAUNCHED(h);
-  k_lambda<<<cdiv(nb, 64), 64, 0, st>>>(h->slots_d, h->links_d, h->lam, h->truncerr_d, chi, nb);
+  k_lambda<<<cdiv(nb, 64), 64, 0, st>>>(h->slots_d, h->links_d, h->lam, h->truncerr_d, chi, nb,
+                                        h->unnormalized ? 0.0 : h->rank_bound);
   TEBD_LAUNCHED(h);
   k_store_spectrum<<<nb, 256, 0, st>>>(h->slots_d, h->links_d, h->js.sweeps, h->sig_link_d,
                                        h->sig_count_d, h->sweeps_link_d, n, h->path_d);
@@ -591,7 +611,7 @@ void raw_dense_finish(cudaStream_t st, double2 *gam, double *lam, const int *lin
                       int d) {
   const int n = chi * d;
   k_sigma_sort<<<1, 1024, sizeof(double) * n, st>>>(slots_d, nrm, n, status);
-  k_lambda<<<1, 32, 0, st>>>(slots_d, links_d, lam, truncerr, chi, 1);
+  k_lambda<<<1, 32, 0, st>>>(slots_d, links_d, lam, truncerr, chi, 1, 0.0);
   k_restore_gamma1<<<dim3(cdiv((size_t)n * chi, 256), 1), 256, 0, st>>>(gam, lam, links_d, slots_d,
                                                                        nrm, chi, d);
   k_restore_gamma2<<<dim3(cdiv(chi, 32), cdiv(n, 32), 1), 256, 0, st>>>(gam, lam, links_d, slots_d,

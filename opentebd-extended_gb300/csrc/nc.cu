@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(1024) k_nc_select(int *lab_l, int *lab_r, doub
                                                     const JacobiProblem<double> *probs,
                                                     const double *nrm, double *truncerr,
                                                     double *sig_link, int *sig_count, int chi, int d,
-                                                    int totNum, int bmax, int *status) {
+                                                    int totNum, int bmax, int *status, double rank_bound) {
   extern __shared__ double sh[];  // colnorm[sz] | flat rank scratch
   const int s = blockIdx.x;
   const NcSlot S = nc[s];
@@ -465,6 +465,26 @@ __global__ void __launch_bounds__(1024) k_nc_select(int *lab_l, int *lab_r, doub
     int *ll1 = lab_l + (size_t)link * chi;
     int *lr1 = lab_r + (size_t)link * chi;
     double *l1 = lam + (size_t)link * chi;
+    // kept-rank form (no reference counterpart): the fewest leading values whose
+    // discarded weight stays within rank_bound, as in the dense FormLambda1
+    int keep = chi;
+    if (rank_bound > 0.0) {
+      const int top = min(chi, sz);
+      double all = 0.0;
+      for (int beta = 0; beta < top; ++beta) {
+        const double v = S.ssfl[ord[beta] - 1];
+        if (v > kGuardNC) all = all + v * v;
+      }
+      double w = fmax(1.0 - all, 0.0);
+      keep = top;
+      while (keep > 1) {
+        const double v = S.ssfl[ord[keep - 1] - 1];
+        const double q = v > kGuardNC ? v * v : 0.0;
+        if (w + q > rank_bound) break;
+        w += q;
+        --keep;
+      }
+    }
     double renorm = 0.0;
     for (int beta = 0; beta < chi; ++beta) {
       int pb = 0, pp = 0;
@@ -484,11 +504,12 @@ __global__ void __launch_bounds__(1024) k_nc_select(int *lab_l, int *lab_r, doub
       S.pos_b[beta] = pb;
       S.pos_p[beta] = pp;
       // UpdateLabelLeft (:1583-1604) / UpdateLabelRight (:1615-1624)
-      const int lab = (beta < sz && v > kGuardNC) ? mnl + pb - 1 : kLabelUnused;
+      const bool kept = beta < sz && beta < keep && v > kGuardNC;
+      const int lab = kept ? mnl + pb - 1 : kLabelUnused;
       ll1[beta] = lab;
       lr1[beta] = lab < 1000 ? totNum - lab : kLabelUnused;
       // FormLambdaNC (:1642-1656)
-      const double tl = (beta < sz && v > kGuardNC) ? v : 0.0;
+      const double tl = kept ? v : 0.0;
       l1[beta] = tl;
       renorm = renorm + tl * tl;
     }
@@ -695,7 +716,7 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
   const size_t shb = std::max(sizeof(double) * (size_t)maxsz, sizeof(int) * (size_t)chi) + 16;
   k_nc_select<<<nb, 1024, shb, st>>>(h->lab_l, h->lab_r, h->lam, h->links_d, w->slots_d, w->probs_d,
                                      h->nrm, h->truncerr_d, h->sig_link_d, h->sig_count_d, chi, d, N,
-                                     bmax, h->status_d);
+                                     bmax, h->status_d, h->unnormalized ? 0.0 : h->rank_bound);
   TEBD_LAUNCHED(h);
   k_nc_zero_gammas<<<dim3(64, nb), 256, 0, st>>>(h->gam, h->links_d, chi, d);
   TEBD_LAUNCHED(h);

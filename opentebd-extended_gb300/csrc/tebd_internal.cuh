@@ -171,6 +171,7 @@ struct tebd_handle {
   tebd_stats stats;
   int profiling;
   int unnormalized;        // 1 while Swapping runs: Theta is decomposed without 1/||Theta||
+  double rank_bound;       // kept-rank form: discarded weight bound per bond (0 = keep chi)
   cudaEvent_t ev[6];
 };
 

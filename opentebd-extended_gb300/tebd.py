@@ -68,7 +68,7 @@ EXPORTED_SYMBOLS = (
     "tebd_local_energy", "tebd_total_energy", "tebd_inner_product", "tebd_chain_entropy",
     "tebd_record_lambdas", "tebd_record_gammas", "tebd_record_labels", "tebd_read_gamma_lambda",
     "tebd_read_gamma_lambda_labels", "tebd_swapping", "tebd_trotter_step_pbc", "tebd_canonical_form_all_nc",
-    "tebd_canonical_form", "tebd_canonical_form_all", "tebd_set_conserv",
+    "tebd_canonical_form", "tebd_canonical_form_all", "tebd_set_conserv", "tebd_set_rank_bound",
 )
 
 
@@ -176,6 +176,7 @@ def load_library(path: str = LIB_PATH):
     L.tebd_trotter_step_pbc.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(dp), dp]
     L.tebd_canonical_form_all_nc.argtypes = [vp]
     L.tebd_set_conserv.argtypes = [vp, ip]
+    L.tebd_set_rank_bound.argtypes = [vp, ctypes.c_double]
     L.tebd_canonical_form.argtypes = [vp, ctypes.c_int]
     L.tebd_canonical_form_all.argtypes = [vp]
     cp = ctypes.c_char_p
@@ -231,6 +232,11 @@ class Chain:
         self.conserv = None
         if conserv is not None:
             self.set_conserv(conserv)
+
+    def set_rank_bound(self, bound):
+        """Kept-rank form: keep the fewest singular values whose discarded weight is
+        at most ``bound`` per update (0 = the reference's rule, chi values)."""
+        self._check(self._lib.tebd_set_rank_bound(self.h, float(bound)))
 
     def set_conserv(self, conserv):
         """Internal degrees of freedom for the NC routines: ``conserv`` = Conserv%vi
