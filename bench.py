@@ -295,12 +295,16 @@ def run_ours(args):
               "ms_step_1": step_ms[0], "ms_step_last": step_ms[-1]}
 
     # ---- precision form beside the plain FP64 run (the metric's "mixed vs plain") --
-    prec = None
-    if args.svd == "fp64" and not args.no_precision:
-        num = np.diag(np.arange(D, dtype=float))
-        Hb = H.bose_hubbard(L, D, J, U, MU)
-        ref_obs = (chain.one_site_expval(num), chain.local_energy(Hb), chain.chain_entropy())
-        pc = pkg.Chain(L, D, CHI, device=local, svd_mode=SVD_MODES["df"])
+    num = np.diag(np.arange(D, dtype=float))
+    Hb = H.bose_hubbard(L, D, J, U, MU)
+    ref_obs = (chain.one_site_expval(num), chain.local_energy(Hb), chain.chain_entropy())
+
+    def leg(svd_mode, bound=0.0):
+        """The same K steps from the initial state on a second chain: updates/s from
+        CUDA events on its stream, and final-state observable errors against the
+        plain FP64 run."""
+        pc = pkg.Chain(L, D, CHI, device=local, svd_mode=svd_mode)
+        pc.set_rank_bound(bound)
         pc.set_state(gam, lam)
         for _ in range(args.warmup):
             pc.trotter_step(Udt, ORDER)
@@ -309,22 +313,37 @@ def run_ours(args):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
         e0.record(pstream)
+        te = 0.0
         for _ in range(args.steps):
-            pc.trotter_step(Udt, ORDER)
+            te += pc.trotter_step(Udt, ORDER)
         e1.record(pstream)
         barrier()
         pms = maxall(e0.elapsed_time(e1))
-        obs_p = (pc.one_site_expval(num), pc.local_energy(Hb), pc.chain_entropy())
-        pv = world * UPDATES_PER_STEP * args.steps / (pms / 1e3)
-        prec = {"svd": "TEBD_SVD_DF: bidiagonal route's trailing-matrix passes, trailing updates and "
-                       "back-transformation in double-float on the FP32 pipe; the rest FP64",
-                "value": pv, "unit": "updates/s", "ms_per_step": pms / args.steps,
-                "speedup_vs_plain_fp64": pv / value,
-                "max_abs_err_vs_plain_fp64": {"n_i": float(np.max(np.abs(obs_p[0] - ref_obs[0]))),
-                                              "bond_energy": float(np.max(np.abs(obs_p[1] - ref_obs[1]))),
-                                              "entropy": float(np.max(np.abs(obs_p[2] - ref_obs[2])))},
-                "error_bound": 1e-8}
+        o = (pc.one_site_expval(num), pc.local_energy(Hb), pc.chain_entropy())
+        ranks = [int(np.sum(x > 0)) for x in pc.get_state()[1][1:-1]]
         pc.close()
+        pv = world * UPDATES_PER_STEP * args.steps / (pms / 1e3)
+        err = {"n_i": float(np.max(np.abs(o[0] - ref_obs[0]))),
+               "bond_energy": float(np.max(np.abs(o[1] - ref_obs[1]))),
+               "entropy": float(np.max(np.abs(o[2] - ref_obs[2])))}
+        return {"value": pv, "unit": "updates/s", "ms_per_step": pms / args.steps,
+                "speedup_vs_plain_fp64": pv / value, "max_abs_err_vs_plain_fp64": err,
+                "within_error_bound": max(err.values()) <= 1e-8, "error_bound": 1e-8,
+                "total_truncerr": te, "final_mean_rank": float(np.mean(ranks))}
+
+    prec = None
+    if args.svd == "fp64" and not args.no_precision:
+        prec = {"svd": "TEBD_SVD_DF: bidiagonal route's trailing-matrix passes, trailing updates and "
+                       "back-transformation in double-float on the FP32 pipe; the rest FP64"}
+        prec.update(leg(SVD_MODES["df"]))
+    rank_form = None
+    if args.svd == "fp64" and args.rank_bound:
+        rank_form = []
+        for b in args.rank_bound:
+            for nm in ("fp64", "df"):
+                r = {"rank_bound": b, "svd": nm}
+                r.update(leg(SVD_MODES[nm], b))
+                rank_form.append(r)
 
     # ---- CPU baseline: the oracle port on a bounded sample ------------------
     cpu = None
@@ -386,6 +405,9 @@ def run_ours(args):
         "roofline": roof,
         "cpu_baseline": cpu,
         "precision_form": prec,
+        **({"rank_form": {"what": "kept-rank form: per-update discarded-weight bound "
+                                  "(tebd_set_rank_bound), Lambda beyond the kept rank exactly zero",
+                          "legs": rank_form}} if rank_form else {}),
         "clocks": clocks,
     }
     if rank == 0:
@@ -506,6 +528,9 @@ def main():
     ap.add_argument("--svd", default="fp64", choices=sorted(SVD_MODES))
     ap.add_argument("--save-obs", default=None, help="write final <n_i>, bond energies, Lambdas (npz)")
     ap.add_argument("--no-precision", action="store_true", help="skip the precision-form leg")
+    ap.add_argument("--rank-bound", type=float, nargs="*", default=None,
+                    help="extra legs of the kept-rank form at these discarded-weight bounds (FP64 and "
+                         "double-float), with speedup and observable errors against the plain run")
     ap.add_argument("--cpu-updates", type=int, default=2)
     ap.add_argument("--outdir", default=os.path.join(ROOT, "gpurun_out"))
     args = ap.parse_args()
