@@ -444,15 +444,17 @@ def run_nc(args):
     chain.set_state(gam, lam, ll, lr)
     chain.reset_stats()
     chain.set_profiling(True)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     torch.cuda.synchronize()
-    ev0.record(stream)
-    for _ in range(args.steps):
+    evs[0].record(stream)
+    for k in range(args.steps):
         chain.trotter_step(Udt, 2)
-    ev1.record(stream)
+        evs[k + 1].record(stream)
     torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
+    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    ms = sum(step_ms)
     st = chain.stats()
+    lam_end = chain.get_state()[1]
     per_step = NC_L - 1 + (NC_L // 2)  # 64 + 63 + 64
     out = {"metric": "two-site updates/sec, number-conserving (TwoSiteOpNC)", "value": per_step * args.steps / (ms / 1e3),
            "unit": "updates/s", "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -460,7 +462,11 @@ def run_nc(args):
                       "tot_num": NC_N, "dt": NC_DT, "U": "uniform[1,3] seed 3", "trotter_order": 2,
                       "timed_window": "steps 1..%d from the Mott state" % args.steps},
            "jacobi_ms": st["jacobi_ms"], "jacobi_launches": st["jacobi_launches"],
-           "gpu_launches": st["kernel_launches"]}
+           "gpu_launches": st["kernel_launches"],
+           "phases": {"ms_step_1": step_ms[0], "ms_step_last": step_ms[-1],
+                      "ms_per_step_last_10": sum(step_ms[-10:]) / min(10, args.steps)},
+           "final_rank": {"max": int(max(np.sum(x > 0) for x in lam_end)),
+                          "mean": float(np.mean([np.sum(x > 0) for x in lam_end[1:-1]]))}}
     print(json.dumps(out), flush=True)
     chain.close()
 

@@ -1462,24 +1462,26 @@ size_t bidiag_ws_doubles(int n, int chi) {
   return bd_scratch(n, chi) + 6 * (size_t)(2 * n) * K + 2 * (size_t)n * K;
 }
 
-int run_bidiag(tebd_handle *h, int nb, int nmax) {
+int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
   cudaStream_t st = h->stream;
-  const int kk = h->chi;
+  const int kk = b.kk, nb = b.nb, nmax = b.nmax;
+  Slot *slots_d = b.slots_d;
+  const int *path_d = b.path_d;
   int rc;
   if (h->profiling) cudaEventRecord(h->ev[0], st);
   bool any_t = false;
-  for (int s = 0; s < nb; ++s) any_t |= h->path_h[s] == kPathBidiagT;
+  for (int s = 0; s < nb; ++s) any_t |= b.path_h[s] == kPathBidiagT;
   if (any_t) {
-    k_bd_stage<<<dim3(128, nb), 256, 0, st>>>(h->slots_d, h->path_d);
+    k_bd_stage<<<dim3(128, nb), 256, 0, st>>>(slots_d, path_d);
     TEBD_LAUNCHED(h);
     const unsigned g = cdiv(nmax, 32) < 8 ? cdiv(nmax, 32) : 8;
-    k_bd_transpose<<<dim3(g, g, nb), 256, 0, st>>>(h->slots_d, h->path_d);
+    k_bd_transpose<<<dim3(g, g, nb), 256, 0, st>>>(slots_d, path_d);
     TEBD_LAUNCHED(h);
   }
   {
     cudaLaunchConfig_t cfg = {};
     const size_t smem = sizeof(double2) * ((size_t)nmax + 4 * kPanel) + sizeof(double) * kStageDoubles;
-    const bool dfp = h->opts.svd_mode == TEBD_SVD_DF;
+    const bool dfp = b.dfp;
     auto kern = dfp ? k_gebrd_df : k_gebrd;
     if ((rc = check_cuda(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                          "bidiagonalisation shared memory")))
@@ -1499,7 +1501,7 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     // smaller size (fewer barriers' worth of idle SMs in a partial wave).
     const int cmax = std::max(1, std::min(8, (nmax + 127) / 128));
     int nbd = 0;  // bonds on this route (the others' clusters exit at once)
-    for (int s = 0; s < nb; ++s) nbd += h->path_h[s] != kPathQRJ;
+    for (int s = 0; s < nb; ++s) nbd += b.path_h[s] != kPathQRJ;
     int C = 1;
     double best = 1e300;
     for (int c = 1; c <= cmax; ++c) {
@@ -1519,16 +1521,16 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     cfg.gridDim = dim3(C, nb, 1);
     attr[0].val.clusterDim.x = C;
     if (dfp) {
-      k_bd_to_df<<<dim3(128, nb), 256, 0, st>>>(h->slots_d, h->path_d);
+      k_bd_to_df<<<dim3(128, nb), 256, 0, st>>>(slots_d, path_d);
       TEBD_LAUNCHED(h);
     }
     if (h->profiling) cudaEventRecord(h->ev[4], st);
-    rc = check_cuda(h, cudaLaunchKernelEx(&cfg, kern, h->slots_d, (const int *)h->path_d),
+    rc = check_cuda(h, cudaLaunchKernelEx(&cfg, kern, slots_d, path_d),
                     "bidiagonalisation launch");
     if (rc) return rc;
     if (h->profiling) cudaEventRecord(h->ev[5], st);
     if (dfp) {  // the reflectors stay double-float for k_bd_apply_df; Pv follows
-      k_bd_pv_to_df<<<dim3(128, nb), 256, 0, st>>>(h->slots_d, h->path_d);
+      k_bd_pv_to_df<<<dim3(128, nb), 256, 0, st>>>(slots_d, path_d);
       TEBD_LAUNCHED(h);
     }
     TEBD_LAUNCHED(h);
@@ -1540,11 +1542,11 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
                                                  (int)smem),
                          "bisection shared memory")))
       return rc;
-    k_bd_sigma<<<dim3(cdiv(kk, kSigmaThreads), nb), kSigmaThreads, smem, st>>>(h->slots_d, h->path_d,
+    k_bd_sigma<<<dim3(cdiv(kk, kSigmaThreads), nb), kSigmaThreads, smem, st>>>(slots_d, path_d,
                                                                                 kk);
   }
   TEBD_LAUNCHED(h);
-  k_bd_invit<<<dim3(cdiv(kk, 32), nb), 32, 0, st>>>(h->slots_d, h->path_d, kk);
+  k_bd_invit<<<dim3(cdiv(kk, 32), nb), 32, 0, st>>>(slots_d, path_d, kk);
   TEBD_LAUNCHED(h);
   {
     const size_t smem = sizeof(double) * 5 * (size_t)(kk > 1 ? kk : 1);
@@ -1564,20 +1566,20 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if ((rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_bd_orth, h->slots_d, (const int *)h->path_d, kk),
+    if ((rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_bd_orth, slots_d, path_d, kk),
                          "orthogonalisation launch")))
       return rc;
   }
   TEBD_LAUNCHED(h);
-  if (h->opts.svd_mode == TEBD_SVD_DF) {
-    k_bd_apply_df<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
+  if (b.dfp) {
+    k_bd_apply_df<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(slots_d, path_d, kk);
     TEBD_LAUNCHED(h);
-    k_bd_store_df<<<dim3(256, nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
+    k_bd_store_df<<<dim3(256, nb), 256, 0, st>>>(slots_d, path_d, kk);
     TEBD_LAUNCHED(h);
   } else {
-    k_bd_apply<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
+    k_bd_apply<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(slots_d, path_d, kk);
     TEBD_LAUNCHED(h);
-    k_bd_store<<<dim3(256, nb), 256, 0, st>>>(h->slots_d, h->path_d, kk);
+    k_bd_store<<<dim3(256, nb), 256, 0, st>>>(slots_d, path_d, kk);
     TEBD_LAUNCHED(h);
   }
   if (h->profiling) {
@@ -1588,6 +1590,26 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
     if (cudaEventElapsedTime(&ms, h->ev[4], h->ev[5]) == cudaSuccess) h->stats.gebrd_ms += ms;
   }
   return check_cuda(h, cudaGetLastError(), "bidiag launch");
+}
+
+int run_bidiag(tebd_handle *h, int nb, int nmax) {
+  BidiagBatch b;
+  b.slots_d = h->slots_d;
+  b.path_d = h->path_d;
+  b.path_h = h->path_h.data();
+  b.nb = nb;
+  b.nmax = nmax;
+  b.kk = h->chi;
+  b.dfp = h->opts.svd_mode == TEBD_SVD_DF;
+  return run_bidiag_batch(h, b);
+}
+
+// Workspace of one bidiagonal problem of M x N (M >= N) computing all N triplets
+// (kk = the batch's largest N): aux, tau, taup (complex) and bdws (doubles).
+void bidiag_block_ws(int M, int N, int kk, size_t *aux_elems, size_t *bdws_doubles) {
+  const int K = std::min(kk, N);
+  *aux_elems = bd_aux_elems(M, N);
+  *bdws_doubles = bd_scratch(N, kk) + 6 * (size_t)(2 * N) * K + 2 * (size_t)M * K + 4;
 }
 
 }  // namespace tebd

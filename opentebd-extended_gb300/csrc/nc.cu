@@ -7,6 +7,7 @@
 //   FormThetaNC :748, ThetaOperationNC :853/:950, RenormThetaNC :1046,
 //   FormBlockTheta :1445                                                -> k_nc_theta
 //   SVDNC :1470 (one ZGESVD per block)                                  -> persistent Jacobi
+//                                     (blocks with both sides >= 64: bidiagonalisation)
 //   FlattenSS :1494, Ordering :1515, JudgePosition :1540,
 //   UpdateLabelLeft/Right :1567/:1607, FormLambdaNC :1627               -> k_nc_select
 //   FormGamma1NC :1659, FormGamma2NC :1691                               -> k_nc_gamma
@@ -74,7 +75,16 @@ struct NcWorkspace {
   int bmax;
   std::vector<NcSlot> slots;
   NcSlot *slots_d;
-  JacobiProblem<double> *probs_d;  // nslots * bmax problems
+  JacobiProblem<double> *probs_d;   // nslots * bmax problems
+  JacobiProblem<double> *small_d;   // the same list with the bidiagonal blocks emptied
+  // blocks on the bidiagonal route: slot table, records, routes and per-block
+  // workspaces, in one allocation grown on demand
+  char *bd_base = nullptr;
+  size_t bd_bytes = 0;
+  std::vector<JacobiProblem<double>> probs_h;
+  std::vector<Slot> bslots_h;
+  std::vector<Compact> bcp_h;
+  std::vector<int> bpath_h;
 };
 
 
@@ -588,6 +598,19 @@ __global__ void k_nc_gamma(double2 *gam, const double *lam, const int *links, Nc
   }
 }
 
+// The Jacobi list without the blocks that take the bidiagonal route (n = 0 there).
+__global__ void k_nc_mask(const JacobiProblem<double> *probs, JacobiProblem<double> *small, int count,
+                          int min_dim, int max_dim) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  JacobiProblem<double> P = probs[i];
+  if (P.n >= min_dim && P.m <= max_dim) {
+    P.m = 0;
+    P.n = 0;
+  }
+  small[i] = P;
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -606,7 +629,8 @@ int nc_alloc(tebd_handle *h) {
   if (!w) return TEBD_ERR_OOM;
   w->bmax = bmax;
   char *base = nullptr;
-  const size_t bytes = per * ns + al(sizeof(NcSlot) * ns) + sizeof(JacobiProblem<double>) * ns * bmax;
+  const size_t bytes = per * ns + al(sizeof(NcSlot) * ns) + al(sizeof(JacobiProblem<double>) * ns * bmax) +
+                       sizeof(JacobiProblem<double>) * ns * bmax;
   int rc = check_cuda(h, cudaMalloc((void **)&base, bytes), "alloc NC workspace");
   if (rc) {
     delete w;
@@ -647,6 +671,8 @@ int nc_alloc(tebd_handle *h) {
   w->slots_d = (NcSlot *)p;
   p += al(sizeof(NcSlot) * ns);
   w->probs_d = (JacobiProblem<double> *)p;
+  p += al(sizeof(JacobiProblem<double>) * ns * bmax);
+  w->small_d = (JacobiProblem<double> *)p;
   h->nc_ws = base;
   rc = check_cuda(h, cudaMemcpy(w->slots_d, w->slots.data(), sizeof(NcSlot) * ns,
                                 cudaMemcpyHostToDevice), "upload NC slot table");
@@ -663,9 +689,116 @@ int nc_alloc(tebd_handle *h) {
 void nc_free(tebd_handle *h) {
   if (h->nc_ws) cudaFree(h->nc_ws);
   h->nc_ws = nullptr;
-  delete reinterpret_cast<NcWorkspace *>(h->nc_meta);
+  NcWorkspace *w = reinterpret_cast<NcWorkspace *>(h->nc_meta);
+  if (w && w->bd_base) cudaFree(w->bd_base);
+  delete w;
   h->nc_meta = nullptr;
 }
+
+namespace {
+
+// Blocks whose both sides are >= kBidiagMinDim (the Jacobi problem is always
+// tall, m >= n) take the dense path's bidiagonal route, all n triplets each: the
+// block slot table points at the block's X (ld m) and V (ld n), so the output has
+// the Jacobi route's layout (X(:,c) = sigma_c u_c, V(:,c) = v_c) that the
+// selection and the Gamma scatter read.  Returns the number of such blocks; the
+// rest stay on the grouped Jacobi with `small_maxdim` its largest n.
+int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small_maxdim) {
+  const int bmax = w->bmax, count = nb * bmax;
+  cudaStream_t st = h->stream;
+  w->probs_h.resize(count);
+  int rc = check_cuda(h, cudaMemcpyAsync(w->probs_h.data(), w->probs_d, sizeof(JacobiProblem<double>) * count,
+                                         cudaMemcpyDeviceToHost, st), "read NC block problems");
+  if (rc) return rc;
+  if ((rc = check_cuda(h, cudaStreamSynchronize(st), "NC block problems"))) return rc;
+  w->bslots_h.clear();
+  w->bcp_h.clear();
+  int mmax = 0, nmaxb = 0, smax = 0;
+  for (int i = 0; i < count; ++i) {
+    const JacobiProblem<double> &P = w->probs_h[i];
+    if (P.n >= kBidiagMinDim && P.m <= kBidiagMaxDim) {
+      Slot b = {};
+      b.X = P.X;
+      b.V = P.V;
+      w->bslots_h.push_back(b);
+      Compact c = {};
+      c.m = P.m;
+      c.n = P.n;
+      c.k = P.n;
+      w->bcp_h.push_back(c);
+      mmax = std::max(mmax, P.m);
+      nmaxb = std::max(nmaxb, P.n);
+      h->stats.gebrd_flops += 16.0 * P.m * (double)P.n * P.n - 16.0 / 3.0 * (double)P.n * P.n * P.n;
+    } else {
+      smax = std::max(smax, P.n);
+    }
+  }
+  const int nl = (int)w->bslots_h.size();
+  *nbd = nl;
+  *small_maxdim = smax;
+  if (nl == 0) return TEBD_OK;
+  // workspace: tables, then per block aux | tau | taup | bdws
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t need = al(sizeof(Slot) * nl) + al(sizeof(Compact) * nl) + al(sizeof(int) * nl);
+  std::vector<size_t> aux_e(nl), bd_d(nl);
+  for (int i = 0; i < nl; ++i) {
+    bidiag_block_ws(w->bcp_h[i].m, w->bcp_h[i].n, nmaxb, &aux_e[i], &bd_d[i]);
+    need += al(sizeof(double2) * aux_e[i]) + 2 * al(sizeof(double2) * w->bcp_h[i].n) + al(sizeof(double) * bd_d[i]);
+  }
+  if (need > w->bd_bytes) {
+    if (w->bd_base) {
+      if ((rc = check_cuda(h, cudaStreamSynchronize(st), "NC bidiagonal workspace"))) return rc;
+      cudaFree(w->bd_base);
+      w->bd_base = nullptr;
+      w->bd_bytes = 0;
+    }
+    const size_t grow = need + need / 4;
+    if ((rc = check_cuda(h, cudaMalloc((void **)&w->bd_base, grow), "alloc NC bidiagonal workspace"))) return rc;
+    w->bd_bytes = grow;
+  }
+  char *p = w->bd_base;
+  Slot *tab_d = (Slot *)p;
+  p += al(sizeof(Slot) * nl);
+  Compact *cp_d = (Compact *)p;
+  p += al(sizeof(Compact) * nl);
+  int *path_d = (int *)p;
+  p += al(sizeof(int) * nl);
+  for (int i = 0; i < nl; ++i) {
+    Slot &b = w->bslots_h[i];
+    b.cp = cp_d + i;
+    b.aux = (double2 *)p;
+    p += al(sizeof(double2) * aux_e[i]);
+    b.tau = (double2 *)p;
+    p += al(sizeof(double2) * w->bcp_h[i].n);
+    b.taup = (double2 *)p;
+    p += al(sizeof(double2) * w->bcp_h[i].n);
+    b.bdws = (double *)p;
+    p += al(sizeof(double) * bd_d[i]);
+  }
+  w->bpath_h.assign(nl, kPathBidiag);
+  if ((rc = check_cuda(h, cudaMemcpyAsync(tab_d, w->bslots_h.data(), sizeof(Slot) * nl, cudaMemcpyHostToDevice, st),
+                       "upload NC block slots")))
+    return rc;
+  if ((rc = check_cuda(h, cudaMemcpyAsync(cp_d, w->bcp_h.data(), sizeof(Compact) * nl, cudaMemcpyHostToDevice, st),
+                       "upload NC block records")))
+    return rc;
+  if ((rc = check_cuda(h, cudaMemcpyAsync(path_d, w->bpath_h.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, st),
+                       "upload NC block routes")))
+    return rc;
+  k_nc_mask<<<(count + 255) / 256, 256, 0, st>>>(w->probs_d, w->small_d, count, kBidiagMinDim, kBidiagMaxDim);
+  TEBD_LAUNCHED(h);
+  BidiagBatch b;
+  b.slots_d = tab_d;
+  b.path_d = path_d;
+  b.path_h = w->bpath_h.data();
+  b.nb = nl;
+  b.nmax = mmax;
+  b.kk = nmaxb;
+  b.dfp = h->opts.svd_mode == TEBD_SVD_DF;
+  return run_bidiag_batch(h, b);
+}
+
+}  // namespace
 
 int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*truncerr*/) {
   NcWorkspace *w = reinterpret_cast<NcWorkspace *>(h->nc_meta);
@@ -712,7 +845,18 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
     maxdim = std::max(maxdim, hdr[(size_t)s * H_COUNT + H_MAXDIM]);
     maxsz = std::max(maxsz, hdr[(size_t)s * H_COUNT + H_SZ]);
   }
-  if ((rc = run_jacobi_problems(h, w->probs_d, nb * bmax, maxdim))) return rc;
+  if (maxdim >= kBidiagMinDim) {
+    // large blocks: bidiagonal route (launched first), the rest: grouped Jacobi
+    int nbd = 0, small_max = 0;
+    if ((rc = nc_route_blocks(h, w, nb, &nbd, &small_max))) return rc;
+    if (nbd == 0) {
+      if ((rc = run_jacobi_problems(h, w->probs_d, nb * bmax, maxdim))) return rc;
+    } else if (small_max > 0 && (rc = run_jacobi_problems(h, w->small_d, nb * bmax, small_max))) {
+      return rc;
+    }
+  } else if ((rc = run_jacobi_problems(h, w->probs_d, nb * bmax, maxdim))) {
+    return rc;
+  }
   const size_t shb = std::max(sizeof(double) * (size_t)maxsz, sizeof(int) * (size_t)chi) + 16;
   k_nc_select<<<nb, 1024, shb, st>>>(h->lab_l, h->lab_r, h->lam, h->links_d, w->slots_d, w->probs_d,
                                      h->nrm, h->truncerr_d, h->sig_link_d, h->sig_count_d, chi, d, N,

@@ -192,6 +192,17 @@ int jacobi_persistent_double(tebd_handle *h, const JacobiProblem<double> *probs_
                              int nmax, double tol, int max_sweeps);
 int run_qrj(tebd_handle *h, int nb, int nmax);
 int run_bidiag(tebd_handle *h, int nb, int nmax);
+// A batch of bidiagonal problems described by slot entries (X, V, aux, tau, taup,
+// bdws, cp) and routes; kk triplets per problem (min(kk, N) computed).
+struct BidiagBatch {
+  Slot *slots_d;
+  const int *path_d;
+  const int *path_h;
+  int nb, nmax, kk;
+  bool dfp;
+};
+int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b);
+void bidiag_block_ws(int M, int N, int kk, size_t *aux_elems, size_t *bdws_doubles);
 size_t bidiag_ws_doubles(int n, int chi);
 size_t bidiag_aux_elems(int n);
 constexpr int kBidiagMaxDim = 4096;  // larger compacted Theta take the QR + Jacobi route

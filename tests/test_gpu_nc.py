@@ -125,3 +125,52 @@ def test_nc_mode_errors(pkg):
         with pytest.raises(pkg.TebdError) as e:
             pkg.TwoSiteOp(1, np.eye(9, dtype=complex), c)
         assert e.value.code == 6
+
+
+def _nc_bond_with_large_blocks(chi=96, d=3, N=20, seed=8):
+    """A link-2 bond of an L=4 chain whose charge blocks are 64x32, 96x64, 64x96
+    and 32x64: alpha labels {8,9,10}, beta labels {9..12}, gamma labels {7,8,9}."""
+    rng = np.random.default_rng(seed)
+    L = 4
+    gam = [np.asfortranarray(rng.standard_normal((chi, d, chi)) + 1j * rng.standard_normal((chi, d, chi)))
+           for _ in range(L)]
+    lam = []
+    for _ in range(L + 1):
+        l = np.exp(-np.arange(chi) / 24.0)
+        lam.append(l / np.linalg.norm(l))
+    ll = [np.full(chi, 10000, dtype=np.int32) for _ in range(L + 1)]
+    lr = [np.full(chi, 10000, dtype=np.int32) for _ in range(L + 1)]
+    ll[1] = np.repeat(np.array([8, 9, 10], dtype=np.int32), chi // 3)
+    ll[2] = np.repeat(np.array([9, 10, 11, 12], dtype=np.int32), chi // 4)
+    lr[3] = np.repeat(np.array([7, 8, 9], dtype=np.int32), chi // 3)
+    for k in (1, 2):
+        lr[k] = (N - ll[k]).astype(np.int32)
+    ll[3] = (N - lr[3]).astype(np.int32)
+    return gam, lam, ll, lr
+
+
+@pytest.mark.parametrize("svd_mode", [0, 5])
+def test_nc_large_blocks_take_the_bidiagonal_route(pkg, oracle, svd_mode):
+    """Blocks with both sides >= 64 go through the bidiagonal route (all their
+    triplets), the others through the grouped Jacobi; the update matches the
+    oracle's per-block ZGESVD."""
+    chi, d, N = 96, 3, 20
+    gam, lam, ll, lr = _nc_bond_with_large_blocks(chi, d, N)
+    Hb = pkg.hamiltonians.bose_hubbard(4, d, 1.0, 2.0)
+    U = pkg.hamiltonians.matrix_exponential(Hb[1], 0.3)
+    with pkg.Chain(4, d, chi, mode=pkg.MODE_NC, tot_num=N, svd_mode=svd_mode) as c:
+        c.set_state(gam, lam, ll, lr)
+        c.reset_stats()
+        te = c.two_site_op(2, U)
+        assert c.stats()["gebrd_launches"] >= 1
+        g1, g2, l1 = c.get_gamma(2), c.get_gamma(3), c.get_lambda(3)
+        la, lb = c.get_labels(3)
+    r = oracle.two_site_op_nc(gam[1], gam[2], lam[1], lam[2], lam[3], U, ll[1], ll[2], lr[2], lr[3], N, d - 1)
+    rg1, rg2, rl1, rll1, rlr1, rte, rs = r
+    assert abs(te - rte) < 1e-11
+    assert np.allclose(np.sort(l1), np.sort(rl1), atol=1e-11)
+    assert sorted(zip(np.round(l1, 8), la)) == sorted(zip(np.round(rl1, 8), rll1))
+    assert np.all(np.isfinite(g1)) and np.all(np.isfinite(g2))
+    rho = obs.two_site_rho(lam[1], g1, l1, g2, lam[3])
+    rrho = obs.two_site_rho(lam[1], rg1, rl1, rg2, lam[3])
+    assert np.allclose(rho, rrho, atol=1e-11)
