@@ -435,40 +435,61 @@ def run_nc(args):
     H = pkg.hamiltonians
     gam, lam, ll, lr = H.initial_set_nc(NC_L, NC_D, NC_CHI, NC_N)
     Uvec = np.random.default_rng(3).uniform(1.0, 3.0, NC_L)
-    Udt = H.construct_propagators(H.bose_hubbard(NC_L, NC_D, 1.0, Uvec), NC_DT, 2)
-    chain = pkg.Chain(NC_L, NC_D, NC_CHI, mode=pkg.MODE_NC, tot_num=NC_N)
-    chain.set_state(gam, lam, ll, lr)
-    stream = torch.cuda.ExternalStream(chain.stream())
-    for _ in range(args.warmup):
-        chain.trotter_step(Udt, 2)
-    chain.set_state(gam, lam, ll, lr)
-    chain.reset_stats()
-    chain.set_profiling(True)
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    torch.cuda.synchronize()
-    evs[0].record(stream)
-    for k in range(args.steps):
-        chain.trotter_step(Udt, 2)
-        evs[k + 1].record(stream)
-    torch.cuda.synchronize()
-    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
-    ms = sum(step_ms)
-    st = chain.stats()
-    lam_end = chain.get_state()[1]
+    Hb = H.bose_hubbard(NC_L, NC_D, 1.0, Uvec)
+    Udt = H.construct_propagators(Hb, NC_DT, 2)
+    num = np.diag(np.arange(NC_D, dtype=float))
     per_step = NC_L - 1 + (NC_L // 2)  # 64 + 63 + 64
-    out = {"metric": "two-site updates/sec, number-conserving (TwoSiteOpNC)", "value": per_step * args.steps / (ms / 1e3),
+
+    def run(svd_mode):
+        chain = pkg.Chain(NC_L, NC_D, NC_CHI, mode=pkg.MODE_NC, tot_num=NC_N, svd_mode=svd_mode)
+        chain.set_state(gam, lam, ll, lr)
+        stream = torch.cuda.ExternalStream(chain.stream())
+        for _ in range(args.warmup):
+            chain.trotter_step(Udt, 2)
+        chain.set_state(gam, lam, ll, lr)
+        chain.reset_stats()
+        chain.set_profiling(True)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        torch.cuda.synchronize()
+        evs[0].record(stream)
+        for k in range(args.steps):
+            chain.trotter_step(Udt, 2)
+            evs[k + 1].record(stream)
+        torch.cuda.synchronize()
+        step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+        st = chain.stats()
+        lam_end = chain.get_state()[1]
+        obs = (chain.one_site_expval(num), chain.local_energy(Hb), chain.chain_entropy())
+        chain.close()
+        return step_ms, st, lam_end, obs
+
+    step_ms, st, lam_end, ref_obs = run(SVD_MODES[args.svd])
+    ms = sum(step_ms)
+    value = per_step * args.steps / (ms / 1e3)
+    out = {"metric": "two-site updates/sec, number-conserving (TwoSiteOpNC)", "value": value,
            "unit": "updates/s", "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "svd": args.svd,
            "config": {"workload": "nc_bose_hubbard_L128_d5_chi512", "L": NC_L, "d": NC_D, "chi": NC_CHI,
                       "tot_num": NC_N, "dt": NC_DT, "U": "uniform[1,3] seed 3", "trotter_order": 2,
-                      "timed_window": "steps 1..%d from the Mott state" % args.steps},
-           "jacobi_ms": st["jacobi_ms"], "jacobi_launches": st["jacobi_launches"],
+                      "timed_window": "steps 1..%d from the Mott state" % args.steps,
+                      "blocks": "charge blocks with both sides >= 16 bidiagonalised, the rest grouped Jacobi"},
+           "jacobi_ms": st["jacobi_ms"], "gebrd_ms": st["gebrd_ms"], "gebrd_launches": st["gebrd_launches"],
            "gpu_launches": st["kernel_launches"],
            "phases": {"ms_step_1": step_ms[0], "ms_step_last": step_ms[-1],
                       "ms_per_step_last_10": sum(step_ms[-10:]) / min(10, args.steps)},
            "final_rank": {"max": int(max(np.sum(x > 0) for x in lam_end)),
                           "mean": float(np.mean([np.sum(x > 0) for x in lam_end[1:-1]]))}}
+    if args.svd == "fp64" and not args.no_precision:
+        p_ms, _, _, p_obs = run(SVD_MODES["df"])
+        pv = per_step * args.steps / (sum(p_ms) / 1e3)
+        err = {"n_i": float(np.max(np.abs(p_obs[0] - ref_obs[0]))),
+               "bond_energy": float(np.max(np.abs(p_obs[1] - ref_obs[1]))),
+               "entropy": float(np.max(np.abs(p_obs[2] - ref_obs[2])))}
+        out["precision_form"] = {"svd": "TEBD_SVD_DF (double-float bidiagonalisation of the large blocks)",
+                                 "value": pv, "unit": "updates/s", "speedup_vs_plain_fp64": pv / value,
+                                 "max_abs_err_vs_plain_fp64": err, "error_bound": 1e-8,
+                                 "within_error_bound": max(err.values()) <= 1e-8}
     print(json.dumps(out), flush=True)
-    chain.close()
 
 
 # ---------------------------------------------------------------------------

@@ -233,6 +233,7 @@ __global__ void k_nc_blocks(const int *__restrict__ lab_l, const int *__restrict
 // each, so the norm's summation order is fixed.
 // ---------------------------------------------------------------------------
 constexpr int kMaxDnc = 8;
+constexpr int kNcBidiagMinDim = 16;  // smaller block side from which a block is bidiagonalised
 constexpr int kMaxPairs = 16;  // allowed (i, j) pairs of one pair total, intDegFree form
 static_assert(kMaxDnc <= 8, "NcLocal and the handle's table hold 8 local numbers");
 
@@ -697,7 +698,7 @@ void nc_free(tebd_handle *h) {
 
 namespace {
 
-// Blocks whose both sides are >= kBidiagMinDim (the Jacobi problem is always
+// Blocks whose both sides are >= kNcBidiagMinDim (the Jacobi problem is always
 // tall, m >= n) take the dense path's bidiagonal route, all n triplets each: the
 // block slot table points at the block's X (ld m) and V (ld n), so the output has
 // the Jacobi route's layout (X(:,c) = sigma_c u_c, V(:,c) = v_c) that the
@@ -716,7 +717,7 @@ int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small
   int mmax = 0, nmaxb = 0, smax = 0;
   for (int i = 0; i < count; ++i) {
     const JacobiProblem<double> &P = w->probs_h[i];
-    if (P.n >= kBidiagMinDim && P.m <= kBidiagMaxDim) {
+    if (P.n >= kNcBidiagMinDim && P.m <= kBidiagMaxDim) {
       Slot b = {};
       b.X = P.X;
       b.V = P.V;
@@ -785,7 +786,7 @@ int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small
   if ((rc = check_cuda(h, cudaMemcpyAsync(path_d, w->bpath_h.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, st),
                        "upload NC block routes")))
     return rc;
-  k_nc_mask<<<(count + 255) / 256, 256, 0, st>>>(w->probs_d, w->small_d, count, kBidiagMinDim, kBidiagMaxDim);
+  k_nc_mask<<<(count + 255) / 256, 256, 0, st>>>(w->probs_d, w->small_d, count, kNcBidiagMinDim, kBidiagMaxDim);
   TEBD_LAUNCHED(h);
   BidiagBatch b;
   b.slots_d = tab_d;
@@ -845,7 +846,7 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
     maxdim = std::max(maxdim, hdr[(size_t)s * H_COUNT + H_MAXDIM]);
     maxsz = std::max(maxsz, hdr[(size_t)s * H_COUNT + H_SZ]);
   }
-  if (maxdim >= kBidiagMinDim) {
+  if (maxdim >= kNcBidiagMinDim) {
     // large blocks: bidiagonal route (launched first), the rest: grouped Jacobi
     int nbd = 0, small_max = 0;
     if ((rc = nc_route_blocks(h, w, nb, &nbd, &small_max))) return rc;

@@ -151,9 +151,9 @@ def _nc_bond_with_large_blocks(chi=96, d=3, N=20, seed=8):
 
 @pytest.mark.parametrize("svd_mode", [0, 5])
 def test_nc_large_blocks_take_the_bidiagonal_route(pkg, oracle, svd_mode):
-    """Blocks with both sides >= 64 go through the bidiagonal route (all their
-    triplets), the others through the grouped Jacobi; the update matches the
-    oracle's per-block ZGESVD."""
+    """Blocks with both sides >= 16 go through the bidiagonal route (all their
+    triplets; here all four blocks), the update matches the oracle's per-block
+    ZGESVD."""
     chi, d, N = 96, 3, 20
     gam, lam, ll, lr = _nc_bond_with_large_blocks(chi, d, N)
     Hb = pkg.hamiltonians.bose_hubbard(4, d, 1.0, 2.0)
