@@ -968,7 +968,7 @@ __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const i
 //   U0 (reciprocal pivots), U1, U2 (upper factor of the pivoted LU), PV (multipliers),
 //   Y (swap flags), then the vector Z itself.
 // ---------------------------------------------------------------------------
-__global__ void k_bd_invit(Slot *slots, const int *path, int kk) {
+__global__ void k_bd_invit(Slot *slots, const int *path, int kk, int cap) {
   const int s = blockIdx.y;
   const int route = path[s];
   if (!on_route(route)) return;
@@ -976,7 +976,7 @@ __global__ void k_bd_invit(Slot *slots, const int *path, int kk) {
   int m, n;
   bd_dims(*S.cp, route, m, n);
   const int N = 2 * n;
-  const int K = min(kk, n);
+  const int K = cap ? min(min(kk, n), S.cp->k) : min(kk, n);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= K) return;
   const double *dd = S.bdws, *ee = S.bdws + n, *sig = S.bdws + 2 * n;
@@ -1093,7 +1093,7 @@ __global__ void k_bd_invit(Slot *slots, const int *path, int kk) {
 // subtraction one warp per row.
 constexpr int kOrthThreads = 512;
 constexpr int kOrthCluster = 2;
-__global__ void __launch_bounds__(kOrthThreads) k_bd_orth(Slot *slots, const int *path, int kk) {
+__global__ void __launch_bounds__(kOrthThreads) k_bd_orth(Slot *slots, const int *path, int kk, int cap) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks(), crank = (int)cluster.block_rank();
@@ -1103,7 +1103,7 @@ __global__ void __launch_bounds__(kOrthThreads) k_bd_orth(Slot *slots, const int
   const Slot S = slots[s];
   int m, n;
   bd_dims(*S.cp, route, m, n);
-  const int N = 2 * n, K = min(kk, n);
+  const int N = 2 * n, K = cap ? min(min(kk, n), S.cp->k) : min(kk, n);
   double *Z = S.bdws + bd_scratch(n, kk) + 5 * (size_t)N * K;
   double *xch = S.bdws + bd_scratch(n, kk) + (size_t)part * N * K;  // 2 x C x (K + 1)
   const int j0 = (int)((long long)n * crank / C), j1 = (int)((long long)n * (crank + 1) / C);
@@ -1213,14 +1213,14 @@ __global__ void __launch_bounds__(kOrthThreads) k_bd_orth(Slot *slots, const int
 //    Theta^H route: left -> Yu (= V of Theta), right -> Ru (= U of Theta, scratch
 //    in the inverse-iteration LU area, free by now).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_bd_apply(Slot *slots, const int *path, int kk) {
+__global__ void __launch_bounds__(256) k_bd_apply(Slot *slots, const int *path, int kk, int cap) {
   const int s = blockIdx.y;
   const int route = path[s];
   if (!on_route(route)) return;
   const Slot S = slots[s];
   int m, n;
   bd_dims(*S.cp, route, m, n);
-  const int N = 2 * n, K = min(kk, n);
+  const int N = 2 * n, K = cap ? min(min(kk, n), S.cp->k) : min(kk, n);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int col = blockIdx.x * 8 + warp;
   if (col >= 2 * K) return;
@@ -1287,14 +1287,14 @@ __global__ void __launch_bounds__(256) k_bd_apply(Slot *slots, const int *path, 
 
 // X(:, i) = U(:, i) sigma_i (Theta's m rows, ld m) and, on the transposed route,
 // V(:, i) = the left vectors of Theta^H (n rows, ld n).
-__global__ void k_bd_store(Slot *slots, const int *path, int kk) {
+__global__ void k_bd_store(Slot *slots, const int *path, int kk, int cap) {
   const int s = blockIdx.y;
   const int route = path[s];
   if (!on_route(route)) return;
   const Slot S = slots[s];
   int M, N;
   bd_dims(*S.cp, route, M, N);
-  const int m = S.cp->m, n = S.cp->n, K = min(kk, N);
+  const int m = S.cp->m, n = S.cp->n, K = cap ? min(min(kk, N), S.cp->k) : min(kk, N);
   double *base = S.bdws + bd_scratch(N, kk);
   const double *sig = S.bdws + 2 * N;
   const double2 *Yu = reinterpret_cast<const double2 *>(base + 12 * (size_t)N * K);
@@ -1308,21 +1308,26 @@ __global__ void k_bd_store(Slot *slots, const int *path, int kk) {
   if (route == kPathBidiagT)
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * K; e += stride)
       S.V[e] = Yu[e];
-  if (blockIdx.x == 0 && threadIdx.x == 0) S.cp->k = K;
+  if (cap) {  // columns past the capped count read as zero singular values
+    for (size_t e = (size_t)m * K + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)m * n; e += stride)
+      S.X[e] = make_double2(0.0, 0.0);
+  } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S.cp->k = K;
+  }
 }
 
 // Precision form of step 4: the same reflector products in double-float, reading
 // the left reflectors from the double-float matrix the bidiagonalisation left in
 // S.X and the right ones from Pv converted in place (k_bd_pv_to_df); the vectors
 // Yu / Ru are double-float too and k_bd_store_df converts them.
-__global__ void __launch_bounds__(256) k_bd_apply_df(Slot *slots, const int *path, int kk) {
+__global__ void __launch_bounds__(256) k_bd_apply_df(Slot *slots, const int *path, int kk, int cap) {
   const int s = blockIdx.y;
   const int route = path[s];
   if (!on_route(route)) return;
   const Slot S = slots[s];
   int m, n;
   bd_dims(*S.cp, route, m, n);
-  const int N = 2 * n, K = min(kk, n);
+  const int N = 2 * n, K = cap ? min(min(kk, n), S.cp->k) : min(kk, n);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int col = blockIdx.x * 8 + warp;
   if (col >= 2 * K) return;
@@ -1376,14 +1381,14 @@ __global__ void k_bd_pv_to_df(Slot *slots, const int *path) {  // Pv in place, N
     F[e] = dfs(S.aux[e]);
 }
 
-__global__ void k_bd_store_df(Slot *slots, const int *path, int kk) {
+__global__ void k_bd_store_df(Slot *slots, const int *path, int kk, int cap) {
   const int s = blockIdx.y;
   const int route = path[s];
   if (!on_route(route)) return;
   const Slot S = slots[s];
   int M, N;
   bd_dims(*S.cp, route, M, N);
-  const int m = S.cp->m, n = S.cp->n, K = min(kk, N);
+  const int m = S.cp->m, n = S.cp->n, K = cap ? min(min(kk, N), S.cp->k) : min(kk, N);
   double *base = S.bdws + bd_scratch(N, kk);
   const double *sig = S.bdws + 2 * N;
   const float4 *Yu = reinterpret_cast<const float4 *>(base + 12 * (size_t)N * K);
@@ -1397,7 +1402,12 @@ __global__ void k_bd_store_df(Slot *slots, const int *path, int kk) {
   const float4 *Vs = route == kPathBidiagT ? Yu : reinterpret_cast<const float4 *>(S.V);
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * K; e += stride)
     S.V[e] = dfd(Vs[e]);  // in place on the tall route (same element, same size)
-  if (blockIdx.x == 0 && threadIdx.x == 0) S.cp->k = K;
+  if (cap) {  // columns past the capped count read as zero singular values
+    for (size_t e = (size_t)m * K + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)m * n; e += stride)
+      S.X[e] = make_double2(0.0, 0.0);
+  } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S.cp->k = K;
+  }
 }
 
 // Precision form: the M x N matrix of the route as double-float in place before
@@ -1464,10 +1474,11 @@ size_t bidiag_ws_doubles(int n, int chi) {
 
 int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
   cudaStream_t st = h->stream;
-  const int kk = b.kk, nb = b.nb, nmax = b.nmax;
+  const int kk = b.kk, nb = b.nb, nmax = b.nmax, cap = b.cap;
   Slot *slots_d = b.slots_d;
   const int *path_d = b.path_d;
   int rc;
+  if (b.phase != 2) {  // bidiagonalisation and singular values
   if (h->profiling) cudaEventRecord(h->ev[0], st);
   bool any_t = false;
   for (int s = 0; s < nb; ++s) any_t |= b.path_h[s] == kPathBidiagT;
@@ -1546,7 +1557,9 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
                                                                                 kk);
   }
   TEBD_LAUNCHED(h);
-  k_bd_invit<<<dim3(cdiv(kk, 32), nb), 32, 0, st>>>(slots_d, path_d, kk);
+  if (b.phase == 1) return check_cuda(h, cudaGetLastError(), "bidiag launch");
+  }  // vectors
+  k_bd_invit<<<dim3(cdiv(kk, 32), nb), 32, 0, st>>>(slots_d, path_d, kk, cap);
   TEBD_LAUNCHED(h);
   {
     const size_t smem = sizeof(double) * 5 * (size_t)(kk > 1 ? kk : 1);
@@ -1566,20 +1579,20 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if ((rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_bd_orth, slots_d, path_d, kk),
+    if ((rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_bd_orth, slots_d, path_d, kk, cap),
                          "orthogonalisation launch")))
       return rc;
   }
   TEBD_LAUNCHED(h);
   if (b.dfp) {
-    k_bd_apply_df<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(slots_d, path_d, kk);
+    k_bd_apply_df<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(slots_d, path_d, kk, cap);
     TEBD_LAUNCHED(h);
-    k_bd_store_df<<<dim3(256, nb), 256, 0, st>>>(slots_d, path_d, kk);
+    k_bd_store_df<<<dim3(256, nb), 256, 0, st>>>(slots_d, path_d, kk, cap);
     TEBD_LAUNCHED(h);
   } else {
-    k_bd_apply<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(slots_d, path_d, kk);
+    k_bd_apply<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(slots_d, path_d, kk, cap);
     TEBD_LAUNCHED(h);
-    k_bd_store<<<dim3(256, nb), 256, 0, st>>>(slots_d, path_d, kk);
+    k_bd_store<<<dim3(256, nb), 256, 0, st>>>(slots_d, path_d, kk, cap);
     TEBD_LAUNCHED(h);
   }
   if (h->profiling) {
@@ -1601,6 +1614,8 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
   b.nmax = nmax;
   b.kk = h->chi;
   b.dfp = h->opts.svd_mode == TEBD_SVD_DF;
+  b.phase = 0;
+  b.cap = 0;
   return run_bidiag_batch(h, b);
 }
 

@@ -85,6 +85,8 @@ struct NcWorkspace {
   std::vector<Slot> bslots_h;
   std::vector<Compact> bcp_h;
   std::vector<int> bpath_h;
+  std::vector<int> blk2bs_h;  // (bond, block) -> bidiagonal block index, -1 for Jacobi
+  int *blk2bs_d = nullptr;
 };
 
 
@@ -612,6 +614,72 @@ __global__ void k_nc_mask(const JacobiProblem<double> *probs, JacobiProblem<doub
   small[i] = P;
 }
 
+// Between the two phases of the bidiagonal route: every value of the bond --
+// Jacobi blocks' column norms, bidiagonal blocks' bisection values -- is ranked,
+// and each bidiagonal block computes vectors only for its values that can enter
+// the global top chi (>= the chi-th largest, less a 1e-12 relative margin so that
+// near-ties are decided by the final values).  One CTA per bond.
+__global__ void __launch_bounds__(1024) k_nc_cut(NcSlot *nc, const JacobiProblem<double> *probs,
+                                                 const int *blk2bs, Slot *bslots, int bmax, int chi) {
+  extern __shared__ double val[];  // sz values of the bond
+  const int s = blockIdx.x;
+  const NcSlot S = nc[s];
+  const int nb = S.hdr[H_NB], sz = S.hdr[H_SZ];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int k = 0; k < nb; ++k) {
+    const JacobiProblem<double> P = probs[(size_t)s * bmax + k];
+    const int bs = blk2bs[(size_t)s * bmax + k];
+    const int o = S.soff[k];
+    if (bs >= 0) {
+      const double *sig = bslots[bs].bdws + 2 * P.n;
+      for (int c = threadIdx.x; c < P.n; c += blockDim.x) val[o + c] = sig[c];
+    } else {
+      for (int c = warp; c < P.n; c += nw) {
+        double acc = 0.0;
+        for (int r = lane; r < P.m; r += 32) {
+          const double2 v = P.X[r + (size_t)P.ldx * c];
+          acc = fma(v.x, v.x, fma(v.y, v.y, acc));
+        }
+        for (int q = 16; q > 0; q >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, q);
+        if (lane == 0) val[o + c] = sqrt(acc);
+      }
+    }
+  }
+  __syncthreads();
+  // the chi-th largest value: the smallest one with fewer than chi values above it
+  __shared__ double tau_s;
+  if (threadIdx.x == 0) tau_s = 0.0;
+  __syncthreads();
+  if (sz > chi) {
+    double best = INFINITY;
+    for (int t = threadIdx.x; t < sz; t += blockDim.x) {
+      const double v = val[t];
+      int above = 0;
+      for (int q = 0; q < sz; ++q) above += val[q] > v;
+      if (above < chi) best = fmin(best, v);
+    }
+    for (int q = 16; q > 0; q >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, q));
+    __shared__ double wmin[32];
+    if (lane == 0) wmin[warp] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = INFINITY;
+      for (int w = 0; w < nw; ++w) b = fmin(b, wmin[w]);
+      tau_s = b;
+    }
+    __syncthreads();
+  }
+  const double tau = tau_s * (1.0 - 1e-12);
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+    const int bs = blk2bs[(size_t)s * bmax + k];
+    if (bs < 0) continue;
+    const int n = probs[(size_t)s * bmax + k].n, o = S.soff[k];
+    int keep = 0;
+    while (keep < n && val[o + keep] >= tau) ++keep;  // bisection values are descending
+    bslots[bs].cp->k = keep > 0 ? keep : 1;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -704,7 +772,7 @@ namespace {
 // the Jacobi route's layout (X(:,c) = sigma_c u_c, V(:,c) = v_c) that the
 // selection and the Gamma scatter read.  Returns the number of such blocks; the
 // rest stay on the grouped Jacobi with `small_maxdim` its largest n.
-int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small_maxdim) {
+int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small_maxdim, BidiagBatch *out) {
   const int bmax = w->bmax, count = nb * bmax;
   cudaStream_t st = h->stream;
   w->probs_h.resize(count);
@@ -714,10 +782,12 @@ int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small
   if ((rc = check_cuda(h, cudaStreamSynchronize(st), "NC block problems"))) return rc;
   w->bslots_h.clear();
   w->bcp_h.clear();
+  w->blk2bs_h.assign(count, -1);
   int mmax = 0, nmaxb = 0, smax = 0;
   for (int i = 0; i < count; ++i) {
     const JacobiProblem<double> &P = w->probs_h[i];
     if (P.n >= kNcBidiagMinDim && P.m <= kBidiagMaxDim) {
+      w->blk2bs_h[i] = (int)w->bslots_h.size();
       Slot b = {};
       b.X = P.X;
       b.V = P.V;
@@ -740,7 +810,7 @@ int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small
   if (nl == 0) return TEBD_OK;
   // workspace: tables, then per block aux | tau | taup | bdws
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  size_t need = al(sizeof(Slot) * nl) + al(sizeof(Compact) * nl) + al(sizeof(int) * nl);
+  size_t need = al(sizeof(Slot) * nl) + al(sizeof(Compact) * nl) + al(sizeof(int) * nl) + al(sizeof(int) * count);
   std::vector<size_t> aux_e(nl), bd_d(nl);
   for (int i = 0; i < nl; ++i) {
     bidiag_block_ws(w->bcp_h[i].m, w->bcp_h[i].n, nmaxb, &aux_e[i], &bd_d[i]);
@@ -764,6 +834,8 @@ int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small
   p += al(sizeof(Compact) * nl);
   int *path_d = (int *)p;
   p += al(sizeof(int) * nl);
+  w->blk2bs_d = (int *)p;
+  p += al(sizeof(int) * count);
   for (int i = 0; i < nl; ++i) {
     Slot &b = w->bslots_h[i];
     b.cp = cp_d + i;
@@ -786,17 +858,22 @@ int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small
   if ((rc = check_cuda(h, cudaMemcpyAsync(path_d, w->bpath_h.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, st),
                        "upload NC block routes")))
     return rc;
+  if ((rc = check_cuda(h, cudaMemcpyAsync(w->blk2bs_d, w->blk2bs_h.data(), sizeof(int) * count,
+                                          cudaMemcpyHostToDevice, st),
+                       "upload NC block map")))
+    return rc;
   k_nc_mask<<<(count + 255) / 256, 256, 0, st>>>(w->probs_d, w->small_d, count, kNcBidiagMinDim, kBidiagMaxDim);
   TEBD_LAUNCHED(h);
-  BidiagBatch b;
-  b.slots_d = tab_d;
-  b.path_d = path_d;
-  b.path_h = w->bpath_h.data();
-  b.nb = nl;
-  b.nmax = mmax;
-  b.kk = nmaxb;
-  b.dfp = h->opts.svd_mode == TEBD_SVD_DF;
-  return run_bidiag_batch(h, b);
+  out->slots_d = tab_d;
+  out->path_d = path_d;
+  out->path_h = w->bpath_h.data();
+  out->nb = nl;
+  out->nmax = mmax;
+  out->kk = nmaxb;
+  out->dfp = h->opts.svd_mode == TEBD_SVD_DF;
+  out->phase = 0;
+  out->cap = 0;
+  return TEBD_OK;
 }
 
 }  // namespace
@@ -847,13 +924,24 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
     maxsz = std::max(maxsz, hdr[(size_t)s * H_COUNT + H_SZ]);
   }
   if (maxdim >= kNcBidiagMinDim) {
-    // large blocks: bidiagonal route (launched first), the rest: grouped Jacobi
+    // large blocks: bidiagonal route, the rest: grouped Jacobi.  The Jacobi blocks
+    // and the bidiagonal singular values come first, then the cut decides how
+    // many vectors each bidiagonal block needs.
     int nbd = 0, small_max = 0;
-    if ((rc = nc_route_blocks(h, w, nb, &nbd, &small_max))) return rc;
+    BidiagBatch bb;
+    if ((rc = nc_route_blocks(h, w, nb, &nbd, &small_max, &bb))) return rc;
     if (nbd == 0) {
       if ((rc = run_jacobi_problems(h, w->probs_d, nb * bmax, maxdim))) return rc;
-    } else if (small_max > 0 && (rc = run_jacobi_problems(h, w->small_d, nb * bmax, small_max))) {
-      return rc;
+    } else {
+      if (small_max > 0 && (rc = run_jacobi_problems(h, w->small_d, nb * bmax, small_max))) return rc;
+      bb.phase = 1;
+      if ((rc = run_bidiag_batch(h, bb))) return rc;
+      k_nc_cut<<<nb, 1024, sizeof(double) * (size_t)std::max(maxsz, 1), st>>>(w->slots_d, w->probs_d, w->blk2bs_d,
+                                                                           bb.slots_d, bmax, chi);
+      TEBD_LAUNCHED(h);
+      bb.phase = 2;
+      bb.cap = 1;
+      if ((rc = run_bidiag_batch(h, bb))) return rc;
     }
   } else if ((rc = run_jacobi_problems(h, w->probs_d, nb * bmax, maxdim))) {
     return rc;

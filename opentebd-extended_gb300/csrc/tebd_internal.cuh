@@ -200,6 +200,8 @@ struct BidiagBatch {
   const int *path_h;
   int nb, nmax, kk;
   bool dfp;
+  int phase;  // 0: whole route; 1: through the singular values; 2: the vectors
+  int cap;    // 1: vectors only for the first cp->k values of each problem (set between phases)
 };
 int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b);
 void bidiag_block_ws(int M, int N, int kk, size_t *aux_elems, size_t *bdws_doubles);
