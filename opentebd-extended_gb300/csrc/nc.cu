@@ -783,8 +783,16 @@ int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small
   w->bslots_h.clear();
   w->bcp_h.clear();
   w->blk2bs_h.assign(count, -1);
+  // largest problems first (16 M N^2 flops), so that the long bidiagonalisations
+  // start in the first wave and the small ones fill in behind them
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    const JacobiProblem<double> &A = w->probs_h[a], &B = w->probs_h[b];
+    return (double)A.m * A.n * A.n > (double)B.m * B.n * B.n;
+  });
   int mmax = 0, nmaxb = 0, smax = 0;
-  for (int i = 0; i < count; ++i) {
+  for (int i : order) {
     const JacobiProblem<double> &P = w->probs_h[i];
     if (P.n >= kNcBidiagMinDim && P.m <= kBidiagMaxDim) {
       w->blk2bs_h[i] = (int)w->bslots_h.size();
