@@ -493,6 +493,79 @@ def run_nc(args):
 
 
 # ---------------------------------------------------------------------------
+# Fermi-Hubbard precision-form configuration (extra line, not the headline):
+# spin-1/2 Hubbard chain L=64, d=4, t=1, U=4, mu=0 (half filling), a seeded random
+# MPS at chi=256 (complex Gaussian Gammas, seed 2, flat Lambdas) made canonical
+# with CanonicalFormAll on the device, then Forest-Ruth steps at dt=0.01.  Every
+# bond is a saturated 1024 x 1024 Theta from the first step.  The same K steps run
+# in plain FP64 and in the double-float form from the same canonical state;
+# observables after K steps are compared.
+# ---------------------------------------------------------------------------
+FH_L, FH_D, FH_CHI, FH_T, FH_U, FH_DT = 64, 4, 256, 1.0, 4.0, 0.01
+
+
+def run_fermi(args):
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    pkg = ge.load_package()
+    H = pkg.hamiltonians
+    rng = np.random.default_rng(2)
+    gam = [np.asfortranarray(rng.standard_normal((FH_CHI, FH_D, FH_CHI)) + 1j * rng.standard_normal((FH_CHI, FH_D, FH_CHI)))
+           for _ in range(FH_L)]
+    lam = [np.full(FH_CHI, 1.0 / np.sqrt(FH_CHI)) for _ in range(FH_L + 1)]
+    lam[0] = np.eye(FH_CHI)[0]
+    lam[FH_L] = np.eye(FH_CHI)[0]
+    Hb = H.fermi_hubbard(FH_L, FH_T, FH_U)
+    Udt = H.construct_propagators(Hb, FH_DT, 5)
+    with pkg.Chain(FH_L, FH_D, FH_CHI) as c:
+        c.set_state(gam, lam)
+        c.canonical_form_all()
+        gam, lam = c.get_state()
+    _, _, _, nop, _, _ = H.fermi_ops()
+    per_step = 4 * (FH_L // 2) + 3 * ((FH_L - 1) // 2)  # 4 odd + 3 even sweeps
+    legs = {}
+    for nm in ("fp64", "df"):
+        chain = pkg.Chain(FH_L, FH_D, FH_CHI, svd_mode=SVD_MODES[nm])
+        chain.set_state(gam, lam)
+        stream = torch.cuda.ExternalStream(chain.stream())
+        chain.trotter_step(Udt, 5)  # warm-up (kernels, workspaces) on the same chain ...
+        chain.set_state(gam, lam)   # ... then the timed steps from the canonical state
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        te = 0.0
+        for _ in range(args.steps):
+            te += chain.trotter_step(Udt, 5)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        legs[nm] = {"ms": ms, "te": te, "obs": (chain.one_site_expval(nop), chain.local_energy(Hb),
+                                                chain.chain_entropy()),
+                    "bidiag_updates": chain.stats()["bidiag_updates"]}
+        chain.close()
+    v = per_step * args.steps / (legs["fp64"]["ms"] / 1e3)
+    pv = per_step * args.steps / (legs["df"]["ms"] / 1e3)
+    ref, o = legs["fp64"]["obs"], legs["df"]["obs"]
+    err = {"n_i": float(np.max(np.abs(o[0] - ref[0]))), "bond_energy": float(np.max(np.abs(o[1] - ref[1]))),
+           "entropy": float(np.max(np.abs(o[2] - ref[2])))}
+    out = {"metric": "two-site updates/sec, Fermi-Hubbard chi=256 (Forest-Ruth)", "value": v, "unit": "updates/s",
+           "steps": args.steps, "ms_per_step": legs["fp64"]["ms"] / args.steps, "svd": "fp64",
+           "config": {"workload": "fermi_hubbard_L64_d4_chi256_forest_ruth", "L": FH_L, "d": FH_D, "chi": FH_CHI,
+                      "t": FH_T, "U": FH_U, "mu": 0.0, "dt": FH_DT, "trotter_order": 5,
+                      "updates_per_step": per_step,
+                      "initial": "random MPS chi=256 (seed 2) made canonical with CanonicalFormAll",
+                      "timed_window": "Forest-Ruth steps 1..%d" % args.steps},
+           "bidiag_updates": legs["fp64"]["bidiag_updates"], "total_truncerr": legs["fp64"]["te"],
+           "precision_form": {"svd": "TEBD_SVD_DF", "value": pv, "unit": "updates/s",
+                              "speedup_vs_plain_fp64": pv / v, "max_abs_err_vs_plain_fp64": err,
+                              "error_bound": 1e-8, "within_error_bound": max(err.values()) <= 1e-8}}
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
 # saturated-bond batch (extra line, not the headline): the cost regime that
 # dominates the configured run after step ~50.  The same chain shape (L=64, d=5,
 # chi=128) with every Lambda full (lambda_k ~ exp(-k/16), normalised) and complex
@@ -550,7 +623,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "nc", "saturated"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "nc", "saturated", "fermi_hubbard"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--svd", default="fp64", choices=sorted(SVD_MODES))
     ap.add_argument("--save-obs", default=None, help="write final <n_i>, bond energies, Lambdas (npz)")
@@ -568,6 +641,8 @@ def main():
         run_nc(args)
     elif args.workload == "saturated":
         run_saturated(args)
+    elif args.workload == "fermi_hubbard":
+        run_fermi(args)
     else:
         run_ours(args)
 

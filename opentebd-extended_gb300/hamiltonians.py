@@ -111,6 +111,48 @@ def bose_hubbard(L, d, J, U, mu=0.0, V=0.0):
 # ---------------------------------------------------------------------------
 # propagators
 # ---------------------------------------------------------------------------
+def fermi_ops():
+    """Spin-1/2 fermion operators of CreateFermiSops (fermi_hubbard_module.f90:100-245)
+    on the local Fock basis |n_up, n_down> in onsiteStateListIdof's order by total
+    number: (0,0), (1,0), (0,1), (1,1).  a_k carries the Jordan-Wigner phase
+    (-1)^(n of the components before k); returns a_up, a_down, one, ntot,
+    fermiPhase and the two-site tunnelling operator ttot."""
+    states = [(0, 0), (1, 0), (0, 1), (1, 1)]
+    d = len(states)
+    idx = {s: i for i, s in enumerate(states)}
+    a = []
+    for k in range(2):
+        m = np.zeros((d, d))
+        for j, sj in enumerate(states):
+            if sj[k] == 0:
+                continue
+            nj = list(sj)
+            nj[k] -= 1
+            m[idx[tuple(nj)], j] = (-1.0) ** sum(sj[:k])
+        a.append(m)
+    one = np.eye(d)
+    ntot = sum(x.T @ x for x in a)
+    fphase = np.diag((-1.0) ** np.diag(ntot))
+    ttot = sum(np.kron(x, one).T @ np.kron(fphase, x) + np.kron(fphase, x).T @ np.kron(x, one) for x in a)
+    return a[0], a[1], one, ntot, fphase, ttot
+
+
+def fermi_hubbard(L, J, U, mu=0.0):
+    """HamiltonianHubbard (fermi_hubbard_module.f90:289-356), spin 1/2, open
+    boundaries, no extPot/V0: -mu/2 (n x 1 + 1 x n) - J ttot + U/2 [(n_up - 1/2)
+    (n_dn - 1/2) x 1 + 1 x (...)] per bond, the edge bonds carrying the missing
+    halves of the first and last site."""
+    au, ad, one, n, _, ttot = fermi_ops()
+    hu = (au.T @ au - 0.5 * one) @ (ad.T @ ad - 0.5 * one)
+    H = []
+    for _ in range(L - 1):
+        H.append(-0.5 * mu * (np.kron(n, one) + np.kron(one, n)) - J * ttot
+                 + 0.5 * U * (np.kron(hu, one) + np.kron(one, hu)))
+    H[0] = H[0] - 0.5 * mu * np.kron(n, one) + 0.5 * U * np.kron(hu, one)
+    H[L - 2] = H[L - 2] - 0.5 * mu * np.kron(one, n) + 0.5 * U * np.kron(one, hu)
+    return H
+
+
 def matrix_exponential(H, t):
     """matrix_exponential_c (TEBDtools_module.f90:176-222): exp(-i t H) through the
     eigendecomposition of the Hermitian H (ZHEEV there, numpy eigh here)."""

@@ -136,3 +136,20 @@ def test_pbc_steps_follow_the_exact_ring_evolution(oracle, H, L, order, dt, boun
     w, v = np.linalg.eigh(_ring_hamiltonian(L, hb, d))
     exact = v @ (np.exp(-1j * w * dt * steps) * (v.conj().T @ psi0))
     assert 1.0 - abs(np.vdot(exact, obs.state_vector(gam, lam))) < bound
+
+
+def test_fermi_hubbard_two_site_known_answer(H):
+    """Two-site Hubbard at half filling: ground energy -sqrt(U^2/4 + 4 J^2) with the
+    particle-hole symmetric interaction; the bond term conserves the number."""
+    J, U = 1.0, 4.0
+    h = H.fermi_hubbard(2, J, U)[0]
+    assert np.allclose(h, h.conj().T)
+    _, _, one, n, _, _ = H.fermi_ops()
+    N = np.kron(n, one) + np.kron(one, n)
+    assert np.allclose(h @ N, N @ h)
+    sector = np.where(np.isclose(np.diag(N), 2.0))[0]
+    e = np.linalg.eigvalsh(h[np.ix_(sector, sector)])
+    assert abs(e[0] + np.sqrt(U * U / 4 + 4 * J * J)) < 1e-12
+    # one particle: hopping only (the interaction terms cancel), -J and +J twice each
+    s1 = np.where(np.isclose(np.diag(N), 1.0))[0]
+    assert np.allclose(np.linalg.eigvalsh(h[np.ix_(s1, s1)]), [-J, -J, J, J])
