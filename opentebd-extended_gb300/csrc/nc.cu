@@ -41,6 +41,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "df.cuh"
 #include "tebd_internal.cuh"
 
 namespace tebd {
@@ -239,7 +240,35 @@ constexpr int kNcBidiagMinDim = 16;  // smaller block side from which a block is
 constexpr int kMaxPairs = 16;  // allowed (i, j) pairs of one pair total, intDegFree form
 static_assert(kMaxDnc <= 8, "NcLocal and the handle's table hold 8 local numbers");
 
-template <bool kIdf>
+// Precision form: A = l0 G1 l1 and B = G2 l2 of each bond as double-float
+// (float4 per complex element) in the slot's V buffer, which the block SVDs only
+// use after the Theta kernel (k_nc_prepare_svd resets it).
+__global__ void k_nc_to_df(const double2 *__restrict__ gam, const double *__restrict__ lam,
+                           const int *links, Slot *slots, int chi, int d) {
+  const int s = blockIdx.y;
+  const int link = links[s];
+  const size_t csz = (size_t)chi * d * chi;
+  const double2 *G1 = gam + (size_t)(link - 1) * csz;
+  const double2 *G2 = gam + (size_t)link * csz;
+  const double *l0 = lam + (size_t)(link - 1) * chi;
+  const double *l1 = lam + (size_t)link * chi;
+  const double *l2 = lam + (size_t)(link + 1) * chi;
+  float4 *A = reinterpret_cast<float4 *>(slots[s].V), *B = A + csz;
+  const size_t cd = (size_t)chi * d;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < csz; e += (size_t)gridDim.x * blockDim.x) {
+    const int a = (int)(e % chi), b = (int)(e / cd);  // A: (a, i, b); B: (b, j, g) with g = e / (chi d)
+    const double wa = l0[a] * l1[b];
+    const double2 x = G1[e], y = G2[e];
+    A[e] = dfs(make_double2(wa * x.x, wa * x.y));
+    const double wb = l2[b];
+    B[e] = dfs(make_double2(wb * y.x, wb * y.y));
+  }
+}
+
+// kDF (precision form): the class dot products read A = l0 G1 l1 and B = G2 l2,
+// prepared as double-float in the slot's V buffer by k_nc_to_df, and accumulate
+// in double-float on the FP32 pipe; the gate mix and the norm stay FP64.
+template <bool kIdf, bool kDF>
 __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ gam,
                                                   const double *__restrict__ lam,
                                                   const int *__restrict__ lab_l,
@@ -263,6 +292,35 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
   const double2 *op = slots[s].gate;
   const int d2 = d * d;
   const int mnl = S.hdr[H_MINNL];
+  const float4 *Adf = reinterpret_cast<const float4 *>(slots[s].V);  // kDF: l0 G1 l1
+  const float4 *Bdf = Adf + csz;                                      // kDF: G2 l2
+  // Theta(a, i, jj, g) = sum over the betas of class q with LabelRight(link+1) =
+  // rgtN + r of l0 G1(a,i,b) l1 G2(b,jj,g) l2
+  auto cdot = [&](int q, int i, int jj, int r, int a, int g, int rgtN) -> double2 {
+    if (kDF) {
+      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+      for (int p = S.cls_off[q]; p < S.cls_off[q + 1]; ++p) {
+        const int b = S.cls_beta[p];
+        const int rgtN2 = lr1[b];
+        if (rgtN2 >= 1000 || rgtN2 - rgtN != r) continue;
+        df_cmac(rh, rl, ih, il, Adf[a + (size_t)chi * i + (size_t)chi * d * b],
+                Bdf[b + (size_t)chi * jj + (size_t)chi * d * g]);
+      }
+      return make_double2((double)rh + (double)rl, (double)ih + (double)il);
+    }
+    double2 sacc = make_double2(0.0, 0.0);
+    for (int p = S.cls_off[q]; p < S.cls_off[q + 1]; ++p) {
+      const int b = S.cls_beta[p];
+      const int rgtN2 = lr1[b];
+      if (rgtN2 >= 1000 || rgtN2 - rgtN != r) continue;
+      const double2 x = G1[a + (size_t)chi * i + (size_t)chi * d * b];
+      const double2 y = G2[b + (size_t)chi * jj + (size_t)chi * d * g];
+      const double w = l0[a] * l1[b] * l2[g];
+      sacc.x += w * (x.x * y.x - x.y * y.y);
+      sacc.y += w * (x.x * y.y + x.y * y.x);
+    }
+    return sacc;
+  };
   const size_t total = (size_t)chi * chi;
   const size_t chunk = (total + kNormParts - 1) / kNormParts;
   const size_t beg = blockIdx.x * chunk, end = min(beg + chunk, total);
@@ -288,18 +346,7 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
           // LabelRight(link+1) = rgtN + n_l, both differences within [0, maxFilling]
           double2 sacc = make_double2(0.0, 0.0);
           const int q = lftN + nl.n[i];
-          if (nl.n[i] <= maxFilling && q >= 0 && q <= totNum) {
-            for (int p = S.cls_off[q]; p < S.cls_off[q + 1]; ++p) {
-              const int b = S.cls_beta[p];
-              const int rgtN2 = lr1[b];
-              if (rgtN2 >= 1000 || rgtN2 - rgtN != r) continue;
-              const double2 x = G1[a + (size_t)chi * i + (size_t)chi * d * b];
-              const double2 y = G2[b + (size_t)chi * l + (size_t)chi * d * g];
-              const double w = l0[a] * l1[b] * l2[g];
-              sacc.x += w * (x.x * y.x - x.y * y.y);
-              sacc.y += w * (x.x * y.y + x.y * y.x);
-            }
-          }
+          if (nl.n[i] <= maxFilling && q >= 0 && q <= totNum) sacc = cdot(q, i, l, r, a, g, rgtN);
           th[np] = sacc;
           pi[np] = i;
           pl[np] = l;
@@ -335,18 +382,7 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
       if (li < 0 || li > maxFilling) continue;
       const int q = lftN + i;  // LabelLeft(link+1) of the contributing betas
       if (q < 0 || q > totNum) continue;
-      double2 sacc = make_double2(0.0, 0.0);
-      for (int p = S.cls_off[q]; p < S.cls_off[q + 1]; ++p) {
-        const int b = S.cls_beta[p];
-        const int rgtN2 = lr1[b];
-        if (rgtN2 >= 1000 || rgtN2 - rgtN != li) continue;  // j = rgtN2 - rgtN1 + 1
-        const double2 x = G1[a + (size_t)chi * i + (size_t)chi * d * b];
-        const double2 y = G2[b + (size_t)chi * li + (size_t)chi * d * g];
-        const double w = l0[a] * l1[b] * l2[g];
-        sacc.x += w * (x.x * y.x - x.y * y.y);
-        sacc.y += w * (x.x * y.y + x.y * y.x);
-      }
-      th[i] = sacc;
+      th[i] = cdot(q, i, li, li, a, g, rgtN);  // j = rgtN2 - rgtN1 + 1
     }
     // ThetaOperationNC: Theta'(a,k,jj,g) = sum_i Op2((k)d+jj, (i)d+ll) Theta(a,i,ll,g)
     for (int k = 0; k < d; ++k) {
@@ -904,12 +940,17 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
   k_nc_blocks<<<nb, 32, 0, st>>>(h->lab_l, h->lab_r, h->links_d, h->slots_d, w->slots_d, w->probs_d,
                                  chi, d, N, mf, bmax, nl);
   TEBD_LAUNCHED(h);
-  if (h->nc_idf)
-    k_nc_theta<true><<<dim3(kNormParts, nb), 256, 0, st>>>(h->gam, h->lam, h->lab_l, h->lab_r, h->links_d,
-                                                           h->slots_d, w->slots_d, chi, d, N, mf, nl);
-  else
-    k_nc_theta<false><<<dim3(kNormParts, nb), 256, 0, st>>>(h->gam, h->lam, h->lab_l, h->lab_r, h->links_d,
-                                                            h->slots_d, w->slots_d, chi, d, N, mf, nl);
+  const bool df = h->opts.svd_mode == TEBD_SVD_DF && d >= 2;  // A and B fill 2/d of V
+  if (df) {
+    k_nc_to_df<<<dim3(64, nb), 256, 0, st>>>(h->gam, h->lam, h->links_d, h->slots_d, chi, d);
+    TEBD_LAUNCHED(h);
+  }
+  {
+    auto kern = h->nc_idf ? (df ? k_nc_theta<true, true> : k_nc_theta<true, false>)
+                          : (df ? k_nc_theta<false, true> : k_nc_theta<false, false>);
+    kern<<<dim3(kNormParts, nb), 256, 0, st>>>(h->gam, h->lam, h->lab_l, h->lab_r, h->links_d, h->slots_d,
+                                               w->slots_d, chi, d, N, mf, nl);
+  }
   TEBD_LAUNCHED(h);
   k_nc_prepare_svd<<<dim3(32, nb), 256, 0, st>>>(w->slots_d, w->probs_d, h->nrm, bmax, h->status_d,
                                                  h->unnormalized);
