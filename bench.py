@@ -140,9 +140,46 @@ def cpu_sample(gam, lam, Udt, links, workers):
     return len(jobs) / wall, wall
 
 
+# ---------------------------------------------------------------------------
+# replicas (bench.py --gpus N under torchrun): one independent chain per GPU;
+# a gloo group serves only the barrier and the max over ranks of the timed
+# region -- there is no data-path collective
+# ---------------------------------------------------------------------------
+def replica_env():
+    """(rank, world size, local rank) from torchrun's environment; one process without it."""
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def replica_group(world):
+    """The gloo process group of N > 1 replicas, None for one process."""
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo")
+    return dist
+
+
+def replica_max(dist, x):
+    """Largest value of x over the replicas (the job's time is its slowest rank's)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
+def whole_job_rate(world, units_per_replica, ms_max):
+    """Units all replicas processed per second of the slowest replica's time."""
+    return world * units_per_replica / (ms_max / 1e3)
+
+
 def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    rank = replica_env()[0]
+    if rank != 0:  # under torchrun rank 0 alone times the host-core reference
         return
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     import __graft_entry__ as ge
@@ -195,14 +232,8 @@ def run_reference(args):
 def run_ours(args):
     import torch
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:  # independent replicas, one per GPU; gloo only for barrier/max
-        import torch.distributed as dist
-
-        dist.init_process_group("gloo")
+    rank, world, local = replica_env()
+    dist = replica_group(world)  # independent replicas, one per GPU; gloo only for barrier/max
     torch.cuda.set_device(local)
     import __graft_entry__ as ge
 
@@ -224,11 +255,7 @@ def run_ours(args):
             dist.barrier()
 
     def maxall(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t[0])
+        return replica_max(dist, x)
 
     # warm-up on the same chain; the timed pass then uploads the initial state
     # again, so that the timed K steps are steps 1..K of the configured run (the
@@ -285,8 +312,8 @@ def run_ours(args):
     st = chain.stats()
     chain.set_profiling(False)
     state_g, state_l = pin_g, pin_l
-    value = world * UPDATES_PER_STEP * args.steps / (ms / 1e3)
-    e2e = world * UPDATES_PER_STEP * args.steps / (e2e_ms / 1e3)
+    value = whole_job_rate(world, UPDATES_PER_STEP * args.steps, ms)
+    e2e = whole_job_rate(world, UPDATES_PER_STEP * args.steps, e2e_ms)
     h2d = gate_bytes + state_bytes / args.steps
     d2h = 8 * UPDATES_PER_STEP + 16 * 3 + state_bytes / args.steps
     sat = step_ms[49:] if args.steps > 60 else []
@@ -322,7 +349,7 @@ def run_ours(args):
         o = (pc.one_site_expval(num), pc.local_energy(Hb), pc.chain_entropy())
         ranks = [int(np.sum(x > 0)) for x in pc.get_state()[1][1:-1]]
         pc.close()
-        pv = world * UPDATES_PER_STEP * args.steps / (pms / 1e3)
+        pv = whole_job_rate(world, UPDATES_PER_STEP * args.steps, pms)
         err = {"n_i": float(np.max(np.abs(o[0] - ref_obs[0]))),
                "bond_energy": float(np.max(np.abs(o[1] - ref_obs[1]))),
                "entropy": float(np.max(np.abs(o[2] - ref_obs[2])))}
