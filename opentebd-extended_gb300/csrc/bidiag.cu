@@ -82,6 +82,7 @@ __host__ __device__ __forceinline__ size_t bd_scratch(int n, int kk) {
 //    Output (as ZGEBD2): d, e in bdws; tauq in S.tau, v_i below the diagonal of
 //    column i; taup in S.taup, u_i in column i of Pv with u_i(i+1) = 1.
 // ---------------------------------------------------------------------------
+constexpr int kDfLoads = 8;  // loads in flight per lane in the double-float passes
 constexpr int kPanel = 8;   // columns per panel (narrow: the per-column corrections grow with it)
 constexpr int kChunk = 32;  // columns per task of the w = A0 u pass
 constexpr int kTile = 64;   // trailing-update tile (rows and columns)
@@ -568,12 +569,12 @@ __global__ void __launch_bounds__(kBW * 32) k_gebrd_df(Slot *slots, const int *p
             const float4 *col = &AE(0, it < ncol ? i + 1 + it : p + (it - ncol));
             float ar = 0.f, arl = 0.f, ai = 0.f, ail = 0.f;
             int r = i + lane;
-            for (; r + 96 < M; r += 128) {
-              float4 c[4];
+            for (; r + 32 * (kDfLoads - 1) < M; r += 32 * kDfLoads) {
+              float4 c[kDfLoads];
 #pragma unroll
-              for (int q = 0; q < 4; ++q) c[q] = __ldcg(col + r + 32 * q);
+              for (int q = 0; q < kDfLoads; ++q) c[q] = __ldcg(col + r + 32 * q);
 #pragma unroll
-              for (int q = 0; q < 4; ++q) df_cmac_ca(ar, arl, ai, ail, c[q], vec[r + 32 * q - i]);
+              for (int q = 0; q < kDfLoads; ++q) df_cmac_ca(ar, arl, ai, ail, c[q], vec[r + 32 * q - i]);
             }
             for (; r < M; r += 32) df_cmac_ca(ar, arl, ai, ail, __ldcg(col + r), vec[r - i]);
             acc = make_double2(df_warp_sum(ar, arl), df_warp_sum(ai, ail));
@@ -655,12 +656,12 @@ __global__ void __launch_bounds__(kBW * 32) k_gebrd_df(Slot *slots, const int *p
               float ar = 0.f, arl = 0.f, ai = 0.f, ail = 0.f;
               const float4 *rp = &AE(r, 0);
               int c = c0;
-              for (; c + 3 < c1; c += 4) {
-                float4 a[4];
+              for (; c + kDfLoads - 1 < c1; c += kDfLoads) {
+                float4 a[kDfLoads];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) a[q] = __ldcg(rp + (size_t)M * (c + q));
+                for (int q = 0; q < kDfLoads; ++q) a[q] = __ldcg(rp + (size_t)M * (c + q));
 #pragma unroll
-                for (int q = 0; q < 4; ++q) df_cmac(ar, arl, ai, ail, a[q], vec[c + q - i - 1]);
+                for (int q = 0; q < kDfLoads; ++q) df_cmac(ar, arl, ai, ail, a[q], vec[c + q - i - 1]);
               }
               for (; c < c1; ++c) df_cmac(ar, arl, ai, ail, __ldcg(rp + (size_t)M * c), vec[c - i - 1]);
               ax.part[(size_t)cc * M + r] = make_double2((double)ar + (double)arl, (double)ai + (double)ail);
