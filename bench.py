@@ -659,7 +659,8 @@ def main():
                     help="extra legs of the kept-rank form at these discarded-weight bounds (FP64 and "
                          "double-float), with speedup and observable errors against the plain run")
     ap.add_argument("--cpu-updates", type=int, default=2)
-    ap.add_argument("--outdir", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--outdir", default=os.path.join(ROOT, "bench_out"),
+                    help="where the clock samples of the timed region are written")
     args = ap.parse_args()
     os.makedirs(args.outdir, exist_ok=True)
     if args.impl == "reference":

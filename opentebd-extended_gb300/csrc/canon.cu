@@ -1,7 +1,7 @@
 // canon.cu -- CanonicalForm and CanonicalFormAll of the dense chain
 // (VidalCore_v_2.0/local_operations_module.f90:496-610, propagation_module.f90:617-634),
 // the re-orthogonalisation of the Schmidt bases the reference's imaginary-time
-// driver runs after its steps.  For one bond (Lambda0, Gamma1, Lambda1, Gamma2,
+// evolution (ImagTimeProp) runs after its steps.  For one bond (Lambda0, Gamma1, Lambda1, Gamma2,
 // Lambda2), chi x chi matrices throughout:
 //   M1 = sum_{i,g} conj(G1(g,i,:))^T l0(g)^2 G1(g,i,:)      = U1 S1 U1^H
 //   G1t(:,i,b) = G1(:,i,:) U1(:,b) / sqrt(S1(b))   (0 where S1(b) <= 1e-8)

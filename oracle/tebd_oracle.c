@@ -926,8 +926,8 @@ int oracle_trotter_step_nc(int L, int chi, int d, int totNum, int maxFilling, in
  * SwappingNC with the labels); the sequences are the reference's, which are the
  * same for both (propagation_module.f90:116-614 and 1019-1940).  The edge bond
  * (L,1) is applied on bond 1 after swapping site L down to site 2: the edge calls
- * in the NC drivers pass the loop variable after `DO i=systemSize-1,2,(-1)`,
- * which is 1 there. */
+ * of the NC Trotter routines pass the loop variable after
+ * `DO i=systemSize-1,2,(-1)`, which is 1 there. */
 typedef struct {
   int nc, chi, d, totNum, maxFilling;
   double **gammas, **lambdas;
