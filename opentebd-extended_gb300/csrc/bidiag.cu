@@ -889,13 +889,20 @@ __device__ __forceinline__ int gk_count_df(const float2 *sqd, int n1, float xh, 
 //   Each value is found by a team of kTeam lanes that evaluate kTeam points of
 //   the bracket at once (multisection): the counts are monotone in x, so the
 //   leading run of "count <= target" in the team's ballot picks one of kTeam + 1
-//   subintervals, about 3.2 bits per step instead of bisection's 1.  The kernel
-//   is bound by the latency of the sequential Sturm recurrences (one thread per
-//   value gave one warp per SM), so the extra lanes cost no time.
+//   subintervals (8 lanes: about 3.2 bits per step instead of bisection's 1).
+//   With few values in the batch (a dense sweep: 32 bonds x chi) the kernel is
+//   bound by the latency of the sequential Sturm recurrences and the extra lanes
+//   are free; with many (number-conserving blocks: every value of every block)
+//   the counts fill the GPU on their own and teams of 1 lane (bisection) do the
+//   least work.  The host picks kTeam per launch.
 constexpr int kSigmaThreads = 32;
-constexpr int kTeam = 8;
-constexpr int kSigmaValues = kSigmaThreads / kTeam;  // values per block
+template <int kTeam>
 __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const int *path, int kk) {
+  constexpr int kSigmaValues = kSigmaThreads / kTeam;  // values per block
+  // step caps (safety only; the width tests end the loops): log2(kTeam + 1) bits
+  // per step for the 22 bits of the FP32 stage and the ~26 of the double-float one
+  constexpr int kIt32 = kTeam == 1 ? 26 : kTeam == 2 ? 17 : kTeam == 4 ? 12 : 10;
+  constexpr int kItDf = kTeam == 1 ? 34 : kTeam == 2 ? 22 : kTeam == 4 ? 16 : 12;
   const int s = blockIdx.y;
   const int route = path[s];
   if (!on_route(route)) return;
@@ -926,7 +933,7 @@ __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const i
   }
   __syncthreads();
   const int team = threadIdx.x / kTeam, t = threadIdx.x % kTeam;
-  const unsigned tmask = ((1u << kTeam) - 1u) << (kTeam * team);
+  const unsigned tmask = (kTeam == 32 ? 0xffffffffu : ((1u << kTeam) - 1u)) << (kTeam * team);
   const int i = blockIdx.x * kSigmaValues + team;
   if (i >= K) return;  // the whole team leaves together
   const int target = 2 * n - 1 - i;  // count(< x) <= target  <=>  x <= sigma_i
@@ -938,7 +945,7 @@ __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const i
   };
   // 1. FP32 bracket of width 2^-22 on the scaled problem
   float lf = 0.0f, hf = 1.0f;
-  for (int it = 0; it < 12 && hf - lf > 2.384185791015625e-07f; ++it) {
+  for (int it = 0; it < kIt32 && hf - lf > 2.384185791015625e-07f; ++it) {
     const float w = (hf - lf) * (1.0f / (kTeam + 1));
     const int k = lead(gk_count_f32(sqf, n1, lf + w * (float)(t + 1)) <= target);
     const float nl = k > 0 ? lf + w * (float)k : lf;
@@ -947,7 +954,7 @@ __global__ void __launch_bounds__(kSigmaThreads) k_bd_sigma(Slot *slots, const i
   }
   // 2. double-float stage to 2^-42 from the FP32 bracket widened by 2^-18
   double ls = fmax(0.0, (double)lf - 3.814697265625e-06), hs = fmin(1.0, (double)hf + 3.814697265625e-06);
-  for (int it = 0; it < 24 && hs - ls > 2.2737367544323206e-13; ++it) {
+  for (int it = 0; it < kItDf && hs - ls > 2.2737367544323206e-13; ++it) {
     const double w = (hs - ls) * (1.0 / (kTeam + 1));
     const double x = ls + w * (double)(t + 1);
     const float xh = (float)x;
@@ -1566,11 +1573,19 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
   }
   {
     const size_t smem = (sizeof(double) + sizeof(float2) + sizeof(float)) * (size_t)(2 * nmax);
-    if ((rc = check_cuda(h, cudaFuncSetAttribute(k_bd_sigma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem),
+    // team size: multisection while the batch's values (nb x kk at most) leave the
+    // GPU's resident threads idle, plain bisection once they fill them
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const double values = (double)nb * kk, slots_resident = 2048.0 * std::max(sms, 1);
+    const int team = values * 8 <= slots_resident ? 8 : values * 4 <= slots_resident ? 4
+                     : values * 2 <= slots_resident ? 2 : 1;
+    auto kern = team == 8 ? k_bd_sigma<8> : team == 4 ? k_bd_sigma<4> : team == 2 ? k_bd_sigma<2> : k_bd_sigma<1>;
+    if ((rc = check_cuda(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                          "bisection shared memory")))
       return rc;
-    k_bd_sigma<<<dim3(cdiv(kk, kSigmaValues), nb), kSigmaThreads, smem, st>>>(slots_d, path_d, kk);
+    kern<<<dim3(cdiv(kk, kSigmaThreads / team), nb), kSigmaThreads, smem, st>>>(slots_d, path_d, kk);
   }
   TEBD_LAUNCHED(h);
   if (b.phase == 1) return check_cuda(h, cudaGetLastError(), "bidiag launch");

@@ -867,7 +867,7 @@ int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small
       w->bd_base = nullptr;
       w->bd_bytes = 0;
     }
-    const size_t grow = need + need / 4;
+    const size_t grow = 2 * need;  // doubling: a few reallocations over a run whose blocks grow
     if ((rc = check_cuda(h, cudaMalloc((void **)&w->bd_base, grow), "alloc NC bidiagonal workspace"))) return rc;
     w->bd_bytes = grow;
   }
