@@ -1230,6 +1230,156 @@ __global__ void __launch_bounds__(kOrthThreads) k_bd_orth(Slot *slots, const int
 #undef XC
 }
 
+// Precision form of step 3's re-orthogonalisation: the same schedule on Z held
+// as double-float (float2 per real, converted in place by k_bd_z_df before and
+// back after), so the dot products and the subtractions run on the FP32 pipe;
+// the cross-lane and cross-CTA sums and the norms stay FP64.
+__global__ void k_bd_z_df(Slot *slots, const int *path, int kk, int cap, int to_df) {
+  const int s = blockIdx.y;
+  const int route = path[s];
+  if (!on_route(route)) return;
+  const Slot S = slots[s];
+  int m, n;
+  bd_dims(*S.cp, route, m, n);
+  const int N = 2 * n, K = cap ? min(min(kk, n), S.cp->k) : min(kk, n);
+  double *Z = S.bdws + bd_scratch(n, kk) + 5 * (size_t)N * K;
+  float2 *Zf = reinterpret_cast<float2 *>(Z);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)N * K;
+       e += (size_t)gridDim.x * blockDim.x) {
+    if (to_df) {
+      const double x = Z[e];
+      const float h = (float)x;
+      Zf[e] = make_float2(h, (float)(x - (double)h));
+    } else {
+      const float2 v = Zf[e];
+      Z[e] = (double)v.x + (double)v.y;
+    }
+  }
+}
+
+__device__ __forceinline__ void df_fma2(float &h, float &l, float2 a, float2 b) { df_mac(h, l, a.x, a.y, b.x, b.y); }
+
+__global__ void __launch_bounds__(kOrthThreads) k_bd_orth_df(Slot *slots, const int *path, int kk, int cap) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks(), crank = (int)cluster.block_rank();
+  const int s = blockIdx.y, part = blockIdx.x / C;  // part 0: v = z[2j], 1: u = z[2j+1]
+  const int route = path[s];
+  if (!on_route(route)) return;  // uniform per cluster
+  const Slot S = slots[s];
+  int m, n;
+  bd_dims(*S.cp, route, m, n);
+  const int N = 2 * n, K = cap ? min(min(kk, n), S.cp->k) : min(kk, n);
+  float2 *Z = reinterpret_cast<float2 *>(S.bdws + bd_scratch(n, kk) + 5 * (size_t)N * K);
+  double *xch = S.bdws + bd_scratch(n, kk) + (size_t)part * N * K;  // 2 x C x (K + 1)
+  const int j0 = (int)((long long)n * crank / C), j1 = (int)((long long)n * (crank + 1) / C);
+  extern __shared__ double dots[];  // K dot products, then 4 x K partial sums
+  double *psum = dots + K;
+  float2 *dotf = reinterpret_cast<float2 *>(psum);  // the dots as double-float for the subtraction
+  __shared__ double red[kOrthThreads / 32];
+  __shared__ double nrm_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarp = kOrthThreads / 32;
+  const int qt = tid & 127, jc = tid >> 7;
+  int post = 0;
+#define ZE(j, i) Z[(size_t)(2 * (j) + part) * K + (i)]
+#define XC(buf, r, q) xch[((size_t)(buf) * C + (r)) * (K + 1) + (q)]
+  auto norm_part = [&](int i) -> double {
+    float h = 0.f, l = 0.f;
+    for (int j = j0 + tid; j < j1; j += kOrthThreads) df_fma2(h, l, ZE(j, i), ZE(j, i));
+    const double a = bsum((double)h + (double)l);
+    __syncthreads();
+    if (lane == 0) red[warp] = a;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < nwarp; ++w) t += red[w];
+    return t;
+  };
+  auto post_dots = [&](int i, bool with_norm) {
+    const int buf = post & 1;
+    for (int q = qt; q < i; q += 128) {
+      float h = 0.f, l = 0.f;
+      for (int j = j0 + jc; j < j1; j += 4) df_fma2(h, l, ZE(j, q), ZE(j, i));
+      psum[jc * K + q] = (double)h + (double)l;
+    }
+    const double nr = with_norm ? norm_part(i) : 0.0;  // (its barriers also order psum)
+    __syncthreads();
+    for (int q = tid; q < i; q += kOrthThreads)
+      XC(buf, crank, q) = (psum[q] + psum[K + q]) + (psum[2 * K + q] + psum[3 * K + q]);
+    if (with_norm && tid == 0) XC(buf, crank, K) = nr;
+  };
+  auto gather = [&](int i, bool dots_too) -> double {
+    const int buf = post & 1;
+    if (dots_too)
+      for (int q = tid; q < i; q += kOrthThreads) {
+        double t = 0.0;
+        for (int r = 0; r < C; ++r) t += __ldcg(&XC(buf, r, q));
+        dots[q] = t;
+      }
+    if (tid == 0) {
+      double t = 0.0;
+      for (int r = 0; r < C; ++r) t += __ldcg(&XC(buf, r, K));
+      nrm_s = t;
+    }
+    __syncthreads();
+    ++post;
+    return nrm_s;
+  };
+  auto subtract = [&](int i) {
+    for (int q = tid; q < i; q += kOrthThreads) {  // the dots as double-float (psum is free here)
+      const double x = dots[q];
+      const float hq = (float)x;
+      dotf[q] = make_float2(hq, (float)(x - (double)hq));
+    }
+    __syncthreads();
+    // one thread per row: row j of Z is contiguous in q, the dots are broadcast
+    // from shared memory, and no cross-lane reduction is needed
+    for (int j = j0 + tid; j < j1; j += kOrthThreads) {
+      float h = 0.f, l = 0.f;
+      for (int q = 0; q < i; ++q) df_fma2(h, l, dotf[q], ZE(j, q));
+      const float2 z = ZE(j, i);
+      const double r = ((double)z.x + (double)z.y) - ((double)h + (double)l);
+      const float rh = (float)r;
+      ZE(j, i) = make_float2(rh, (float)(r - (double)rh));
+    }
+    __syncthreads();
+  };
+  auto post_norm = [&](int i) {
+    const double nr = norm_part(i);
+    if (tid == 0) XC(post & 1, crank, K) = nr;
+  };
+  for (int i = 0; i < K; ++i) {
+    post_dots(i, true);
+    cluster.sync();
+    const double nrm0 = gather(i, true);
+    double nrm = nrm0;
+    if (i > 0) {
+      subtract(i);
+      post_norm(i);
+      cluster.sync();
+      nrm = gather(i, false);
+      if (nrm < 0.5 * nrm0) {  // second pass
+        post_dots(i, false);
+        cluster.sync();
+        gather(i, true);
+        subtract(i);
+        post_norm(i);
+        cluster.sync();
+        nrm = gather(i, false);
+      }
+    }
+    const double inv = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+    for (int j = j0 + tid; j < j1; j += kOrthThreads) {
+      const float2 z = ZE(j, i);
+      const double r = ((double)z.x + (double)z.y) * inv;
+      const float rh = (float)r;
+      ZE(j, i) = make_float2(rh, (float)(r - (double)rh));
+    }
+    __syncthreads();
+  }
+#undef ZE
+#undef XC
+}
+
 // ---------------------------------------------------------------------------
 // 4. left vectors Q [Ub; 0] (M x K) and right vectors P Vb (N x K) of the
 //    bidiagonalised matrix, one warp per kept column.
@@ -1594,10 +1744,14 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
   TEBD_LAUNCHED(h);
   {
     const size_t smem = sizeof(double) * 5 * (size_t)(kk > 1 ? kk : 1);
-    if ((rc = check_cuda(h, cudaFuncSetAttribute(k_bd_orth, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem),
+    auto okern = b.dfp ? k_bd_orth_df : k_bd_orth;
+    if ((rc = check_cuda(h, cudaFuncSetAttribute(okern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                          "orthogonalisation shared memory")))
       return rc;
+    if (b.dfp) {
+      k_bd_z_df<<<dim3(64, nb), 256, 0, st>>>(slots_d, path_d, kk, cap, 1);
+      TEBD_LAUNCHED(h);
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(2 * kOrthCluster, nb, 1);
     cfg.blockDim = dim3(kOrthThreads, 1, 1);
@@ -1610,9 +1764,13 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if ((rc = check_cuda(h, cudaLaunchKernelEx(&cfg, k_bd_orth, slots_d, path_d, kk, cap),
+    if ((rc = check_cuda(h, cudaLaunchKernelEx(&cfg, okern, slots_d, path_d, kk, cap),
                          "orthogonalisation launch")))
       return rc;
+    if (b.dfp) {
+      TEBD_LAUNCHED(h);
+      k_bd_z_df<<<dim3(64, nb), 256, 0, st>>>(slots_d, path_d, kk, cap, 0);
+    }
   }
   TEBD_LAUNCHED(h);
   if (b.dfp) {
