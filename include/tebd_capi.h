@@ -11,6 +11,10 @@
  *   tebd_two_site_op_nc_r  TwoSiteOpNC_r  local_operations_module.f90:1723-1843
  *   tebd_trotter_step      TrotterStep / TrotterStepNC with BoundaryCond='O'
  *                          VidalCore_v_2.0/propagation_module.f90:42-114,200-252,890-1018
+ *   tebd_trotter_step_pbc  the same with BoundaryCond='P' (:116-614, 1019-1940)
+ *   tebd_swapping          Swapping / SwappingNC  local_operations_module.f90:651-689,1966-2095
+ *   tebd_set_conserv       the OPTIONAL intDegFree argument + Conserv%vi
+ *   observables, record I/O and canonical forms: see their declarations below
  *   tebd_create/destroy    AllocateGamLam + AllocateLabel + SVDInit/SVDFinish
  *                          VidalCore_v_2.0/TEBDtools_module.f90:486-521,589-620;
  *                          local_operations_module.f90:84-151
@@ -58,7 +62,7 @@ extern "C" {
 #define TEBD_MODE_DENSE 0         /* TwoSiteOp: no symmetry                            */
 #define TEBD_MODE_NC 1            /* TwoSiteOpNC: U(1) number conservation             */
 
-/* SVD algorithm (all FP64) */
+/* SVD algorithm (all FP64 but the precision form) */
 #define TEBD_SVD_FP64 0           /* default: per bond, bidiagonalisation when both
                                      dimensions of the compacted Theta are >= 64 (a wide
                                      one as Theta^H), else column-pivoted QR + one-sided
@@ -67,9 +71,11 @@ extern "C" {
 #define TEBD_SVD_BIDIAG 3         /* bidiagonalisation for every Theta (>= 2 x 2)       */
 #define TEBD_SVD_QRJ 4            /* pivoted QR + Jacobi on R^H for every bond          */
 #define TEBD_SVD_DF 5             /* precision form: as TEBD_SVD_FP64, but the bidiagonal
-                                     route's two passes over the trailing matrix and its
-                                     trailing updates run in double-float (pairs of FP32,
-                                     48-bit significands) on the FP32 pipe               */
+                                     route's passes over the trailing matrix, trailing
+                                     updates, back-transformation and Gram-Schmidt, and
+                                     the Theta formation, run in double-float (pairs of
+                                     FP32, 48-bit significands) on the FP32 pipe; number-
+                                     conserving blocks on the bidiagonal route too       */
 
 #define TEBD_OPTS_VERSION 1
 
@@ -77,8 +83,9 @@ typedef struct tebd_opts {
   int version;        /* must be TEBD_OPTS_VERSION                                     */
   int device;         /* CUDA device ordinal                                           */
   int tot_num;        /* NC mode: total particle number (reference global totNum)      */
-  int max_filling;    /* NC mode: maximum occupation (reference global maxFilling)     */
-  int svd_mode;       /* TEBD_SVD_FP64 (default), _JACOBI, _BIDIAG or _QRJ             */
+  int max_filling;    /* NC mode: maximum occupation (reference global maxFilling);
+                         d-1 unless tebd_set_conserv gives internal degrees of freedom */
+  int svd_mode;       /* TEBD_SVD_FP64 (default), _JACOBI, _BIDIAG, _QRJ or _DF        */
   int max_sweeps;     /* Jacobi sweep cap; 0 selects the default (60)                  */
   int max_batch;      /* bonds updated concurrently; 0 = all bonds of one parity       */
   int reserved;
@@ -110,7 +117,9 @@ int tebd_two_site_op(tebd_handle *h, int link, const double *op2, double *trunce
 int tebd_two_site_op_r(tebd_handle *h, int link, const double *op2, double *truncerr);
 
 /* Number-conserving bond update; replaces TwoSiteOpNC(link, Op2, Gammas, Lambdas,
- * LabelLeft, LabelRight, truncerr) without the intDegFree argument. */
+ * LabelLeft, LabelRight, truncerr[, intDegFree]) -- with intDegFree after
+ * tebd_set_conserv.  Charge blocks with both sides >= 16 take the bidiagonal
+ * route, the others the grouped Jacobi. */
 int tebd_two_site_op_nc(tebd_handle *h, int link, const double *op2, double *truncerr);
 int tebd_two_site_op_nc_r(tebd_handle *h, int link, const double *op2, double *truncerr);
 
