@@ -240,10 +240,13 @@ constexpr int kNcBidiagMinDim = 16;  // smaller block side from which a block is
 constexpr int kMaxPairs = 16;  // allowed (i, j) pairs of one pair total, intDegFree form
 static_assert(kMaxDnc <= 8, "NcLocal and the handle's table hold 8 local numbers");
 
-// Precision form: A = l0 G1 l1 and B = G2 l2 of each bond as double-float
-// (float4 per complex element) in the slot's V buffer, which the block SVDs only
-// use after the Theta kernel (k_nc_prepare_svd resets it).
-__global__ void k_nc_to_df(const double2 *__restrict__ gam, const double *__restrict__ lam,
+// A = l0 G1 l1 and B = G2 l2 of each bond, once per update, so that each term of
+// the Theta kernel's class dot products is one complex multiply-add: FP64
+// (double2), or double-float (float4) in the precision form.  They live in the
+// slot's V buffer, which the block SVDs only use after the Theta kernel
+// (k_nc_prepare_svd resets it).
+template <bool kDF>
+__global__ void k_nc_scale(const double2 *__restrict__ gam, const double *__restrict__ lam,
                            const int *links, Slot *slots, int chi, int d) {
   const int s = blockIdx.y;
   const int link = links[s];
@@ -253,20 +256,26 @@ __global__ void k_nc_to_df(const double2 *__restrict__ gam, const double *__rest
   const double *l0 = lam + (size_t)(link - 1) * chi;
   const double *l1 = lam + (size_t)link * chi;
   const double *l2 = lam + (size_t)(link + 1) * chi;
-  float4 *A = reinterpret_cast<float4 *>(slots[s].V), *B = A + csz;
+  float4 *A = reinterpret_cast<float4 *>(slots[s].V), *B = A + csz;  // double-float form
+  double2 *Ad = slots[s].V, *Bd = Ad + csz;                           // FP64 form
   const size_t cd = (size_t)chi * d;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < csz; e += (size_t)gridDim.x * blockDim.x) {
     const int a = (int)(e % chi), b = (int)(e / cd);  // A: (a, i, b); B: (b, j, g) with g = e / (chi d)
     const double wa = l0[a] * l1[b];
     const double2 x = G1[e], y = G2[e];
-    A[e] = dfs(make_double2(wa * x.x, wa * x.y));
     const double wb = l2[b];
-    B[e] = dfs(make_double2(wb * y.x, wb * y.y));
+    if (kDF) {
+      A[e] = dfs(make_double2(wa * x.x, wa * x.y));
+      B[e] = dfs(make_double2(wb * y.x, wb * y.y));
+    } else {
+      Ad[e] = make_double2(wa * x.x, wa * x.y);
+      Bd[e] = make_double2(wb * y.x, wb * y.y);
+    }
   }
 }
 
 // kDF (precision form): the class dot products read A = l0 G1 l1 and B = G2 l2,
-// prepared as double-float in the slot's V buffer by k_nc_to_df, and accumulate
+// prepared as double-float in the slot's V buffer by k_nc_scale, and accumulate
 // in double-float on the FP32 pipe; the gate mix and the norm stay FP64.
 template <bool kIdf, bool kDF>
 __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ gam,
@@ -294,6 +303,7 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
   const int mnl = S.hdr[H_MINNL];
   const float4 *Adf = reinterpret_cast<const float4 *>(slots[s].V);  // kDF: l0 G1 l1
   const float4 *Bdf = Adf + csz;                                      // kDF: G2 l2
+  const double2 *Apre = slots[s].V, *Bpre = Apre + csz;               // FP64: l0 G1 l1, G2 l2
   // Theta(a, i, jj, g) = sum over the betas of class q with LabelRight(link+1) =
   // rgtN + r of l0 G1(a,i,b) l1 G2(b,jj,g) l2
   auto cdot = [&](int q, int i, int jj, int r, int a, int g, int rgtN) -> double2 {
@@ -313,11 +323,10 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
       const int b = S.cls_beta[p];
       const int rgtN2 = lr1[b];
       if (rgtN2 >= 1000 || rgtN2 - rgtN != r) continue;
-      const double2 x = G1[a + (size_t)chi * i + (size_t)chi * d * b];
-      const double2 y = G2[b + (size_t)chi * jj + (size_t)chi * d * g];
-      const double w = l0[a] * l1[b] * l2[g];
-      sacc.x += w * (x.x * y.x - x.y * y.y);
-      sacc.y += w * (x.x * y.y + x.y * y.x);
+      const double2 x = Apre[a + (size_t)chi * i + (size_t)chi * d * b];
+      const double2 y = Bpre[b + (size_t)chi * jj + (size_t)chi * d * g];
+      sacc.x = fma(x.x, y.x, fma(-x.y, y.y, sacc.x));
+      sacc.y = fma(x.x, y.y, fma(x.y, y.x, sacc.y));
     }
     return sacc;
   };
@@ -940,11 +949,16 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
   k_nc_blocks<<<nb, 32, 0, st>>>(h->lab_l, h->lab_r, h->links_d, h->slots_d, w->slots_d, w->probs_d,
                                  chi, d, N, mf, bmax, nl);
   TEBD_LAUNCHED(h);
-  const bool df = h->opts.svd_mode == TEBD_SVD_DF && d >= 2;  // A and B fill 2/d of V
-  if (df) {
-    k_nc_to_df<<<dim3(64, nb), 256, 0, st>>>(h->gam, h->lam, h->links_d, h->slots_d, chi, d);
-    TEBD_LAUNCHED(h);
-  }
+  // A = l0 G1 l1 and B = G2 l2 of each bond, once per update, in the slot's V
+  // buffer (they fill 2/d of it; d >= 2 in NC mode): FP64, or double-float in the
+  // precision form
+  if (d < 2) return set_error(h, TEBD_ERR_ARG, "NC mode needs d >= 2");
+  const bool df = h->opts.svd_mode == TEBD_SVD_DF;
+  if (df)
+    k_nc_scale<true><<<dim3(64, nb), 256, 0, st>>>(h->gam, h->lam, h->links_d, h->slots_d, chi, d);
+  else
+    k_nc_scale<false><<<dim3(64, nb), 256, 0, st>>>(h->gam, h->lam, h->links_d, h->slots_d, chi, d);
+  TEBD_LAUNCHED(h);
   {
     auto kern = h->nc_idf ? (df ? k_nc_theta<true, true> : k_nc_theta<true, false>)
                           : (df ? k_nc_theta<false, true> : k_nc_theta<false, false>);
