@@ -72,3 +72,27 @@ def test_fortran_binding_mentions_every_entry_point():
     doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     assert mod in doc
     assert max(len(line) for line in f90.splitlines()) <= 132  # free-form line limit
+
+
+def test_header_is_plain_c(tmp_path):
+    """tebd_capi.h compiles as C99 (the language a Fortran or C host binds to):
+    a translation unit that takes the address of every entry point."""
+    import re
+    import shutil
+    import subprocess
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    hdr = open(os.path.join(ROOT, "include", "tebd_capi.h")).read()
+    names = sorted(set(re.findall(r"\b(tebd_[a-z0-9_]+)\s*\(", re.sub(r"/\*.*?\*/", "", hdr, flags=re.S))))
+    src = tmp_path / "use_capi.c"
+    src.write_text('#include "tebd_capi.h"\n#include <stddef.h>\n'
+                   "typedef void (*entry_fn)(void);\n"
+                   "const entry_fn entry_points[] = {\n"
+                   + ",\n".join("  (entry_fn)&%s" % n for n in names) + "\n};\n"
+                   "size_t n_entry_points = sizeof(entry_points) / sizeof(entry_points[0]);\n")
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-c", str(src),
+                        "-I", os.path.join(ROOT, "include"), "-o", str(tmp_path / "use_capi.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
