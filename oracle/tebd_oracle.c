@@ -769,6 +769,11 @@ static int nc_core(int chi, int d, int totNum, int maxFilling, double *g1_, doub
     free(theta);
     return st;
   }
+  if (B.nb < 1) { /* build_blocks returns an error first; kept explicit for the allocations */
+    nc_free(&B);
+    free(theta);
+    return OR_ERR_ARG;
+  }
   /* per-block SVD (FormBlockTheta :1445-1468, SVDNC :1470-1492) */
   int sz = 0;
   for (int k = 0; k < B.nb; ++k) sz += B.rows[k] < B.cols[k] ? B.rows[k] : B.cols[k];
