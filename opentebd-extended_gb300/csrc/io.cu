@@ -150,7 +150,8 @@ int write_all(tebd_handle *h, FILE *f, const std::string &s, const char *path) {
 int read_lambdas(tebd_handle *h, const char *path, char kind, int chi_now, std::vector<double> &lam) {
   FILE *f = fopen(path, "r");
   if (!f) return set_error(h, TEBD_ERR_ARG, std::string("cannot open ") + path);
-  Reader r{f};
+  Reader r;
+  r.f = f;
   const int w = width(kind);
   for (int link = 0; link < h->L + 1; ++link) {
     if (!r.next() || (int)r.line.size() < w * chi_now) {
@@ -170,7 +171,8 @@ int read_lambdas(tebd_handle *h, const char *path, char kind, int chi_now, std::
 int read_gammas(tebd_handle *h, const char *path, char kind, int chi_now, std::vector<double> &gam) {
   FILE *f = fopen(path, "r");
   if (!f) return set_error(h, TEBD_ERR_ARG, std::string("cannot open ") + path);
-  Reader r{f};
+  Reader r;
+  r.f = f;
   const int w = width(kind), d = h->d, chi = h->chi;
   const size_t csz = (size_t)chi * d * chi;
   for (int part = 0; part < 2; ++part)  // real parts, then imaginary parts
@@ -197,7 +199,8 @@ int read_gammas(tebd_handle *h, const char *path, char kind, int chi_now, std::v
 int read_labels(tebd_handle *h, const char *path, int chi_now, std::vector<int> &lab) {
   FILE *f = fopen(path, "r");
   if (!f) return set_error(h, TEBD_ERR_ARG, std::string("cannot open ") + path);
-  Reader r{f};
+  Reader r;
+  r.f = f;
   for (int link = 0; link < h->L + 1; ++link) {
     if (!r.next() || (int)r.line.size() < 16 * chi_now) {
       fclose(f);

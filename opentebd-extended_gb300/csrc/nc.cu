@@ -290,11 +290,6 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
   const int nb = S.hdr[H_NB];
   const int link = links[s];
   const size_t csz = (size_t)chi * d * chi;
-  const double2 *G1 = gam + (size_t)(link - 1) * csz;
-  const double2 *G2 = gam + (size_t)link * csz;
-  const double *l0 = lam + (size_t)(link - 1) * chi;
-  const double *l1 = lam + (size_t)link * chi;
-  const double *l2 = lam + (size_t)(link + 1) * chi;
   const int *ll0 = lab_l + (size_t)(link - 1) * chi;
   const int *lr1 = lab_r + (size_t)link * chi;
   const int *lr2 = lab_r + (size_t)(link + 1) * chi;
@@ -307,7 +302,7 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
   // Theta(a, i, jj, g) = sum over the betas of class q with LabelRight(link+1) =
   // rgtN + r of l0 G1(a,i,b) l1 G2(b,jj,g) l2
   auto cdot = [&](int q, int i, int jj, int r, int a, int g, int rgtN) -> double2 {
-    if (kDF) {
+    if constexpr (kDF) {
       float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
       for (int p = S.cls_off[q]; p < S.cls_off[q + 1]; ++p) {
         const int b = S.cls_beta[p];
@@ -317,18 +312,19 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
                 Bdf[b + (size_t)chi * jj + (size_t)chi * d * g]);
       }
       return make_double2((double)rh + (double)rl, (double)ih + (double)il);
+    } else {
+      double2 sacc = make_double2(0.0, 0.0);
+      for (int p = S.cls_off[q]; p < S.cls_off[q + 1]; ++p) {
+        const int b = S.cls_beta[p];
+        const int rgtN2 = lr1[b];
+        if (rgtN2 >= 1000 || rgtN2 - rgtN != r) continue;
+        const double2 x = Apre[a + (size_t)chi * i + (size_t)chi * d * b];
+        const double2 y = Bpre[b + (size_t)chi * jj + (size_t)chi * d * g];
+        sacc.x = fma(x.x, y.x, fma(-x.y, y.y, sacc.x));
+        sacc.y = fma(x.x, y.y, fma(x.y, y.x, sacc.y));
+      }
+      return sacc;
     }
-    double2 sacc = make_double2(0.0, 0.0);
-    for (int p = S.cls_off[q]; p < S.cls_off[q + 1]; ++p) {
-      const int b = S.cls_beta[p];
-      const int rgtN2 = lr1[b];
-      if (rgtN2 >= 1000 || rgtN2 - rgtN != r) continue;
-      const double2 x = Apre[a + (size_t)chi * i + (size_t)chi * d * b];
-      const double2 y = Bpre[b + (size_t)chi * jj + (size_t)chi * d * g];
-      sacc.x = fma(x.x, y.x, fma(-x.y, y.y, sacc.x));
-      sacc.y = fma(x.x, y.y, fma(x.y, y.x, sacc.y));
-    }
-    return sacc;
   };
   const size_t total = (size_t)chi * chi;
   const size_t chunk = (total + kNormParts - 1) / kNormParts;
@@ -339,7 +335,7 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
     const int lftN = ll0[a], rgtN = lr2[g];
     if (max(lftN, rgtN) >= 1000) continue;
     const int ntot = totNum - lftN - rgtN;
-    if (kIdf) {
+    if constexpr (kIdf) {
       // intDegFree form.  Pairs (i, l) with 0 <= ntot - n_i <= maxFilling and
       // n_l = ntot - n_i, i outer and l inner: the entries ThetaOperationNC reads
       // and writes (:970-1010) and RenormThetaNC sums (:1062-1102).
@@ -381,43 +377,43 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
         else
           Xk[cpn + (size_t)n * rp] = make_double2(v.x, -v.y);
       }
-      continue;
-    }
-    // FormThetaNC restricted to the entries ThetaOperationNC reads: (i, ll = ntot - i)
-    double2 th[kMaxDnc];
-    for (int i = 0; i < d; ++i) {
-      th[i] = make_double2(0.0, 0.0);
-      const int li = ntot - i;  // 0-based second physical index
-      if (li < 0 || li > maxFilling) continue;
-      const int q = lftN + i;  // LabelLeft(link+1) of the contributing betas
-      if (q < 0 || q > totNum) continue;
-      th[i] = cdot(q, i, li, li, a, g, rgtN);  // j = rgtN2 - rgtN1 + 1
-    }
-    // ThetaOperationNC: Theta'(a,k,jj,g) = sum_i Op2((k)d+jj, (i)d+ll) Theta(a,i,ll,g)
-    for (int k = 0; k < d; ++k) {
-      const int jj = ntot - k;
-      if (jj < 0 || jj > maxFilling) continue;
-      double2 o = make_double2(0.0, 0.0);
+    } else {
+      // FormThetaNC restricted to the entries ThetaOperationNC reads: (i, ll = ntot - i)
+      double2 th[kMaxDnc];
       for (int i = 0; i < d; ++i) {
-        const int li = ntot - i;
+        th[i] = make_double2(0.0, 0.0);
+        const int li = ntot - i;  // 0-based second physical index
         if (li < 0 || li > maxFilling) continue;
-        const double2 gv = op[(size_t)(k * d + jj) + (size_t)d2 * (i * d + li)];
-        o.x += gv.x * th[i].x - gv.y * th[i].y;
-        o.y += gv.x * th[i].y + gv.y * th[i].x;
+        const int q = lftN + i;  // LabelLeft(link+1) of the contributing betas
+        if (q < 0 || q > totNum) continue;
+        th[i] = cdot(q, i, li, li, a, g, rgtN);  // j = rgtN2 - rgtN1 + 1
       }
-      acc += o.x * o.x + o.y * o.y;  // RenormThetaNC sums every allowed entry
-      // FormBlockTheta: row (a,k) of block NL = lftN + k, column (g,jj)
-      const int NL = lftN + k;
-      const int rp = S.rowpos[a * d + k], cpn = S.colpos[g * d + jj];
-      if (nb == 0 || rp < 0 || cpn < 0) continue;
-      const int blk = NL - mnl;
-      const int m = S.rows[blk], n = S.cols[blk];
-      double2 *Xk = slots[s].X + S.boffx[blk];
-      if (m >= n)
-        Xk[rp + (size_t)m * cpn] = o;
-      else
-        Xk[cpn + (size_t)n * rp] = make_double2(o.x, -o.y);
-    }
+      // ThetaOperationNC: Theta'(a,k,jj,g) = sum_i Op2((k)d+jj, (i)d+ll) Theta(a,i,ll,g)
+      for (int k = 0; k < d; ++k) {
+        const int jj = ntot - k;
+        if (jj < 0 || jj > maxFilling) continue;
+        double2 o = make_double2(0.0, 0.0);
+        for (int i = 0; i < d; ++i) {
+          const int li = ntot - i;
+          if (li < 0 || li > maxFilling) continue;
+          const double2 gv = op[(size_t)(k * d + jj) + (size_t)d2 * (i * d + li)];
+          o.x += gv.x * th[i].x - gv.y * th[i].y;
+          o.y += gv.x * th[i].y + gv.y * th[i].x;
+        }
+        acc += o.x * o.x + o.y * o.y;  // RenormThetaNC sums every allowed entry
+        // FormBlockTheta: row (a,k) of block NL = lftN + k, column (g,jj)
+        const int NL = lftN + k;
+        const int rp = S.rowpos[a * d + k], cpn = S.colpos[g * d + jj];
+        if (nb == 0 || rp < 0 || cpn < 0) continue;
+        const int blk = NL - mnl;
+        const int m = S.rows[blk], n = S.cols[blk];
+        double2 *Xk = slots[s].X + S.boffx[blk];
+        if (m >= n)
+          Xk[rp + (size_t)m * cpn] = o;
+        else
+          Xk[cpn + (size_t)n * rp] = make_double2(o.x, -o.y);
+      }
+    }  // plain form
   }
   red[threadIdx.x] = acc;
   __syncthreads();

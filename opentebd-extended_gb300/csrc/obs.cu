@@ -353,7 +353,8 @@ extern "C" int tebd_two_site_rho(tebd_handle *h, int link, double *rho2) {
   int rc;
   if ((rc = obs_begin(h))) return rc;
   std::vector<double2> out;
-  if ((rc = obs_rho2(h, std::vector<int>{link}, out))) return rc;
+  const std::vector<int> one_link{link};
+  if ((rc = obs_rho2(h, one_link, out))) return rc;
   memcpy(rho2, out.data(), sizeof(double2) * out.size());
   return TEBD_OK;
 }
