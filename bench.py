@@ -145,6 +145,24 @@ def cpu_sample(gam, lam, Udt, links, workers):
 # a gloo group serves only the barrier and the max over ranks of the timed
 # region -- there is no data-path collective
 # ---------------------------------------------------------------------------
+def hbm_roofline(traffic_bytes, avg_launch_ms, peaks_path):
+    """The dominant kernel on the HBM roofline: its measured DRAM traffic per
+    launch over its average launch time, against the measured copy bandwidth of
+    this machine's GPUs (None when a figure is missing).  k_gebrd is bound by the FP64
+    pipe, so this fraction is far below one; it shows how far from memory-bound
+    the kernel is."""
+    if not traffic_bytes or not avg_launch_ms or not os.path.exists(peaks_path):
+        return None
+    try:
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+    except (ValueError, KeyError, TypeError):
+        return None
+    achieved = traffic_bytes / (avg_launch_ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)",
+            "kernel": "k_gebrd"}
+
+
 def replica_env():
     """(rank, world size, local rank) from torchrun's environment; one process without it."""
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
@@ -430,6 +448,8 @@ def run_ours(args):
                                               "tebd_get_gamma/lambda, host wall clock"},
         "gpu_launches": launches,
         "roofline": roof,
+        "roofline_hbm": hbm_roofline(roof["traffic"], roof["avg_launch_ms"],
+                                     os.path.join(ROOT, "MEASURED_PEAKS.json")),
         "cpu_baseline": cpu,
         "precision_form": prec,
         **({"rank_form": {"what": "kept-rank form: per-update discarded-weight bound "

@@ -64,3 +64,17 @@ def test_one_process_needs_no_group():
     assert bench.replica_group(1) is None
     assert bench.replica_max(None, 3.5) == 3.5
     assert bench.whole_job_rate(1, 95, 1000.0) == 95.0
+
+
+def test_hbm_roofline_view(tmp_path):
+    import json
+
+    import bench
+
+    peaks = tmp_path / "peaks.json"
+    peaks.write_text(json.dumps({"hbm_gbs": 6800.0}))
+    r = bench.hbm_roofline(5.0e10, 125.0, str(peaks))  # 50 GB in 125 ms -> 400 GB/s
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s"
+    assert abs(r["achieved"] - 400.0) < 1e-9 and abs(r["frac"] - 400.0 / 6800.0) < 1e-12
+    assert bench.hbm_roofline(None, 125.0, str(peaks)) is None
+    assert bench.hbm_roofline(5.0e10, 125.0, str(tmp_path / "missing.json")) is None
