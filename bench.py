@@ -402,23 +402,20 @@ def run_ours(args):
                          % (len(links), ",".join(map(str, links)), wall)}
 
     # ---- roofline of the dominant kernel: the bidiagonalisation, FP64 pipe ----
-    prof = {}
-    pth = os.path.join(ROOT, "profiles", "k_gebrd_traffic.json")
-    if os.path.exists(pth):
-        prof = json.load(open(pth))
     nl = max(1, st["gebrd_launches"])
     flops_launch = st["gebrd_flops"] / nl
     achieved = st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12 if st["gebrd_ms"] > 0 else None
     roof = {
         "kernel": "k_gebrd", "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
         "frac": (achieved / fp64_peak) if achieved else None,
-        "traffic": prof["dram_bytes_per_flop"] * flops_launch if prof else None,
+        "traffic": None,
         "peak_source": "measured FP64 FMA throughput of this GPU (tebd_measure_fp64_peak); "
                        "MEASURED_PEAKS.json carries no FP64 figure",
         "algorithmic": "16 M N^2 - 16 N^3/3 real flops per bond (complex Householder bidiagonalisation, M >= N)",
         "flops_per_launch": flops_launch, "launches": st["gebrd_launches"],
         "avg_launch_ms": st["gebrd_ms"] / nl, "share_of_timed": st["gebrd_ms"] / ms if ms > 0 else None,
-        "traffic_source": prof.get("source"),
+        "traffic_source": "not measured for this window: DRAM traffic comes only from an ncu capture, "
+                          "never from a run that is timed",
         "bidiag_route_share_of_timed": st["bidiag_ms"] / ms if ms > 0 else None,
         "qrj": {"kernel": "k_jacobi_persistent<double>",
                 "achieved": st["jacobi_flops"] / (st["jacobi_ms"] / 1e3) / 1e12 if st["jacobi_ms"] > 0 else None,

@@ -55,6 +55,11 @@ extern "C" {
 #define TEBD_ERR_OOM 3            /* device or host allocation failed                 */
 #define TEBD_ERR_SVD_NOCONV 4     /* Jacobi SVD hit its sweep cap before converging   */
 #define TEBD_ERR_NONFINITE 5      /* NaN/Inf met in Theta or in the singular values   */
+/* On TEBD_ERR_SVD_NOCONV and TEBD_ERR_NONFINITE the bonds of the batch that met
+ * the failure keep their Gammas, Lambdas and labels (nothing of that batch is
+ * written); batches completed earlier in the same call (the previous sweeps of a
+ * Trotter step) stay applied.  The reference ignores ZGESVD's info
+ * (local_operations_module.f90:335-336). */
 #define TEBD_ERR_STATE 6          /* call not valid in this handle's mode             */
 #define TEBD_ERR_NC_BLOCKS 7      /* a charge label fell outside the block range      */
 
@@ -291,21 +296,32 @@ int tebd_read_gamma_lambda_labels(tebd_handle *h, const char *lambda_path, const
                                   int chi_now);
 
 /* Allocation-free dense update of bond `link` of a chain the caller already
- * holds in device memory.  No counterpart in the reference: it exists for
- * callers that must not allocate (a region under CUDA-graph capture, a device
- * memory pool that may not grow after start-up, a host that keeps its own
- * device-resident chain and no handle).  It calls no cudaMalloc/cudaFree and no
- * allocating library routine; every temporary lives in one static device array
- * of about 2.1 MB that each GPU loading this library holds until exit.
+ * holds in device memory.  No counterpart in the reference.  It exists for
+ * callers that cannot allocate device memory when they run the update: a host
+ * whose device memory comes from a fixed pool sized at start-up (a further
+ * cudaMalloc fails or breaks the pool's budget), a host that keeps its own
+ * device-resident chain and cannot own a handle (tebd_create allocates SVD
+ * workspaces for a whole sweep), and time-critical loops that keep cudaMalloc
+ * and cudaFree (which synchronises the device) out of their steady state.
+ * It calls no cudaMalloc/cudaFree and no allocating library routine; every
+ * temporary lives in one static device array of about 2.1 MB that each GPU
+ * loading this library holds until exit.
  *   gammas   device, L Gammas back to back, each chi x d x chi complex (Fortran order)
  *   lambdas  device, L+1 Lambdas back to back, each chi doubles
  *   op2      device, complex (d^2 x d^2) gate, layout as for tebd_two_site_op
  *   truncerr host, receives the truncation error
- *   stream   cudaStream_t to run on (NULL: the legacy default stream)
- * Limit: d*chi <= 256 (and chi <= 256); larger sizes return TEBD_ERR_ARG.
+ *   stream   cudaStream_t to run on (NULL: the legacy default stream); the call
+ *            synchronises this stream before it returns
+ * Limit: d*chi <= 256 (and chi <= 256, d <= 8); larger sizes return TEBD_ERR_ARG.
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make it before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race and must be serialised. */
+ * (cudaGetSymbolAddress) and keeps it for the life of the process: make that
+ * first call before any stream capture begins, and do not call this entry point
+ * on a device after cudaDeviceReset.  All calls share the array and it keeps the
+ * last call's contents (what must start at zero is cleared by each call): calls
+ * that overlap on the GPU race and must be serialised.
+ * A CUDA error already pending on the calling thread is left in place and the
+ * call returns TEBD_ERR_CUDA without running.  On TEBD_ERR_SVD_NOCONV and
+ * TEBD_ERR_NONFINITE the caller's Gammas and Lambdas are left unmodified. */
 int tebd_two_site_op_noalloc(int L, int d, int chi, int link, double *gammas, double *lambdas,
                              const double *op2, double *truncerr, void *stream);
 

@@ -1,5 +1,5 @@
 ! tebd_cuda_iface.f90 -- ISO_C_BINDING interfaces of include/tebd_capi.h for a
-! Fortran host of OpenTEBD-extended (the module INTEGRATION.md documents).
+! Fortran host of OpenTEBD-extended.
 ! Gammas, Lambdas and labels are passed as C_LOC of the host's own arrays: the
 ! layouts are the reference's, so nothing is transposed or copied on the host.
 MODULE tebd_cuda_iface

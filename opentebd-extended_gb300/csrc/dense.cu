@@ -246,36 +246,62 @@ __global__ void __launch_bounds__(256) k_theta_form_df(const double2 *__restrict
 // is multiplied by Op2 (row (i-1)d+j, column (k-1)d+l).  In place.
 // ---------------------------------------------------------------------------
 constexpr int kMaxD = 8;
+constexpr int kGatePairs = 32;  // (alpha, beta) vectors staged per block
 
+// Dynamic shared memory of k_gate_apply: the d^4 gate and kGatePairs d^2-vectors
+// (98 304 B at d = 8, above the 48 KB default: set_gate_smem opts in).
+inline size_t gate_smem_bytes(int d) {
+  return sizeof(double2) * ((size_t)d * d * d * d + (size_t)kGatePairs * d * d);
+}
+
+// One block updates kGatePairs kept (alpha, beta) pairs: their d^2-vectors are
+// read into shared memory (consecutive threads take consecutive alpha, so the
+// reads are coalesced), the block synchronises, and every output element
+// (pair, row) is a d^2-term dot product with one gate row.  Pairs of different
+// blocks are disjoint, so the update is in place.
 __global__ void __launch_bounds__(128) k_gate_apply(Slot *slots, int chi, int d) {
-  extern __shared__ double2 gsm[];  // d^4
+  extern __shared__ double2 gsm[];  // d^4 gate | kGatePairs * d^2 vectors
   const int s = blockIdx.y;
   const Compact cp = *slots[s].cp;
+  const int npairs = cp.r0 * cp.r2;
+  const int p0 = blockIdx.x * kGatePairs;
+  if (p0 >= npairs) return;  // uniform over the block
   const int d2 = d * d;
   const double2 *G = slots[s].gate;
-  for (int e = threadIdx.x; e < d2 * d2; e += blockDim.x) gsm[e] = G[e];
-  __syncthreads();
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= cp.r0 * cp.r2) return;
-  const int a = t % cp.r0, b = t / cp.r0;
+  double2 *vsm = gsm + d2 * d2;
   const int m = cp.m, r0 = cp.r0, r2 = cp.r2;
+  const int np = min(kGatePairs, npairs - p0);
   double2 *X = slots[s].X;
-  double2 v[kMaxD * kMaxD];
-  for (int k = 0; k < d; ++k)
-    for (int l = 0; l < d; ++l) v[k * d + l] = X[(size_t)(k * r0 + a) + (size_t)m * (l * r2 + b)];
-  for (int i = 0; i < d; ++i)
-    for (int j = 0; j < d; ++j) {
-      const int row = i * d + j;
-      double2 acc = make_double2(0.0, 0.0);
-      for (int kl = 0; kl < d2; ++kl) {
-        const double2 g = gsm[row + d2 * kl];
-        acc.x = fma(g.x, v[kl].x, acc.x);
-        acc.x = fma(-g.y, v[kl].y, acc.x);
-        acc.y = fma(g.x, v[kl].y, acc.y);
-        acc.y = fma(g.y, v[kl].x, acc.y);
-      }
-      X[(size_t)(i * r0 + a) + (size_t)m * (j * r2 + b)] = acc;
+  for (int e = threadIdx.x; e < d2 * d2; e += blockDim.x) gsm[e] = G[e];
+  for (int e = threadIdx.x; e < kGatePairs * d2; e += blockDim.x) {
+    const int p = e % kGatePairs, kl = e / kGatePairs;
+    if (p >= np) continue;
+    const int t = p0 + p, a = t % r0, b = t / r0, k = kl / d, l = kl % d;
+    vsm[e] = X[(size_t)(k * r0 + a) + (size_t)m * (l * r2 + b)];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < kGatePairs * d2; e += blockDim.x) {
+    const int p = e % kGatePairs, row = e / kGatePairs;
+    if (p >= np) continue;
+    const int t = p0 + p, a = t % r0, b = t / r0, i = row / d, j = row % d;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int kl = 0; kl < d2; ++kl) {
+      const double2 g = gsm[row + d2 * kl];
+      const double2 v = vsm[kl * kGatePairs + p];
+      acc.x = fma(g.x, v.x, acc.x);
+      acc.x = fma(-g.y, v.y, acc.x);
+      acc.y = fma(g.x, v.y, acc.y);
+      acc.y = fma(g.y, v.x, acc.y);
     }
+    X[(size_t)(i * r0 + a) + (size_t)m * (j * r2 + b)] = acc;
+  }
+}
+
+// Opt k_gate_apply into the shared memory it needs on the current device (a
+// per-function attribute; cheap, made before every launch).
+static cudaError_t set_gate_smem(int d) {
+  return cudaFuncSetAttribute(k_gate_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)gate_smem_bytes(d));
 }
 
 // ---------------------------------------------------------------------------
@@ -378,9 +404,9 @@ __global__ void __launch_bounds__(1024) k_sigma_sort(Slot *slots, const double *
 // within rank_bound; the rest of Lambda1 is set to exactly zero, so that the
 // neighbouring updates compact those Schmidt indices away.
 __global__ void k_lambda(Slot *slots, const int *links, double *lam, double *truncerr, int chi,
-                         int nb, double rank_bound) {
+                         int nb, double rank_bound, const int *status) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nb) return;
+  if (s >= nb || (status[0] & 1)) return;  // non-finite batch: the chain is left as it was
   const double *S = slots[s].S;
   int keep = chi;
   if (rank_bound > 0.0) {
@@ -423,7 +449,8 @@ __global__ void k_store_spectrum(Slot *slots, const int *links, const int *sweep
 // with U(:,beta) = X(:,perm(beta)) / sigma(perm(beta)); zero where the guard fails,
 // where alpha was compacted away, and for columns beyond the rank.
 __global__ void k_restore_gamma1(double2 *gam, const double *lam, const int *links, Slot *slots,
-                                 const double *nrm, int chi, int d) {
+                                 const double *nrm, int chi, int d, const int *status) {
+  if (status[0] & 1) return;  // non-finite batch: the chain is left as it was
   const int s = blockIdx.y;
   const int nf = chi * d;
   const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -451,7 +478,8 @@ __global__ void k_restore_gamma1(double2 *gam, const double *lam, const int *lin
 // VT = V^H, i.e. conj(V(i*r2 + b', perm(alpha))).  32x32 tile transpose through smem.
 __global__ void __launch_bounds__(256) k_restore_gamma2(double2 *gam, const double *lam,
                                                         const int *links, Slot *slots, int chi,
-                                                        int d) {
+                                                        int d, const int *status) {
+  if (status[0] & 1) return;  // non-finite batch: the chain is left as it was
   __shared__ double2 tile[32][33];
   const int s = blockIdx.z;
   const int nf = chi * d;
@@ -505,8 +533,10 @@ int launch_dense_prepare(tebd_handle *h, int nb, bool /*real_gate: converted on 
     k_theta_form<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
                                                                          h->slots_d, chi, d);
   TEBD_LAUNCHED(h);
-  const size_t gsm = sizeof(double2) * (size_t)d * d * d * d;
-  k_gate_apply<<<dim3(cdiv((size_t)chi * chi, 128), nb), 128, gsm, st>>>(h->slots_d, chi, d);
+  int rc = check_cuda(h, set_gate_smem(d), "gate shared memory");
+  if (rc) return rc;
+  k_gate_apply<<<dim3(cdiv((size_t)chi * chi, kGatePairs), nb), 128, gate_smem_bytes(d), st>>>(
+      h->slots_d, chi, d);
   TEBD_LAUNCHED(h);
   k_norm_partial<<<dim3(kNormParts, nb), 256, 0, st>>>(h->slots_d, h->nrm_part);
   TEBD_LAUNCHED(h);
@@ -544,16 +574,17 @@ int launch_dense_finish(tebd_handle *h, int nb) {
   k_sigma_sort<<<nb, 1024, sizeof(double) * n, st>>>(h->slots_d, h->nrm, n, h->status_d);
   TEBD_LAUNCHED(h);
   k_lambda<<<cdiv(nb, 64), 64, 0, st>>>(h->slots_d, h->links_d, h->lam, h->truncerr_d, chi, nb,
-                                        h->unnormalized ? 0.0 : h->rank_bound);
+                                        h->unnormalized ? 0.0 : h->rank_bound, h->status_d);
   TEBD_LAUNCHED(h);
   k_store_spectrum<<<nb, 256, 0, st>>>(h->slots_d, h->links_d, h->js.sweeps, h->sig_link_d,
                                        h->sig_count_d, h->sweeps_link_d, n, h->path_d);
   TEBD_LAUNCHED(h);
   k_restore_gamma1<<<dim3(cdiv((size_t)n * chi, 256), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
-                                                                       h->slots_d, h->nrm, chi, d);
+                                                                       h->slots_d, h->nrm, chi, d,
+                                                                       h->status_d);
   TEBD_LAUNCHED(h);
   k_restore_gamma2<<<dim3(cdiv(chi, 32), cdiv(n, 32), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
-                                                                        h->slots_d, chi, d);
+                                                                        h->slots_d, chi, d, h->status_d);
   TEBD_LAUNCHED(h);
   return check_cuda(h, cudaGetLastError(), "dense finish launch");
 }
@@ -589,33 +620,37 @@ namespace tebd {
 // Handle-free launch sequences for one bond (slot 0), used by the
 // allocation-free entry point in noalloc.cu.  Same kernels, same order as
 // launch_dense_prepare / launch_eye / launch_dense_finish.
-void raw_dense_prepare(cudaStream_t st, double2 *gam, const double *lam, const int *links_d,
-                       Slot *slots_d, JacobiProblem<double> *jp, double *nrm_part, double *nrm,
-                       int *status, int chi, int d) {
+cudaError_t raw_dense_prepare(cudaStream_t st, double2 *gam, const double *lam, const int *links_d,
+                              Slot *slots_d, JacobiProblem<double> *jp, double *nrm_part, double *nrm,
+                              int *status, int chi, int d) {
   const int n = chi * d;
   k_compact<<<1, 96, 0, st>>>(lam, links_d, slots_d, jp, chi, d);
   k_theta_form<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), 1), 256, 0, st>>>(gam, lam, links_d, slots_d,
                                                                       chi, d);
-  const size_t gsm = sizeof(double2) * (size_t)d * d * d * d;
-  k_gate_apply<<<dim3(cdiv((size_t)chi * chi, 128), 1), 128, gsm, st>>>(slots_d, chi, d);
+  cudaError_t e = set_gate_smem(d);
+  if (e != cudaSuccess) return e;
+  k_gate_apply<<<dim3(cdiv((size_t)chi * chi, kGatePairs), 1), 128, gate_smem_bytes(d), st>>>(
+      slots_d, chi, d);
   k_norm_partial<<<dim3(kNormParts, 1), 256, 0, st>>>(slots_d, nrm_part);
   k_norm_final<<<1, 32, 0, st>>>(nrm_part, nrm, jp, 1, status);
   const size_t total = (size_t)n * n;
   unsigned gx = cdiv(total, 256);
   if (gx > 1024) gx = 1024;
   k_eye<<<dim3(gx, 1), 256, 0, st>>>(slots_d);
+  return cudaPeekAtLastError();
 }
 
-void raw_dense_finish(cudaStream_t st, double2 *gam, double *lam, const int *links_d,
-                      Slot *slots_d, const double *nrm, double *truncerr, int *status, int chi,
-                      int d) {
+cudaError_t raw_dense_finish(cudaStream_t st, double2 *gam, double *lam, const int *links_d,
+                             Slot *slots_d, const double *nrm, double *truncerr, int *status, int chi,
+                             int d) {
   const int n = chi * d;
   k_sigma_sort<<<1, 1024, sizeof(double) * n, st>>>(slots_d, nrm, n, status);
-  k_lambda<<<1, 32, 0, st>>>(slots_d, links_d, lam, truncerr, chi, 1, 0.0);
+  k_lambda<<<1, 32, 0, st>>>(slots_d, links_d, lam, truncerr, chi, 1, 0.0, status);
   k_restore_gamma1<<<dim3(cdiv((size_t)n * chi, 256), 1), 256, 0, st>>>(gam, lam, links_d, slots_d,
-                                                                       nrm, chi, d);
+                                                                       nrm, chi, d, status);
   k_restore_gamma2<<<dim3(cdiv(chi, 32), cdiv(n, 32), 1), 256, 0, st>>>(gam, lam, links_d, slots_d,
-                                                                       chi, d);
+                                                                       chi, d, status);
+  return cudaPeekAtLastError();
 }
 
 }  // namespace tebd

@@ -464,6 +464,7 @@ __global__ void __launch_bounds__(1024) k_nc_select(int *lab_l, int *lab_r, doub
                                                     double *sig_link, int *sig_count, int chi, int d,
                                                     int totNum, int bmax, int *status, double rank_bound) {
   extern __shared__ double sh[];  // colnorm[sz] | flat rank scratch
+  if (status[0] & 1) return;  // non-finite ||Theta|| in the batch: the chain is left as it was
   const int s = blockIdx.x;
   const NcSlot S = nc[s];
   const int link = links[s];
@@ -578,7 +579,8 @@ __global__ void __launch_bounds__(1024) k_nc_select(int *lab_l, int *lab_r, doub
 // ---------------------------------------------------------------------------
 // FormGamma1NC / FormGamma2NC: zero both Gammas, then scatter the kept columns.
 // ---------------------------------------------------------------------------
-__global__ void k_nc_zero_gammas(double2 *gam, const int *links, int chi, int d) {
+__global__ void k_nc_zero_gammas(double2 *gam, const int *links, int chi, int d, const int *status) {
+  if (status[0] & 1) return;  // non-finite batch: the chain is left as it was
   const int s = blockIdx.y;
   const size_t csz = (size_t)chi * d * chi;
   double2 *g = gam + (size_t)(links[s] - 1) * csz;
@@ -589,7 +591,8 @@ __global__ void k_nc_zero_gammas(double2 *gam, const int *links, int chi, int d)
 
 __global__ void k_nc_gamma(double2 *gam, const double *lam, const int *links, NcSlot *nc,
                            const JacobiProblem<double> *probs, const double *nrm, int chi, int d,
-                           int bmax) {
+                           int bmax, const int *status) {
+  if (status[0] & 1) return;  // non-finite batch: the chain is left as it was
   const int s = blockIdx.y;
   const int beta = blockIdx.x;
   const NcSlot S = nc[s];
@@ -1010,10 +1013,10 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
                                      h->nrm, h->truncerr_d, h->sig_link_d, h->sig_count_d, chi, d, N,
                                      bmax, h->status_d, h->unnormalized ? 0.0 : h->rank_bound);
   TEBD_LAUNCHED(h);
-  k_nc_zero_gammas<<<dim3(64, nb), 256, 0, st>>>(h->gam, h->links_d, chi, d);
+  k_nc_zero_gammas<<<dim3(64, nb), 256, 0, st>>>(h->gam, h->links_d, chi, d, h->status_d);
   TEBD_LAUNCHED(h);
   k_nc_gamma<<<dim3(chi, nb), 128, 0, st>>>(h->gam, h->lam, h->links_d, w->slots_d, w->probs_d,
-                                            h->nrm, chi, d, bmax);
+                                            h->nrm, chi, d, bmax, h->status_d);
   TEBD_LAUNCHED(h);
   return check_cuda(h, cudaGetLastError(), "NC launch");
 }

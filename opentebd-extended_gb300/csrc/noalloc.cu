@@ -1,12 +1,19 @@
 // noalloc.cu -- tebd_two_site_op_noalloc: the dense two-site update on one bond
 // of a caller-owned device chain, with no device or host allocation at all.
 //
-// Who needs it: a host that has to run the update where allocating is not
-// allowed -- inside a region being captured into a CUDA graph, in a process
-// whose device memory is handed out by a pool that must not grow after start-up,
-// or from a Fortran host that already placed its whole chain in device memory and
-// cannot own a library handle.  They pass their own device Gammas/Lambdas/gate;
-// every temporary of the update lives in the one file-scope array below.
+// Who needs it, and why they cannot allocate:
+//  * a host whose device memory is handed out by a fixed pool sized at start-up
+//    (a Fortran code that reserves its whole budget at once, or a process sharing
+//    a GPU under a hard quota): a further cudaMalloc either fails or breaks the
+//    pool's accounting;
+//  * a host that keeps its own device-resident chain and cannot own a library
+//    handle, which allocates SVD workspaces for every bond of a sweep (~1.3 GB at
+//    d = 5, chi = 128) when it is created;
+//  * a time-critical loop that overlaps other work on other streams: cudaFree
+//    synchronises the whole device and cudaMalloc can stall it, so such a loop
+//    keeps allocation out of its steady state.
+// They pass their own device Gammas/Lambdas/gate; every temporary of the update
+// lives in the one file-scope array below.
 //
 // Scratch: kNoAllocMaxN = 256 columns (d*chi <= 256, chi <= 256), about 2.1 MB,
 // held by every GPU that loads the library until the process exits.  All calls on
@@ -18,7 +25,14 @@
 // Host code cannot use `g_noalloc_scratch` as a device address (it names a host
 // shadow); the device address is fetched once per device with
 // cudaGetSymbolAddress, with that device current, on the first call made on that
-// device.  Make that first call before any stream capture begins.
+// device.  Make that first call before any stream capture begins.  The address
+// is kept for the life of the process: after cudaDeviceReset on a device, this
+// entry point must not be called again on that device.
+//
+// Errors: a CUDA error already pending on the calling thread is left in place and
+// the call returns TEBD_ERR_CUDA without touching the chain.  Launch errors are
+// checked before any kernel writes the caller's Gammas or Lambdas, and a
+// non-finite Theta or singular value leaves them unmodified (TEBD_ERR_NONFINITE).
 #include <string.h>
 
 #include <mutex>
@@ -27,12 +41,12 @@
 
 namespace tebd {
 
-void raw_dense_prepare(cudaStream_t st, double2 *gam, const double *lam, const int *links_d,
-                       Slot *slots_d, JacobiProblem<double> *jp, double *nrm_part, double *nrm,
-                       int *status, int chi, int d);
-void raw_dense_finish(cudaStream_t st, double2 *gam, double *lam, const int *links_d,
-                      Slot *slots_d, const double *nrm, double *truncerr, int *status, int chi,
-                      int d);
+cudaError_t raw_dense_prepare(cudaStream_t st, double2 *gam, const double *lam, const int *links_d,
+                              Slot *slots_d, JacobiProblem<double> *jp, double *nrm_part, double *nrm,
+                              int *status, int chi, int d);
+cudaError_t raw_dense_finish(cudaStream_t st, double2 *gam, double *lam, const int *links_d,
+                             Slot *slots_d, const double *nrm, double *truncerr, int *status, int chi,
+                             int d);
 void raw_jacobi_init(cudaStream_t st, int *rot, int *done, int *sweeps);
 void raw_jacobi_sweep(cudaStream_t st, const JacobiProblem<double> *probs_d, int *rot, int *done,
                       int *sweeps, int *pending, unsigned long long *counters, int nmax,
@@ -106,6 +120,8 @@ extern "C" int tebd_two_site_op_noalloc(int L, int d, int chi, int link, double 
       !op2 || !truncerr)
     return TEBD_ERR_ARG;
   if (d * chi > kNoAllocMaxN || chi > kNoAllocMaxChi) return TEBD_ERR_ARG;  // beyond the scratch
+  // an error left by the caller's earlier work stays theirs: report, do not clear
+  if (cudaPeekAtLastError() != cudaSuccess) return TEBD_ERR_CUDA;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(e);
@@ -150,32 +166,40 @@ extern "C" int tebd_two_site_op_noalloc(int L, int d, int chi, int link, double 
       (e = cudaMemsetAsync(status, 0, sizeof(int) * 4, st)) != cudaSuccess)
     return fail(e);
 
+  // Theta, gate, norm: reads the chain, writes only the scratch
   double2 *gam = reinterpret_cast<double2 *>(gammas);
-  raw_dense_prepare(st, gam, lambdas, link_d, slot_d, prob_d, nrm_part, nrm, status, chi, d);
+  if ((e = raw_dense_prepare(st, gam, lambdas, link_d, slot_d, prob_d, nrm_part, nrm, status, chi,
+                             d)) != cudaSuccess)
+    return fail(e);
   Compact cp;
   if ((e = cudaMemcpyAsync(&cp, slot.cp, sizeof(cp), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return fail(e);
 
+  // one-sided Jacobi on the compacted Theta, one launch sequence per sweep
   const double tol = (double)(cp.n > 16 ? cp.n : 16) * 2.220446049250313e-16;
   raw_jacobi_init(st, state, state + 1, state + 2);
   int pending = 1;
   for (int sw = 0; sw < kNoAllocSweepCap && pending; ++sw) {
     raw_jacobi_sweep(st, prob_d, state, state + 1, state + 2, state + 3, counters, cp.n, tol);
-    if ((e = cudaMemcpyAsync(&pending, state + 3, sizeof(int), cudaMemcpyDeviceToHost, st)) !=
+    if ((e = cudaPeekAtLastError()) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&pending, state + 3, sizeof(int), cudaMemcpyDeviceToHost, st)) !=
             cudaSuccess ||
         (e = cudaStreamSynchronize(st)) != cudaSuccess)
       return fail(e);
   }
-  if (pending) return TEBD_ERR_SVD_NOCONV;
+  if (pending) return TEBD_ERR_SVD_NOCONV;  // the chain has not been written
 
-  raw_dense_finish(st, gam, lambdas, link_d, slot_d, nrm, trunc_d, status, chi, d);
+  // FormLambda1, FormGamma1/2: the only kernels that write the chain; they skip
+  // their writes when the status flag marks a non-finite Theta or sigma
+  if ((e = raw_dense_finish(st, gam, lambdas, link_d, slot_d, nrm, trunc_d, status, chi, d)) !=
+      cudaSuccess)
+    return fail(e);
   int flags[4];
   if ((e = cudaMemcpyAsync(truncerr, trunc_d, sizeof(double), cudaMemcpyDeviceToHost, st)) !=
           cudaSuccess ||
       (e = cudaMemcpyAsync(flags, status, sizeof(flags), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return fail(e);
-  if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
   return (flags[0] & 1) ? TEBD_ERR_NONFINITE : TEBD_OK;
 }
