@@ -295,6 +295,18 @@ int tebd_read_gamma_lambda_labels(tebd_handle *h, const char *lambda_path, const
                                   const char *label_left_path, const char *label_right_path, char kind,
                                   int chi_now);
 
+/* The split-precision complex product on the tensor cores (no counterpart in the
+ * reference, which multiplies only inside FormTheta, local_operations_module.f90:
+ * 184-211): C_p = A_p B_p for p = 0..nprob-1, all device pointers, complex
+ * interleaved, column-major (A_p m x k at A + stride_a*p doubles... in complex
+ * units: element (i, l) at A[2*(stride_a*p + i + lda*l)]), likewise B (k x n) and
+ * C (m x n).  form 3: 3xTF32 (hi*hi + hi*lo + lo*hi, FP32 accumulation, about
+ * FP32 accuracy); form 1: one TF32 pass.  Runs on `stream` and synchronises it;
+ * allocates its operand planes for the call. */
+int tebd_zgemm_tc(int nprob, int m, int n, int k, const double *A, long long stride_a, int lda,
+                  const double *B, long long stride_b, int ldb, double *C, long long stride_c, int ldc,
+                  int form, void *stream);
+
 /* Allocation-free dense update of bond `link` of a chain the caller already
  * holds in device memory.  No counterpart in the reference.  It exists for
  * callers that cannot allocate device memory when they run the update: a host

@@ -277,5 +277,12 @@ INTERFACE
     TYPE(C_PTR), VALUE :: gammas, lambdas, op2, stream
     REAL(C_DOUBLE) :: truncerr
   END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_zgemm_tc(nprob, m, n, k, A, stride_a, lda, B, stride_b, ldb, C, stride_c, &
+      ldc, form, stream) BIND(C, NAME='tebd_zgemm_tc')
+    IMPORT :: C_INT, C_LONG_LONG, C_PTR
+    INTEGER(C_INT), VALUE :: nprob, m, n, k, lda, ldb, ldc, form
+    INTEGER(C_LONG_LONG), VALUE :: stride_a, stride_b, stride_c
+    TYPE(C_PTR), VALUE :: A, B, C, stream
+  END FUNCTION
 END INTERFACE
 END MODULE tebd_cuda_iface

@@ -69,6 +69,7 @@ EXPORTED_SYMBOLS = (
     "tebd_record_lambdas", "tebd_record_gammas", "tebd_record_labels", "tebd_read_gamma_lambda",
     "tebd_read_gamma_lambda_labels", "tebd_swapping", "tebd_trotter_step_pbc", "tebd_canonical_form_all_nc",
     "tebd_canonical_form", "tebd_canonical_form_all", "tebd_set_conserv", "tebd_set_rank_bound",
+    "tebd_zgemm_tc",
 )
 
 
@@ -164,6 +165,8 @@ def load_library(path: str = LIB_PATH):
     L.tebd_get_stream.argtypes = [vp]
     L.tebd_get_stream.restype = ctypes.c_void_p
     L.tebd_two_site_op_noalloc.argtypes = [ctypes.c_int] * 4 + [vp, vp, vp, dp, vp]
+    ll = ctypes.c_longlong
+    L.tebd_zgemm_tc.argtypes = [ctypes.c_int] * 4 + [vp, ll, ctypes.c_int] * 3 + [ctypes.c_int, vp]
     L.tebd_single_site_rho.argtypes = [vp, dp]
     L.tebd_one_site_expval.argtypes = [vp, dp, dp]
     L.tebd_one_site_expval_r.argtypes = [vp, dp, dp]
