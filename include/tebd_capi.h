@@ -301,8 +301,11 @@ int tebd_read_gamma_lambda_labels(tebd_handle *h, const char *lambda_path, const
  * interleaved, column-major (A_p m x k at A + stride_a*p doubles... in complex
  * units: element (i, l) at A[2*(stride_a*p + i + lda*l)]), likewise B (k x n) and
  * C (m x n).  form 3: 3xTF32 (hi*hi + hi*lo + lo*hi, FP32 accumulation, about
- * FP32 accuracy); form 1: one TF32 pass.  Runs on `stream` and synchronises it;
- * allocates its operand planes for the call. */
+ * FP32 accuracy); form 1: one TF32 pass; form 100 + S (S = 1..7): error-free
+ * splitting into S bf16 digit planes of 7 bits per row (the Ozaki scheme), exact
+ * FP32 accumulation of the digit products, combined in FP64 -- error about
+ * 2^(-7S) x row max x column max per term (S = 7: FP64 class).  Runs on
+ * `stream` and synchronises it; allocates its operand planes for the call. */
 int tebd_zgemm_tc(int nprob, int m, int n, int k, const double *A, long long stride_a, int lda,
                   const double *B, long long stride_b, int ldb, double *C, long long stride_c, int ldc,
                   int form, void *stream);

@@ -23,15 +23,16 @@
 #include <mutex>
 
 #include "tc_gemm.cuh"
+#include "tc_ptx.cuh"
 
 namespace tebd {
 namespace {
+using namespace tcx;
 
 constexpr int kStages = 3;
 constexpr int kThreads = 128;
 constexpr uint32_t kTileA = kTcBM * kTcBK * 4;  // bytes of one A plane tile (16 KB)
 constexpr uint32_t kTileB = kTcBN * kTcBK * 4;  // bytes of one B plane tile (16 KB)
-constexpr long long kWaitCycles = 4000000000LL;
 
 // Instruction descriptor of kind::tf32: D F32 (bits 4-5 = 1), A and B TF32
 // (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22,
@@ -43,89 +44,12 @@ size_t smem_bytes(int planes) {
   return 1024 + (size_t)kStages * planes * (kTileA + kTileB) + 256;
 }
 
-__device__ __forceinline__ uint32_t su32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(su32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Wait for the phase of parity `parity` to complete; false when the time limit
-// expires or (if abort is given) another role has aborted.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, const volatile int *abort) {
-  const long long t0 = clock64();
-  while (!mbar_try(bar, parity)) {
-    if (abort && *abort) return false;
-    if (clock64() - t0 > kWaitCycles) return false;
-  }
-  return true;
-}
-
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y,
-                                            int z) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
-      "[%2];" ::"r"(su32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(su32(bar)), "r"(x), "r"(y), "r"(z)
-      : "memory");
-}
-
-__device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor of a K-major tile written by TMA with the
-// 128-byte swizzle: start address >> 4 (bits 0-13), leading byte offset 16 B
-// (bits 16-29; unused by this layout), stride byte offset 1024 B = 8 rows of
-// 128 B (bits 32-45), descriptor version 1 (bits 46-47), swizzle mode 2 =
-// 128-byte (bits 61-63).  A K-step inside the 128-byte row advances the start
-// address by its byte offset (the tiles are 1024-byte aligned).
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-
 __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
       "l"(a), "l"(b), "r"(kIdescTF32), "r"(acc)
       : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
-               : "memory");
-}
-
-// 32 lanes x 16 consecutive 32-bit columns of TMEM into 16 registers per thread.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-      "%14, %15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -428,13 +352,66 @@ cudaError_t tc_pack_b(const double2 *src, long long pstride, int ld, int krows, 
 // ---------------------------------------------------------------------------
 using namespace tebd;
 
+static int zgemm_oz(int nprob, int m, int n, int k, const double2 *A, long long sa, int lda, const double2 *B,
+                    long long sb, int ldb, double2 *C, long long sc, int ldc, int slices, cudaStream_t st) {
+  const int m_pad = tc_pad(m, kTcBM), n_pad = tc_pad(2 * n, kOzBN), k_pad = tc_pad(2 * k, kOzBK);
+  unsigned short *da = nullptr, *db = nullptr;
+  int *ea = nullptr, *eb = nullptr, *err = nullptr;
+  int rc = TEBD_OK;
+  if (cudaMalloc(&da, sizeof(unsigned short) * slices * (size_t)nprob * m_pad * k_pad) != cudaSuccess ||
+      cudaMalloc(&db, sizeof(unsigned short) * slices * (size_t)nprob * n_pad * k_pad) != cudaSuccess ||
+      cudaMalloc(&ea, sizeof(int) * (size_t)nprob * m_pad) != cudaSuccess ||
+      cudaMalloc(&eb, sizeof(int) * (size_t)nprob * n_pad / 2) != cudaSuccess ||
+      cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
+    rc = TEBD_ERR_OOM;
+  } else {
+    OzBatch b = {};
+    b.a_dig = da;
+    b.b_dig = db;
+    b.a_exp = ea;
+    b.b_exp = eb;
+    b.nprob = nprob;
+    b.m_pad = m_pad;
+    b.n_pad = n_pad;
+    b.k_pad = k_pad;
+    b.slices = slices;
+    b.out = C;
+    b.out_stride = sc;
+    b.rs = 1;
+    b.cs = ldc;
+    b.m = m;
+    b.n = n;
+    b.alpha = 1.0;
+    int herr = 0;
+    if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess ||
+        oz_pack_a(A, sa, lda, m, k, 0, 0, nprob, m_pad, k_pad, slices, da, ea, st) != cudaSuccess ||
+        oz_pack_b(B, sb, ldb, k, n, 0, 0, nprob, n_pad, k_pad, slices, db, eb, st) != cudaSuccess ||
+        oz_gemm_launch(b, err, st) != cudaSuccess ||
+        cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess || herr)
+      rc = TEBD_ERR_CUDA;
+  }
+  (void)cudaGetLastError();
+  cudaFree(da);
+  cudaFree(db);
+  cudaFree(ea);
+  cudaFree(eb);
+  cudaFree(err);
+  return rc;
+}
+
 extern "C" int tebd_zgemm_tc(int nprob, int m, int n, int k, const double *A, long long stride_a, int lda,
                              const double *B, long long stride_b, int ldb, double *C, long long stride_c,
                              int ldc, int form, void *stream) {
+  const bool oz = form > 100 && form <= 100 + kOzMaxS;
   if (nprob < 1 || m < 1 || n < 1 || k < 1 || !A || !B || !C || lda < m || ldb < k || ldc < m ||
-      (form != kTc1xTF32 && form != kTc3xTF32))
+      (form != kTc1xTF32 && form != kTc3xTF32 && !oz))
     return TEBD_ERR_ARG;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (oz)
+    return zgemm_oz(nprob, m, n, k, reinterpret_cast<const double2 *>(A), stride_a, lda,
+                    reinterpret_cast<const double2 *>(B), stride_b, ldb, reinterpret_cast<double2 *>(C), stride_c,
+                    ldc, form - 100, st);
   const int m_pad = tc_pad(m, kTcBM), n_pad = tc_pad(2 * n, kTcBN), k_pad = tc_pad(2 * k, kTcBK);
   const int planes = tc_planes(form);
   float *pa = nullptr, *pb = nullptr;

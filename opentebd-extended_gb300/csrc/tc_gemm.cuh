@@ -68,4 +68,54 @@ cudaError_t tc_pack_b(const double2 *src, long long pstride, int ld, int krows, 
 inline int tc_pad(int x, int q) { return (x + q - 1) / q * q; }
 inline int tc_planes(int form) { return form == kTc3xTF32 ? 2 : 1; }
 
+// ---------------------------------------------------------------------------
+// FP64-class products: error-free splitting into bf16 integer digits (the
+// Ozaki scheme; K. Ozaki, T. Ogita, S. Oishi, S. M. Rump, "Error-free
+// transformations of matrix multiplication by using fast routines of matrix
+// multiplication", Numer. Algorithms 59, 2012).
+//
+// Every real row r of A_r (and of B_r) gets the power of two 2^e_r above its
+// largest magnitude and S digit planes: x = 2^e_r sum_s D_s 2^(-7(s+1)) + rest,
+// with D_0 in [-128, 128], D_s in [-64, 64] (s > 0), integers held exactly in
+// bf16, |rest| <= 2^(e_r - 7S - 1).  The real product is
+//   c_rc = 2^(e_r + f_c) sum_g 2^(-7(g+2)) sum_{s+t=g} (D^A_s D^B_t^T)_rc,
+// keeping the groups g = 0..S-1.  One group's sum over a K chunk of 512 real
+// terms stays below 2^24 for g <= 5 (each digit product is at most 2^14), so the
+// tensor cores' FP32 accumulation of it is exact; the chunks and groups are
+// combined in FP64.  Accuracy: about 2^(-7S) relative to (row max x column max)
+// per term -- S = 7 is FP64 class (~1e-15), S = 5 ~ 1e-11.
+// ---------------------------------------------------------------------------
+constexpr int kOzBN = 64;      // real output columns per CTA
+constexpr int kOzBK = 32;      // bf16 per 64-byte row (K block)
+constexpr int kOzMaxS = 7;
+
+struct OzBatch {
+  const unsigned short *a_dig;  // bf16 digits [S][nprob][m_pad][k_pad]
+  const unsigned short *b_dig;  // bf16 digits [S][nprob][n_pad][k_pad] (n_pad real rows)
+  const int *a_exp;             // [nprob][m_pad] row exponents
+  const int *b_exp;             // [nprob][n_pad / 2] exponents of the complex columns
+  int nprob, m_pad, n_pad, k_pad, slices;
+  double2 *out;                 // as TcBatch
+  long long out_stride, rs, cs;
+  const int *m_d, *n_d;         // per-problem sizes at m_d[p * dim_stride] (complex units), or null
+  int dim_stride;
+  int m, n;
+  int accumulate;
+  double alpha;
+  const unsigned char *optr;    // optional: output base of problem p read at optr + p * optr_stride
+  int optr_stride;
+};
+
+cudaError_t oz_gemm_launch(const OzBatch &b, int *err_d, cudaStream_t st);
+
+// Digits and exponents of the A operand (same source conventions as tc_pack_a);
+// exps must hold nprob * m_pad ints.
+cudaError_t oz_pack_a(const double2 *src, long long pstride, int ld, int rows, int cols, int trans,
+                      int conj, int nprob, int m_pad, int k_pad, int slices, unsigned short *dig,
+                      int *exps, cudaStream_t st);
+// Digits and exponents of the B operand (as tc_pack_b); exps: nprob * n_pad / 2 ints.
+cudaError_t oz_pack_b(const double2 *src, long long pstride, int ld, int krows, int ncols, int trans,
+                      int conj, int nprob, int n_pad, int k_pad, int slices, unsigned short *dig,
+                      int *exps, cudaStream_t st);
+
 }  // namespace tebd

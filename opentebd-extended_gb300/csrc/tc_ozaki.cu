@@ -1,0 +1,430 @@
+// tc_ozaki.cu -- FP64-class complex products on the sm_103a tensor cores by
+// error-free splitting into bf16 integer digits (scheme and accuracy in
+// tc_gemm.cuh).
+//
+// One CTA of 6 warps computes a 128 x 64 tile of the real product of one
+// problem:
+//   warp 4, lane 0   TMA producer: per 32-wide K block the S digit tiles of A
+//                    (128 rows x 64 B) and of B (64 rows x 64 B), 64-byte
+//                    swizzle, into one of `stages` shared-memory stages;
+//   warp 5, lane 0   MMA issuer: per K block two K-steps of 16, and per step
+//                    one tcgen05.mma (M 128, N 64, K 16, kind::f16, bf16 in,
+//                    FP32 accumulation) for every digit pair (s, t) with
+//                    s + t < S, into the TMEM accumulator of group g = s + t
+//                    (columns 64 g .. 64 g + 63);
+//   warps 0-3        epilogue (warp w reads TMEM lanes 32w..32w+31): after every chunk of 16 K blocks (512 real
+//                    terms: the group sums are exact integers below 2^24) they
+//                    read the S accumulators of their 32 rows, add
+//                    2^(-7(g+2)) x group into 64 FP64 registers, and release
+//                    TMEM to the issuer; after the last chunk the row and
+//                    column exponents are applied and the complex FP64 result
+//                    is written.
+// The issuer waits for the epilogue between chunks, so the two roles live in
+// different warps (a warp's lanes reconverge before tcgen05.ld).
+// Every wait is bounded as in tc_gemm.cu; on expiry *err is set and nothing is
+// written.
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "tc_gemm.cuh"
+#include "tc_ptx.cuh"
+
+namespace tebd {
+namespace {
+using namespace tcx;
+
+constexpr int kOzThreads = 192;
+constexpr int kOzMaxStages = 4;
+constexpr int kOzChunk = 16;  // K blocks per exact chunk (512 real terms)
+constexpr uint32_t kOzTileA = kTcBM * kOzBK * 2;  // 8 KB per digit tile of A
+constexpr uint32_t kOzTileB = kOzBN * kOzBK * 2;  // 4 KB per digit tile of B
+constexpr uint32_t kOzTmemCols = 512;
+
+// Instruction descriptor of kind::f16: D F32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdescBF16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kOzBN >> 3) << 17) |
+                                ((uint32_t)(kTcBM >> 4) << 24);
+constexpr int kExpZero = -2000;  // exponents below this mark an all-zero row
+
+int oz_stages(int S) {
+  const int per = S * (int)(kOzTileA + kOzTileB);
+  const int st = (220 * 1024) / per;
+  return st > kOzMaxStages ? kOzMaxStages : st;
+}
+size_t oz_smem(int S) { return 1024 + (size_t)oz_stages(S) * S * (kOzTileA + kOzTileB) + 512; }
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(kIdescBF16), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(kOzThreads, 1)
+    k_tc_oz(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzBatch b,
+            int stages, int *err) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int S = b.slices;
+  unsigned char *sA = smem;                                  // [stage][slice] kOzTileA
+  unsigned char *sB = sA + (size_t)stages * S * kOzTileA;    // [stage][slice] kOzTileB
+  uint64_t *full = reinterpret_cast<uint64_t *>(sB + (size_t)stages * S * kOzTileB);
+  uint64_t *empty = full + kOzMaxStages;
+  uint64_t *cfull = empty + kOzMaxStages;  // a chunk's MMAs are complete
+  uint64_t *tfree = cfull + 1;             // the epilogue has read the chunk (4 arrivals)
+  uint64_t *done = tfree + 1;              // every MMA issued has completed
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int p = blockIdx.z;
+  const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kOzBN;
+  const int mp = b.m_d ? b.m_d[(size_t)p * b.dim_stride] : b.m;
+  const int np = b.n_d ? b.n_d[(size_t)p * b.dim_stride] : b.n;
+  if (m0 >= mp || n0 >= 2 * np) return;  // tile outside this problem: uniform over the CTA
+  const int nk = b.k_pad / kOzBK;
+  const int nchunks = (nk + kOzChunk - 1) / kOzChunk;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(cfull, 1);
+    mbar_init(tfree, 4);
+    mbar_init(done, 1);
+    *abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
+                 "r"(kOzTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_before();
+  __syncthreads();
+  tc_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 4) {
+    // ---- TMA producer ----
+    if (lane != 0) goto finish;
+    const uint32_t bytes = S * (kOzTileA + kOzTileB);
+    int issued = 0;
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % stages;
+      if (kb >= stages && !mbar_wait(&empty[s], ((kb / stages) & 1) ^ 1, abort)) {
+        *abort = 1;
+        atomicExch(err, 1);
+        break;
+      }
+      mbar_expect_tx(&full[s], bytes);
+      for (int q = 0; q < S; ++q)
+        tma_load_3d(sA + (size_t)(s * S + q) * kOzTileA, &tmA, &full[s], kb * kOzBK, m0, q * b.nprob + p);
+      for (int q = 0; q < S; ++q)
+        tma_load_3d(sB + (size_t)(s * S + q) * kOzTileB, &tmB, &full[s], kb * kOzBK, n0, q * b.nprob + p);
+      issued = kb + 1;
+    }
+    if (*abort)
+      for (int kb = issued - stages < 0 ? 0 : issued - stages; kb < issued; ++kb)
+        mbar_wait(&full[kb % stages], (kb / stages) & 1, nullptr);
+    goto finish;
+  }
+  if (warp == 5) {
+    // ---- MMA issuer ----
+    if (lane != 0) goto finish;
+    uint32_t written = 0;
+    for (int kb = 0; kb < nk; ++kb) {
+      const int c = kb / kOzChunk, kc = kb % kOzChunk;
+      const int s = kb % stages;
+      if (kc == 0 && c > 0 && !mbar_wait(tfree, (c - 1) & 1, abort)) {
+        *abort = 1;
+        atomicExch(err, 1);
+        break;
+      }
+      if (kc == 0) written = 0;
+      if (!mbar_wait(&full[s], (kb / stages) & 1, abort)) {
+        *abort = 1;
+        atomicExch(err, 1);
+        break;
+      }
+      tc_after();
+      const uint32_t a0 = su32(sA + (size_t)s * S * kOzTileA);
+      const uint32_t b0 = su32(sB + (size_t)s * S * kOzTileB);
+      for (int kk = 0; kk < kOzBK / 16; ++kk) {
+        const uint32_t off = kk * 32;  // 16 bf16 = 32 bytes per K-step
+        for (int sa = 0; sa < S; ++sa)
+          for (int sb = 0; sa + sb < S; ++sb) {
+            const int g = sa + sb;
+            mma_bf16(tmem + (uint32_t)(g * kOzBN), sw64_desc(a0 + sa * kOzTileA + off),
+                     sw64_desc(b0 + sb * kOzTileB + off), (written >> g) & 1u);
+            written |= 1u << g;
+          }
+      }
+      mma_commit(&empty[s]);
+      if (kc == kOzChunk - 1 || kb == nk - 1) mma_commit(cfull);
+    }
+    mma_commit(done);
+    goto finish;
+  }
+
+  {
+  // ---- epilogue (warps 0-3): exact chunk sums into FP64 ----
+  double acc[kOzBN];
+#pragma unroll
+  for (int i = 0; i < kOzBN; ++i) acc[i] = 0.0;
+  bool ok = true;
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+  for (int c = 0; c < nchunks; ++c) {
+    if (!mbar_wait(cfull, c & 1, abort)) {
+      ok = false;
+      break;
+    }
+    tc_after();
+    for (int g = 0; g < S; ++g) {
+      const double sc = ldexp(1.0, -7 * (g + 2));
+#pragma unroll
+      for (int c0 = 0; c0 < kOzBN; c0 += 16) {
+        float v[16];
+        tmem_ld16(lane_base + (uint32_t)(g * kOzBN + c0), v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) acc[c0 + i] = fma(sc, (double)v[i], acc[c0 + i]);
+      }
+    }
+    tc_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(tfree);
+  }
+  const bool all_done = mbar_wait(done, 0, nullptr);
+  tc_after();
+  if (!all_done) atomicExch(err, 1);
+  if (ok && all_done && !*abort) {
+    const int row = m0 + warp * 32 + lane;
+    if (row < mp) {
+      double2 *out = b.optr ? *reinterpret_cast<double2 *const *>(b.optr + (size_t)p * b.optr_stride)
+                            : b.out + (size_t)p * b.out_stride;
+      const int ea = b.a_exp[(size_t)p * b.m_pad + row];
+      const long long cs = b.cs ? b.cs : mp;  // cs == 0: column stride = this problem's row count
+#pragma unroll
+      for (int t = 0; t < kOzBN / 2; ++t) {
+        const int j = n0 / 2 + t;
+        if (j < np) {
+          const int eb = b.b_exp[(size_t)p * (b.n_pad / 2) + j];
+          double2 r = make_double2(0.0, 0.0);
+          if (ea > kExpZero && eb > kExpZero)
+            r = make_double2(b.alpha * ldexp(acc[2 * t], ea + eb), b.alpha * ldexp(acc[2 * t + 1], ea + eb));
+          double2 *o = out + (long long)row * b.rs + (long long)j * cs;
+          if (b.accumulate) {
+            const double2 q = *o;
+            r.x += q.x;
+            r.y += q.y;
+          }
+          *o = r;
+        }
+      }
+    }
+  }
+  }
+finish:
+  tc_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kOzTmemCols)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// digit extraction
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void oz_digits(double x, int e, int S, unsigned short *d) {
+  if (e <= kExpZero) {
+    for (int s = 0; s < S; ++s) d[s] = 0;
+    return;
+  }
+  double t = ldexp(x, -e);  // |t| < 1
+  for (int s = 0; s < S; ++s) {
+    const double y = t * 128.0;
+    const double q = rint(y);
+    d[s] = __bfloat16_as_ushort(__float2bfloat16_rn((float)q));  // |q| <= 128: exact
+    t = y - q;                                                    // exact, |t| <= 1/2
+  }
+}
+
+__device__ __forceinline__ int oz_exp(double mag) {
+  int e = 0;
+  frexp(mag, &e);  // mag = f 2^e, f in [1/2, 1)
+  return e;
+}
+
+// Load a 32 x 32 complex tile of the source as tile[row r][column c] with the
+// same conventions as the TF32 packers: A (trans: element (i, k) at src[k + ld i],
+// else src[i + ld k]); B (element (k, j) at src[j + ld k] if trans, else
+// src[k + ld j]) is loaded as tile[j][k].
+__device__ __forceinline__ void oz_tile_a(double2 (*tile)[33], const double2 *S, int ld, int rows, int cols,
+                                          int trans, int conj, int i0, int k0) {
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int yy = ty; yy < 32; yy += 8) {
+    const int i = trans ? i0 + yy : i0 + tx, k = trans ? k0 + tx : k0 + yy;
+    double2 v = make_double2(0.0, 0.0);
+    if (i < rows && k < cols) v = trans ? S[k + (size_t)ld * i] : S[i + (size_t)ld * k];
+    if (conj) v.y = -v.y;
+    if (trans)
+      tile[yy][tx] = v;
+    else
+      tile[tx][yy] = v;
+  }
+}
+__device__ __forceinline__ void oz_tile_b(double2 (*tile)[33], const double2 *S, int ld, int krows, int ncols,
+                                          int trans, int conj, int j0, int k0) {
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int yy = ty; yy < 32; yy += 8) {
+    const int j = trans ? j0 + tx : j0 + yy, k = trans ? k0 + yy : k0 + tx;
+    double2 v = make_double2(0.0, 0.0);
+    if (k < krows && j < ncols) v = trans ? S[j + (size_t)ld * k] : S[k + (size_t)ld * j];
+    if (conj) v.y = -v.y;
+    if (trans)
+      tile[tx][yy] = v;
+    else
+      tile[yy][tx] = v;
+  }
+}
+
+// Pass 1: the exponent of every row (A) or complex column (B): atomicMax of the
+// tile's row maxima.  Pass 2 (digits = 1): the S digit planes.
+template <bool kB>
+__global__ void __launch_bounds__(256) k_oz_pack(const double2 *src, long long pstride, int ld, int r_ext,
+                                                 int c_ext, int trans, int conj, int nprob, int rows_pad,
+                                                 int k_pad, int S, unsigned short *dig, int *exps,
+                                                 int digits) {
+  __shared__ double2 tile[32][33];
+  const int p = blockIdx.z;
+  const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const double2 *Sp = src + (size_t)p * pstride;
+  if (kB)
+    oz_tile_b(tile, Sp, ld, r_ext, c_ext, trans, conj, r0, k0);
+  else
+    oz_tile_a(tile, Sp, ld, r_ext, c_ext, trans, conj, r0, k0);
+  __syncthreads();
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int nrow = kB ? rows_pad / 2 : rows_pad;  // complex rows (A) / complex columns (B)
+  if (!digits) {
+    for (int yy = ty; yy < 32; yy += 8) {
+      const double2 v = tile[yy][tx];
+      double mx = fmax(fabs(v.x), fabs(v.y));
+      for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      const int r = r0 + yy;
+      if (tx == 0 && r < nrow && mx > 0.0) atomicMax(&exps[(size_t)p * nrow + r], oz_exp(mx));
+    }
+    return;
+  }
+  const size_t plane = (size_t)nprob * rows_pad * k_pad;
+  for (int yy = ty; yy < 32; yy += 8) {
+    const int r = r0 + yy, k = k0 + tx;
+    if (r >= nrow || 2 * k >= k_pad) continue;
+    const double2 v = tile[yy][tx];
+    const int e = exps[(size_t)p * nrow + r];
+    unsigned short dr[kOzMaxS], di[kOzMaxS];
+    oz_digits(v.x, e, S, dr);
+    oz_digits(v.y, e, S, di);
+    if (!kB) {
+      unsigned short *o = dig + ((size_t)p * rows_pad + r) * k_pad + 2 * k;
+      for (int s = 0; s < S; ++s)
+        *reinterpret_cast<uint32_t *>(o + s * plane) = (uint32_t)dr[s] | ((uint32_t)di[s] << 16);
+    } else {
+      // rows 2r: (re, -im); 2r+1: (im, re)
+      unsigned short *o0 = dig + ((size_t)p * rows_pad + 2 * r) * k_pad + 2 * k;
+      unsigned short *o1 = o0 + k_pad;
+      for (int s = 0; s < S; ++s) {
+        const unsigned short ni = di[s] ^ 0x8000u;  // -im (bf16 sign bit; -0 for 0 is harmless)
+        *reinterpret_cast<uint32_t *>(o0 + s * plane) = (uint32_t)dr[s] | ((uint32_t)ni << 16);
+        *reinterpret_cast<uint32_t *>(o1 + s * plane) = (uint32_t)di[s] | ((uint32_t)dr[s] << 16);
+      }
+    }
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 oz_encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    (void)cudaGetLastError();
+  });
+  return fn;
+}
+
+// 3-D map over [depth][rows][k] bf16 with a 32 x box_rows box, 64-byte swizzle.
+bool oz_map(CUtensorMap *map, const unsigned short *base, int k_pad, int rows, int depth, int box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = oz_encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)k_pad, (cuuint64_t)rows, (cuuint64_t)depth};
+  cuuint64_t strides[2] = {(cuuint64_t)k_pad * 2, (cuuint64_t)k_pad * 2 * rows};
+  cuuint32_t box[3] = {(cuuint32_t)kOzBK, (cuuint32_t)box_rows, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<unsigned short *>(base), dims, strides, box,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+cudaError_t oz_gemm_launch(const OzBatch &b, int *err_d, cudaStream_t st) {
+  if (b.m_pad % kTcBM || b.n_pad % kOzBN || b.k_pad % kOzBK || b.k_pad <= 0 || b.nprob <= 0 ||
+      b.slices < 1 || b.slices > kOzMaxS)
+    return cudaErrorInvalidValue;
+  CUtensorMap ma, mb;
+  if (!oz_map(&ma, b.a_dig, b.k_pad, b.m_pad, b.slices * b.nprob, kTcBM) ||
+      !oz_map(&mb, b.b_dig, b.k_pad, b.n_pad, b.slices * b.nprob, kOzBN))
+    return cudaErrorInvalidValue;
+  const size_t smem = oz_smem(b.slices);
+  cudaError_t e = cudaFuncSetAttribute(k_tc_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid(b.m_pad / kTcBM, b.n_pad / kOzBN, b.nprob);
+  k_tc_oz<<<grid, kOzThreads, smem, st>>>(ma, mb, b, oz_stages(b.slices), err_d);
+  return cudaPeekAtLastError();
+}
+
+cudaError_t oz_pack_a(const double2 *src, long long pstride, int ld, int rows, int cols, int trans, int conj,
+                      int nprob, int m_pad, int k_pad, int slices, unsigned short *dig, int *exps,
+                      cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(exps, 0x80, sizeof(int) * (size_t)nprob * m_pad, st);
+  if (e != cudaSuccess) return e;
+  dim3 grid((m_pad + 31) / 32, (k_pad / 2 + 31) / 32, nprob);
+  k_oz_pack<false><<<grid, 256, 0, st>>>(src, pstride, ld, rows, cols, trans, conj, nprob, m_pad, k_pad, slices,
+                                         dig, exps, 0);
+  k_oz_pack<false><<<grid, 256, 0, st>>>(src, pstride, ld, rows, cols, trans, conj, nprob, m_pad, k_pad, slices,
+                                         dig, exps, 1);
+  return cudaPeekAtLastError();
+}
+
+cudaError_t oz_pack_b(const double2 *src, long long pstride, int ld, int krows, int ncols, int trans, int conj,
+                      int nprob, int n_pad, int k_pad, int slices, unsigned short *dig, int *exps,
+                      cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(exps, 0x80, sizeof(int) * (size_t)nprob * (n_pad / 2), st);
+  if (e != cudaSuccess) return e;
+  dim3 grid((n_pad / 2 + 31) / 32, (k_pad / 2 + 31) / 32, nprob);
+  k_oz_pack<true><<<grid, 256, 0, st>>>(src, pstride, ld, krows, ncols, trans, conj, nprob, n_pad, k_pad, slices,
+                                        dig, exps, 0);
+  k_oz_pack<true><<<grid, 256, 0, st>>>(src, pstride, ld, krows, ncols, trans, conj, nprob, n_pad, k_pad, slices,
+                                        dig, exps, 1);
+  return cudaPeekAtLastError();
+}
+
+}  // namespace tebd

@@ -74,3 +74,37 @@ def test_zgemm_tc_leaves_padding_of_c_untouched(pkg):
     assert np.all(C[0, :, 70:] == 7.0 + 3.0j)
     ref = A[0].T @ B[0].T
     assert np.max(np.abs(C[0, :, :70].T - ref)) < 1e-4
+
+
+@pytest.mark.parametrize("slices", [7, 5, 3])
+@pytest.mark.parametrize("nprob,m,n,k", [(1, 1, 1, 1), (2, 130, 70, 33), (1, 640, 160, 640), (1, 300, 40, 700)])
+def test_zgemm_ozaki_error_bound(pkg, slices, nprob, m, n, k):
+    """Error-free splitting into `slices` bf16 digit planes: every element within
+    2^(-7 slices + 2) x (row max of A) x (column max of B) x 2k of the complex128
+    product (k = 700 needs two exact 512-term chunks of the real embedding)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(m + n + k + slices)
+    A = _cplx(rng, (nprob, k, m)) * np.exp(rng.uniform(-3, 3, (nprob, 1, m)))  # rows of different scales
+    B = _cplx(rng, (nprob, n, k)) * np.exp(rng.uniform(-3, 3, (nprob, n, 1)))
+    C = _run(pkg, torch, A, B, 100 + slices)
+    for p in range(nprob):
+        Ap, Bp = A[p].T, B[p].T
+        ref = Ap @ Bp
+        rmax = np.max(np.maximum(np.abs(Ap.real), np.abs(Ap.imag)), axis=1)
+        cmax = np.max(np.maximum(np.abs(Bp.real), np.abs(Bp.imag)), axis=0)
+        bound = 2.0 ** (-7 * slices + 2) * np.outer(rmax, cmax) * 2 * k
+        err = np.abs(C[p].T - ref)
+        assert np.all(err <= bound + 1e-300), np.max(err / bound)
+
+
+def test_zgemm_ozaki7_matches_fp64_to_rounding(pkg):
+    """With 7 slices the product is FP64 class: within 4e-15 of complex128 relative
+    to (|A| |B|)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    A = _cplx(rng, (1, 640, 640))
+    B = _cplx(rng, (1, 128, 640))
+    C = _run(pkg, torch, A, B, 107)
+    ref = A[0].T @ B[0].T
+    scale = np.abs(A[0].T) @ np.abs(B[0].T)
+    assert np.max(np.abs(C[0].T - ref) / scale) < 4e-15
