@@ -635,6 +635,7 @@ def run_saturated(args):
     gate = H.matrix_exponential(H.bose_hubbard(L, D, J, U, MU)[1], DT)
     links = list(range(1, L, 2))
     chain = pkg.Chain(L, D, CHI, svd_mode=SVD_MODES[args.svd])
+    chain.set_theta_form(args.theta_form)
     chain.set_state(gam, lam)
     stream = torch.cuda.ExternalStream(chain.stream())
     for _ in range(args.warmup):
@@ -653,7 +654,8 @@ def run_saturated(args):
     out = {"metric": "two-site updates/sec, saturated bonds (640 x 640 Theta)",
            "value": len(links) * args.steps / (ms / 1e3), "unit": "updates/s", "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps,
-           "config": {"workload": "saturated_bonds_L64_d5_chi128", "bonds_per_step": len(links)},
+           "config": {"workload": "saturated_bonds_L64_d5_chi128", "bonds_per_step": len(links),
+                      "theta_form": args.theta_form},
            "gebrd_tflops": st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12 if st["gebrd_ms"] > 0 else None,
            "gebrd_share": st["gebrd_ms"] / ms, "bidiag_share": st["bidiag_ms"] / ms,
            "gpu_launches": st["kernel_launches"]}
@@ -676,6 +678,8 @@ def main():
                     help="extra legs of the kept-rank form at these discarded-weight bounds (FP64 and "
                          "double-float), with speedup and observable errors against the plain run")
     ap.add_argument("--cpu-updates", type=int, default=2)
+    ap.add_argument("--theta-form", type=int, default=0,
+                    help="Theta formation: 0 CUDA cores, 3 = 3xTF32, 100+S = S bf16 digit planes (tensor cores)")
     ap.add_argument("--outdir", default=os.path.join(ROOT, "bench_out"),
                     help="where the clock samples of the timed region are written")
     args = ap.parse_args()

@@ -185,6 +185,15 @@ int tebd_canonical_form_all_nc(tebd_handle *h);
  * the reference's rule. */
 int tebd_set_rank_bound(tebd_handle *h, double bound);
 
+/* Theta formation (FormTheta, local_operations_module.f90:184-211) on the tensor
+ * cores, dense handles (no counterpart in the reference, which forms Theta in
+ * FP64 loops).  form 0: CUDA cores (FP64, or double-float with TEBD_SVD_DF), the
+ * default; 3: 3xTF32 split-precision product with FP32 accumulation (~FP32
+ * accuracy; the precision tier's Theta); 100 + S, S = 3..7: S bf16 digit planes
+ * (error ~2^(-7S) of the largest terms; S = 7 is FP64 class).  ThetaOperation,
+ * the SVD and the restoration are unchanged. */
+int tebd_set_theta_form(tebd_handle *h, int form);
+
 /* Internal degrees of freedom for every NC routine of the handle: the reference
  * passes the OPTIONAL argument intDegFree to TwoSiteOpNC, TrotterStepNC and
  * CanonicalFormAllNC (local_operations_module.f90:748-1443, 1723-1964;

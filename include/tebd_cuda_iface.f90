@@ -284,5 +284,10 @@ INTERFACE
     INTEGER(C_LONG_LONG), VALUE :: stride_a, stride_b, stride_c
     TYPE(C_PTR), VALUE :: A, B, C, stream
   END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_set_theta_form(h, form) BIND(C, NAME='tebd_set_theta_form')
+    IMPORT :: C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: h
+    INTEGER(C_INT), VALUE :: form
+  END FUNCTION
 END INTERFACE
 END MODULE tebd_cuda_iface

@@ -97,6 +97,7 @@ static void free_all(tebd_handle *h) {
   cudaFree(h->sig_count_d);
   cudaFree(h->sweeps_link_d);
   tebd::nc_free(h);
+  tebd::tc_free(h);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->stream) cudaStreamDestroy(h->stream);
 }

@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int p = blockIdx.z;
   const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kTcBN;
-  const int mp = b.m_d ? b.m_d[p] : b.m, np = b.n_d ? b.n_d[p] : b.n;
+  const int mp = b.m_d ? b.m_d[(size_t)p * b.dim_stride] : b.m;
+  const int np = b.n_d ? b.n_d[(size_t)p * b.dim_stride] : b.n;
   if (m0 >= mp || n0 >= 2 * np) return;  // tile outside this problem: uniform over the CTA
   const int nk = b.k_pad / kTcBK;
 
@@ -151,7 +152,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_after();
   if (ok && !*abort) {
     const int row = m0 + warp * 32 + lane;
-    double2 *out = b.out + (size_t)p * b.out_stride;
+    double2 *out = b.optr ? *reinterpret_cast<double2 *const *>(b.optr + (size_t)p * b.optr_stride)
+                          : b.out + (size_t)p * b.out_stride;
+    const long long cs = b.cs ? b.cs : mp;  // cs == 0: column stride = this problem's row count
 #pragma unroll 1
     for (int c0 = 0; c0 < kTcBN; c0 += 16) {
       float v[16];
@@ -161,7 +164,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int t = 0; t < 8; ++t) {
           const int j = (n0 + c0) / 2 + t;
           if (j < np) {
-            double2 *o = out + (long long)row * b.rs + (long long)j * b.cs;
+            double2 *o = out + (long long)row * b.rs + (long long)j * cs;
             double2 r = make_double2(b.alpha * (double)v[2 * t], b.alpha * (double)v[2 * t + 1]);
             if (b.accumulate) {
               const double2 q = *o;
@@ -346,114 +349,151 @@ cudaError_t tc_pack_b(const double2 *src, long long pstride, int ld, int krows, 
 
 }  // namespace tebd
 
-// ---------------------------------------------------------------------------
-// C ABI: the split-precision complex product on its own (diagnostics; no
-// counterpart in the reference, which multiplies only inside FormTheta)
-// ---------------------------------------------------------------------------
-using namespace tebd;
+namespace tebd {
 
-static int zgemm_oz(int nprob, int m, int n, int k, const double2 *A, long long sa, int lda, const double2 *B,
-                    long long sb, int ldb, double2 *C, long long sc, int ldc, int slices, cudaStream_t st) {
-  const int m_pad = tc_pad(m, kTcBM), n_pad = tc_pad(2 * n, kOzBN), k_pad = tc_pad(2 * k, kOzBK);
-  unsigned short *da = nullptr, *db = nullptr;
-  int *ea = nullptr, *eb = nullptr, *err = nullptr;
-  int rc = TEBD_OK;
-  if (cudaMalloc(&da, sizeof(unsigned short) * slices * (size_t)nprob * m_pad * k_pad) != cudaSuccess ||
-      cudaMalloc(&db, sizeof(unsigned short) * slices * (size_t)nprob * n_pad * k_pad) != cudaSuccess ||
-      cudaMalloc(&ea, sizeof(int) * (size_t)nprob * m_pad) != cudaSuccess ||
-      cudaMalloc(&eb, sizeof(int) * (size_t)nprob * n_pad / 2) != cudaSuccess ||
-      cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
-    rc = TEBD_ERR_OOM;
-  } else {
+static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct ZDims {
+  int m_pad, n_pad, k_pad, planes;
+};
+static ZDims zdims(const ZProd &z) {
+  ZDims d;
+  const bool oz = zprod_oz(z.form);
+  d.m_pad = tc_pad(z.m, kTcBM);
+  d.n_pad = tc_pad(2 * z.n, oz ? kOzBN : kTcBN);
+  d.k_pad = tc_pad(2 * z.k, oz ? kOzBK : kTcBK);
+  d.planes = oz ? z.form - 100 : tc_planes(z.form);
+  return d;
+}
+
+size_t zprod_ws_bytes(const ZProd &z) {
+  const ZDims d = zdims(z);
+  const size_t el = zprod_oz(z.form) ? 2 : 4;
+  size_t b = al256(el * d.planes * (size_t)z.nprob * d.m_pad * d.k_pad) +
+             al256(el * d.planes * (size_t)z.nprob * d.n_pad * d.k_pad);
+  if (zprod_oz(z.form)) b += al256(sizeof(int) * (size_t)z.nprob * d.m_pad) + al256(sizeof(int) * (size_t)z.nprob * d.n_pad / 2);
+  return b;
+}
+
+cudaError_t zprod_run(const ZProd &z, void *ws, int *err_d, cudaStream_t st) {
+  const ZDims d = zdims(z);
+  char *p = static_cast<char *>(ws);
+  const size_t el = zprod_oz(z.form) ? 2 : 4;
+  char *pa = p;
+  p += al256(el * d.planes * (size_t)z.nprob * d.m_pad * d.k_pad);
+  char *pb = p;
+  p += al256(el * d.planes * (size_t)z.nprob * d.n_pad * d.k_pad);
+  cudaError_t e;
+  if (zprod_oz(z.form)) {
+    int *ea = reinterpret_cast<int *>(p);
+    p += al256(sizeof(int) * (size_t)z.nprob * d.m_pad);
+    int *eb = reinterpret_cast<int *>(p);
+    const int S = d.planes;
+    auto *da = reinterpret_cast<unsigned short *>(pa);
+    auto *db = reinterpret_cast<unsigned short *>(pb);
+    if ((e = oz_pack_a(z.a, z.a_stride, z.lda, z.m, z.k, z.a_trans, z.a_conj, z.nprob, d.m_pad, d.k_pad, S, da,
+                       ea, st)) != cudaSuccess ||
+        (e = oz_pack_b(z.b, z.b_stride, z.ldb, z.k, z.n, z.b_trans, z.b_conj, z.nprob, d.n_pad, d.k_pad, S, db,
+                       eb, st)) != cudaSuccess)
+      return e;
     OzBatch b = {};
     b.a_dig = da;
     b.b_dig = db;
     b.a_exp = ea;
     b.b_exp = eb;
-    b.nprob = nprob;
-    b.m_pad = m_pad;
-    b.n_pad = n_pad;
-    b.k_pad = k_pad;
-    b.slices = slices;
-    b.out = C;
-    b.out_stride = sc;
-    b.rs = 1;
-    b.cs = ldc;
-    b.m = m;
-    b.n = n;
-    b.alpha = 1.0;
-    int herr = 0;
-    if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess ||
-        oz_pack_a(A, sa, lda, m, k, 0, 0, nprob, m_pad, k_pad, slices, da, ea, st) != cudaSuccess ||
-        oz_pack_b(B, sb, ldb, k, n, 0, 0, nprob, n_pad, k_pad, slices, db, eb, st) != cudaSuccess ||
-        oz_gemm_launch(b, err, st) != cudaSuccess ||
-        cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess || herr)
-      rc = TEBD_ERR_CUDA;
+    b.nprob = z.nprob;
+    b.m_pad = d.m_pad;
+    b.n_pad = d.n_pad;
+    b.k_pad = d.k_pad;
+    b.slices = S;
+    b.out = z.out;
+    b.out_stride = z.out_stride;
+    b.rs = z.rs;
+    b.cs = z.cs;
+    b.m_d = z.m_d;
+    b.n_d = z.n_d;
+    b.dim_stride = z.dim_stride;
+    b.m = z.m;
+    b.n = z.n;
+    b.accumulate = z.accumulate;
+    b.alpha = z.alpha;
+    b.optr = z.optr;
+    b.optr_stride = z.optr_stride;
+    return oz_gemm_launch(b, err_d, st);
   }
-  (void)cudaGetLastError();
-  cudaFree(da);
-  cudaFree(db);
-  cudaFree(ea);
-  cudaFree(eb);
-  cudaFree(err);
-  return rc;
+  float *fa = reinterpret_cast<float *>(pa), *fb = reinterpret_cast<float *>(pb);
+  if ((e = tc_pack_a(z.a, z.a_stride, z.lda, z.m, z.k, z.a_trans, z.a_conj, z.nprob, d.m_pad, d.k_pad, z.form,
+                     fa, st)) != cudaSuccess ||
+      (e = tc_pack_b(z.b, z.b_stride, z.ldb, z.k, z.n, z.b_trans, z.b_conj, z.nprob, d.n_pad, d.k_pad, z.form,
+                     fb, st)) != cudaSuccess)
+    return e;
+  TcBatch b = {};
+  b.a_planes = fa;
+  b.b_planes = fb;
+  b.nprob = z.nprob;
+  b.m_pad = d.m_pad;
+  b.n_pad = d.n_pad;
+  b.k_pad = d.k_pad;
+  b.form = z.form;
+  b.out = z.out;
+  b.out_stride = z.out_stride;
+  b.rs = z.rs;
+  b.cs = z.cs;
+  b.m_d = z.m_d;
+  b.n_d = z.n_d;
+  b.dim_stride = z.dim_stride;
+  b.m = z.m;
+  b.n = z.n;
+  b.accumulate = z.accumulate;
+  b.alpha = z.alpha;
+  b.optr = z.optr;
+  b.optr_stride = z.optr_stride;
+  return tc_gemm_launch(b, err_d, st);
 }
+
+}  // namespace tebd
+
+// ---------------------------------------------------------------------------
+// C ABI: the complex product on its own (diagnostics; no counterpart in the
+// reference, which multiplies only inside FormTheta)
+// ---------------------------------------------------------------------------
+using namespace tebd;
 
 extern "C" int tebd_zgemm_tc(int nprob, int m, int n, int k, const double *A, long long stride_a, int lda,
                              const double *B, long long stride_b, int ldb, double *C, long long stride_c,
                              int ldc, int form, void *stream) {
-  const bool oz = form > 100 && form <= 100 + kOzMaxS;
   if (nprob < 1 || m < 1 || n < 1 || k < 1 || !A || !B || !C || lda < m || ldb < k || ldc < m ||
-      (form != kTc1xTF32 && form != kTc3xTF32 && !oz))
+      (form != kTc1xTF32 && form != kTc3xTF32 && !zprod_oz(form)))
     return TEBD_ERR_ARG;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (oz)
-    return zgemm_oz(nprob, m, n, k, reinterpret_cast<const double2 *>(A), stride_a, lda,
-                    reinterpret_cast<const double2 *>(B), stride_b, ldb, reinterpret_cast<double2 *>(C), stride_c,
-                    ldc, form - 100, st);
-  const int m_pad = tc_pad(m, kTcBM), n_pad = tc_pad(2 * n, kTcBN), k_pad = tc_pad(2 * k, kTcBK);
-  const int planes = tc_planes(form);
-  float *pa = nullptr, *pb = nullptr;
+  ZProd z = {};
+  z.a = reinterpret_cast<const double2 *>(A);
+  z.a_stride = stride_a;
+  z.lda = lda;
+  z.b = reinterpret_cast<const double2 *>(B);
+  z.b_stride = stride_b;
+  z.ldb = ldb;
+  z.nprob = nprob;
+  z.m = m;
+  z.n = n;
+  z.k = k;
+  z.form = form;
+  z.out = reinterpret_cast<double2 *>(C);
+  z.out_stride = stride_c;
+  z.rs = 1;
+  z.cs = ldc;
+  z.alpha = 1.0;
+  void *ws = nullptr;
   int *err = nullptr;
-  const size_t sa = sizeof(float) * planes * (size_t)nprob * m_pad * k_pad;
-  const size_t sb = sizeof(float) * planes * (size_t)nprob * n_pad * k_pad;
-  int rc = TEBD_OK;
-  if (cudaMalloc(&pa, sa) != cudaSuccess || cudaMalloc(&pb, sb) != cudaSuccess ||
-      cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
+  int rc = TEBD_OK, herr = 0;
+  if (cudaMalloc(&ws, zprod_ws_bytes(z)) != cudaSuccess || cudaMalloc(&err, sizeof(int)) != cudaSuccess)
     rc = TEBD_ERR_OOM;
-  } else {
-    TcBatch b = {};
-    b.a_planes = pa;
-    b.b_planes = pb;
-    b.nprob = nprob;
-    b.m_pad = m_pad;
-    b.n_pad = n_pad;
-    b.k_pad = k_pad;
-    b.form = form;
-    b.out = reinterpret_cast<double2 *>(C);
-    b.out_stride = stride_c;
-    b.rs = 1;
-    b.cs = ldc;
-    b.m = m;
-    b.n = n;
-    b.alpha = 1.0;
-    int herr = 0;
-    if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess ||
-        tc_pack_a(reinterpret_cast<const double2 *>(A), stride_a, lda, m, k, 0, 0, nprob, m_pad, k_pad, form,
-                  pa, st) != cudaSuccess ||
-        tc_pack_b(reinterpret_cast<const double2 *>(B), stride_b, ldb, k, n, 0, 0, nprob, n_pad, k_pad, form,
-                  pb, st) != cudaSuccess ||
-        tc_gemm_launch(b, err, st) != cudaSuccess ||
-        cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      rc = TEBD_ERR_CUDA;
-    else if (herr)
-      rc = TEBD_ERR_CUDA;
-  }
+  else if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess || zprod_run(z, ws, err, st) != cudaSuccess ||
+           cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+           cudaStreamSynchronize(st) != cudaSuccess || herr)
+    rc = TEBD_ERR_CUDA;
   (void)cudaGetLastError();
-  cudaFree(pa);
-  cudaFree(pb);
+  cudaFree(ws);
   cudaFree(err);
   return rc;
 }

@@ -42,10 +42,13 @@ struct TcBatch {
   double2 *out;
   long long out_stride;
   long long rs, cs;
-  const int *m_d, *n_d;   // device arrays of per-problem sizes (complex units), or null
+  const int *m_d, *n_d;   // per-problem sizes at m_d[p * dim_stride] (complex units), or null
+  int dim_stride;
   int m, n;               // sizes used when m_d / n_d are null
   int accumulate;         // 1: out += C, 0: out = C
   double alpha;           // scale applied to C
+  const unsigned char *optr;  // optional: output base of problem p read at optr + p * optr_stride
+  int optr_stride;            // (cs == 0 then means: column stride = the problem's m)
 };
 
 // Launch one batch on `st`.  err_d: device int set non-zero if a pipeline wait
@@ -117,5 +120,37 @@ cudaError_t oz_pack_a(const double2 *src, long long pstride, int ld, int rows, i
 cudaError_t oz_pack_b(const double2 *src, long long pstride, int ld, int krows, int ncols, int trans,
                       int conj, int nprob, int n_pad, int k_pad, int slices, unsigned short *dig,
                       int *exps, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// One batched complex product C_p (m x n) = op(A_p) (m x k) op(B_p) (k x n) in
+// any of the forms: 1 / 3 (1xTF32, 3xTF32) or 100 + S (S bf16 digit planes).
+// op(A): element (i, l) at a[i + lda l] (a_trans = 0) or a[l + lda i] (a_trans = 1),
+// conjugated when a_conj; op(B): (l, j) at b[l + ldb j] or b[j + ldb l].  The
+// sizes are the batch maxima: each operand is read up to them (the caller
+// zero-fills beyond a problem's own extent), the output is written only inside
+// the problem's own m_d / n_d.
+// ---------------------------------------------------------------------------
+struct ZProd {
+  const double2 *a;
+  long long a_stride;
+  int lda, a_trans, a_conj;
+  const double2 *b;
+  long long b_stride;
+  int ldb, b_trans, b_conj;
+  int nprob, m, n, k;
+  int form;
+  double2 *out;
+  long long out_stride, rs, cs;
+  const int *m_d, *n_d;
+  int dim_stride;
+  int accumulate;
+  double alpha;
+  const unsigned char *optr;
+  int optr_stride;
+};
+inline bool zprod_oz(int form) { return form > 100 && form <= 100 + kOzMaxS; }
+size_t zprod_ws_bytes(const ZProd &z);
+// ws: zprod_ws_bytes(z) bytes of device memory (256-byte aligned).
+cudaError_t zprod_run(const ZProd &z, void *ws, int *err_d, cudaStream_t st);
 
 }  // namespace tebd

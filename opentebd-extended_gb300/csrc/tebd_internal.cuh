@@ -173,6 +173,12 @@ struct tebd_handle {
   int unnormalized;        // 1 while Swapping runs: Theta is decomposed without 1/||Theta||
   double rank_bound;       // kept-rank form: discarded weight bound per bond (0 = keep chi)
   cudaEvent_t ev[6];
+  // tensor-core products (theta_tc.cu)
+  int theta_form;          // 0: CUDA cores (FP64, or double-float with TEBD_SVD_DF);
+                           // 3: 3xTF32; 100 + S: S bf16 digit planes (tcgen05)
+  void *tc_ws;             // operand planes / digits, grown on demand
+  size_t tc_ws_bytes;
+  int *tc_err;             // set by a tensor-core kernel whose pipeline wait expired
 };
 
 namespace tebd {
@@ -215,6 +221,12 @@ int nc_alloc(tebd_handle *h);
 void nc_free(tebd_handle *h);
 
 constexpr int kNormParts = 64;
+
+// tensor-core Theta formation (theta_tc.cu)
+int launch_theta_tc(tebd_handle *h, int nb);
+int tc_reserve(tebd_handle *h, size_t bytes);
+int tc_check(tebd_handle *h);  // reads and clears tc_err (synchronises the stream)
+void tc_free(tebd_handle *h);
 
 }  // namespace tebd
 

@@ -69,7 +69,7 @@ EXPORTED_SYMBOLS = (
     "tebd_record_lambdas", "tebd_record_gammas", "tebd_record_labels", "tebd_read_gamma_lambda",
     "tebd_read_gamma_lambda_labels", "tebd_swapping", "tebd_trotter_step_pbc", "tebd_canonical_form_all_nc",
     "tebd_canonical_form", "tebd_canonical_form_all", "tebd_set_conserv", "tebd_set_rank_bound",
-    "tebd_zgemm_tc",
+    "tebd_zgemm_tc", "tebd_set_theta_form",
 )
 
 
@@ -180,6 +180,7 @@ def load_library(path: str = LIB_PATH):
     L.tebd_canonical_form_all_nc.argtypes = [vp]
     L.tebd_set_conserv.argtypes = [vp, ip]
     L.tebd_set_rank_bound.argtypes = [vp, ctypes.c_double]
+    L.tebd_set_theta_form.argtypes = [vp, ctypes.c_int]
     L.tebd_canonical_form.argtypes = [vp, ctypes.c_int]
     L.tebd_canonical_form_all.argtypes = [vp]
     cp = ctypes.c_char_p
@@ -240,6 +241,11 @@ class Chain:
         """Kept-rank form: keep the fewest singular values whose discarded weight is
         at most ``bound`` per update (0 = the reference's rule, chi values)."""
         self._check(self._lib.tebd_set_rank_bound(self.h, float(bound)))
+
+    def set_theta_form(self, form):
+        """Theta formation: 0 CUDA cores (default), 3 = 3xTF32 on the tensor cores,
+        100 + S = S bf16 digit planes on the tensor cores (S = 7: FP64 class)."""
+        self._check(self._lib.tebd_set_theta_form(self.h, int(form)))
 
     def set_conserv(self, conserv):
         """Internal degrees of freedom for the NC routines: ``conserv`` = Conserv%vi
