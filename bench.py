@@ -48,7 +48,7 @@ J, U, MU, DT, ORDER = 1.0, 2.0, 0.0, 0.005, 2
 AMP, SEED = 1e-3, 1
 UPDATES_PER_STEP = (L // 2) * 2 + (L - 1) // 2  # 32 + 31 + 32 = 95
 METRIC = "two-site updates/sec (Trotter steps/sec = value/95)"
-SVD_MODES = {"fp64": 0, "df": 5}  # plain FP64 / precision form (double-float bidiagonalisation)
+SVD_MODES = {"fp64": 0, "df": 5, "rsvd": 6}  # plain FP64 / double-float / randomized (learned-rank) route
 WORKLOAD = "bose_hubbard_L64_d5_chi128_fp64_trotter2"
 
 
@@ -658,7 +658,9 @@ def run_saturated(args):
                       "theta_form": args.theta_form},
            "gebrd_tflops": st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12 if st["gebrd_ms"] > 0 else None,
            "gebrd_share": st["gebrd_ms"] / ms, "bidiag_share": st["bidiag_ms"] / ms,
-           "gpu_launches": st["kernel_launches"]}
+           "gpu_launches": st["kernel_launches"],
+           "rsvd": {"updates": st["rsvd_updates"], "fallbacks": st["rsvd_fallbacks"],
+                    "worst_residual": st["rsvd_worst_residual"], "tc_flops": st["rsvd_flops"]}}
     print(json.dumps(out), flush=True)
     chain.close()
 

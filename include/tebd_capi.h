@@ -81,6 +81,13 @@ extern "C" {
                                      the Theta formation, run in double-float (pairs of
                                      FP32, 48-bit significands) on the FP32 pipe; number-
                                      conserving blocks on the bidiagonal route too       */
+#define TEBD_SVD_RSVD 6           /* learned-rank form: bonds whose compacted Theta is
+                                     much larger than the kept rank r take a randomized
+                                     sketch of width r + p with FP64-class products on
+                                     the tensor cores and a Rayleigh-Ritz SVD (FP64);
+                                     the full SVD of TEBD_SVD_FP64 is the fallback when
+                                     a kept triplet's residual exceeds the tolerance
+                                     (tebd_set_rsvd); the other bonds as TEBD_SVD_FP64 */
 
 #define TEBD_OPTS_VERSION 1
 
@@ -185,6 +192,19 @@ int tebd_canonical_form_all_nc(tebd_handle *h);
  * the reference's rule. */
 int tebd_set_rank_bound(tebd_handle *h, double bound);
 
+/* Randomized route of TEBD_SVD_RSVD (no reference counterpart; it stands in for
+ * ZGESVD, local_operations_module.f90:322-345, on bonds whose compacted Theta is
+ * much larger than the kept rank).  oversample: sketch columns beyond the kept
+ * rank (default 64); power_iters: extra X^H X applications (default 2, at most
+ * 4); tol: a bond is accepted when every kept triplet's residual
+ * rho = |Theta^H u - sigma v| is at most tol * ||Theta|| (default 1e-5), else its
+ * full SVD is computed -- an accepted triplet's singular value is then within
+ * ~rho^2 / gap and its vectors within ~rho / gap of the exact ones; slices: bf16
+ * digit planes of the range finder's tensor-core products (3..7, default 5, ~2^-35:
+ * a subspace needs no more); the Rayleigh-Ritz products always use 7 (FP64
+ * class).  The learned model may set the sketch per batch instead. */
+int tebd_set_rsvd(tebd_handle *h, int oversample, int power_iters, double tol, int slices);
+
 /* Theta formation (FormTheta, local_operations_module.f90:184-211) on the tensor
  * cores, dense handles (no counterpart in the reference, which forms Theta in
  * FP64 loops).  form 0: CUDA cores (FP64, or double-float with TEBD_SVD_DF), the
@@ -244,6 +264,11 @@ typedef struct tebd_stats {
                                   16 M N^2 - 16 N^3 / 3 per bond (M >= N)                  */
   double gebrd_ms;             /* device time of the bidiagonalisation kernel (profiling on) */
   long long gebrd_launches;    /* bidiagonalisation kernel launches                        */
+  long long rsvd_updates;      /* updates that took the randomized route (TEBD_SVD_RSVD)   */
+  long long rsvd_fallbacks;    /* of those, the ones the judge sent to the full SVD        */
+  double rsvd_flops;           /* algorithmic flops (8 m n k per complex product) of the
+                                  randomized route's tensor-core products                 */
+  double rsvd_worst_residual;  /* largest triplet residual / ||Theta|| the judge saw        */
 } tebd_stats;
 int tebd_set_profiling(tebd_handle *h, int on);
 int tebd_get_stats(tebd_handle *h, tebd_stats *stats);

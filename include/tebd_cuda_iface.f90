@@ -19,6 +19,8 @@ TYPE, BIND(C) :: tebd_stats
   INTEGER(C_LONG_LONG) :: bidiag_updates
   REAL(C_DOUBLE) :: gebrd_flops, gebrd_ms
   INTEGER(C_LONG_LONG) :: gebrd_launches
+  INTEGER(C_LONG_LONG) :: rsvd_updates, rsvd_fallbacks
+  REAL(C_DOUBLE) :: rsvd_flops, rsvd_worst_residual
 END TYPE
 INTERFACE
   SUBROUTINE tebd_default_opts(o) BIND(C, NAME='tebd_default_opts')
@@ -288,6 +290,12 @@ INTERFACE
     IMPORT :: C_INT, C_PTR
     TYPE(C_PTR), VALUE :: h
     INTEGER(C_INT), VALUE :: form
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_set_rsvd(h, oversample, power_iters, tol, slices) BIND(C, NAME='tebd_set_rsvd')
+    IMPORT :: C_DOUBLE, C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: h
+    INTEGER(C_INT), VALUE :: oversample, power_iters, slices
+    REAL(C_DOUBLE), VALUE :: tol
   END FUNCTION
 END INTERFACE
 END MODULE tebd_cuda_iface

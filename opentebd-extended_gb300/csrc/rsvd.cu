@@ -1,0 +1,601 @@
+// rsvd.cu -- the randomized SVD route of the learned-rank form (TEBD_SVD_RSVD):
+// ZGESVD of SVDTruncation (VidalCore_v_2.0/local_operations_module.f90:322-345)
+// replaced, for bonds whose compacted Theta is much larger than the rank kept,
+// by a sketch of its leading singular subspace, with the full SVD as the fallback
+// and the judge.
+//
+// Per bond (X = the gated, unnormalised Theta, m x n; r triplets wanted, sketch
+// width s = r + p).  Every product below runs on the tensor cores as an
+// error-free digit-plane product (tc_ozaki.cu): the range finder with S_sk
+// planes (default 5, ~2^-35: a subspace needs no more), everything from the
+// final basis on with 7 planes (FP64 class).  The only FP64 CUDA-core work is
+// O(s^3): the Cholesky factors of s x s Grams and one s x s SVD.
+//   1. Xp = X zero-padded to the batch's m_max x n_max (kept: the fallback
+//      restarts from it);
+//   2. Q = orth(Xp Om) (Om: n x s complex Gaussian, fixed per handle), then q
+//      times P = orth(Xp^H Q), Q = orth(Xp P); finally P = orth(Xp^H Q) --
+//      span(P) approximates the top-s right singular subspace with error
+//      ~ (sigma_{s+1}/sigma_i)^(2q+2);
+//      orth(A) is CholQR: G = A^H A, G = R^H R (FP64, pivots below the Gram's
+//      rounding level dropped), A <- A R^-1 -- once for the intermediate bases,
+//      twice (CholQR2) for the final P;
+//   3. C = Xp P (m x s), M = C^H C (s x s) and its SVD M = W Lambda W^H (the
+//      bidiagonal route, FP64): the Rayleigh-Ritz triplets of Theta in span(P)
+//      are (C w_i / |C w_i|, |C w_i|, P w_i);
+//   4. the slot's X = C W (= U Sigma, m x r) and V = P W (n x r): the layout the
+//      bidiagonal route leaves, so FormLambda1/FormGamma1/2 run unchanged;
+//   5. the judge: for each kept triplet the residual of the other side,
+//      rho_i = |Xp^H u_i - sigma_i v_i| (one more product, Xp^H (U Sigma)); a bond
+//      whose largest rho_i exceeds tol * ||Theta|| is re-run from Xp with the
+//      full SVD.  An accepted triplet's singular value is within ~rho^2/gap and
+//      its vectors within ~rho/gap of the exact ones.
+// The sketch width and power count come from tebd_set_rsvd or, per batch, from
+// the learned model (mlp.cu).
+#include <math.h>
+#include <stddef.h>
+
+#include <algorithm>
+
+#include "tc_gemm.cuh"
+
+namespace tebd {
+
+namespace {
+
+size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// per-slot carve of the randomized-SVD workspace (bytes), for n_full x n_full
+// Theta, sketch capacity sc and chi kept triplets at most
+struct RsCarve {
+  size_t xp, a, b, z, c, g, ri, w, rr, aux, tau, taup, bdws, per;
+};
+RsCarve rs_carve(int n, int sc, int chi) {
+  RsCarve c;
+  size_t aux_el = 0, bd_d = 0;
+  bidiag_block_ws(sc, sc, std::min(chi, sc), &aux_el, &bd_d);
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = o;
+    o += al(bytes);
+    return at;
+  };
+  c.xp = take(sizeof(double2) * (size_t)n * n);
+  c.a = take(sizeof(double2) * (size_t)n * sc);
+  c.b = take(sizeof(double2) * (size_t)n * sc);
+  c.z = take(sizeof(double2) * (size_t)n * sc);
+  c.c = take(sizeof(double2) * (size_t)n * sc);
+  c.g = take(sizeof(double2) * (size_t)sc * sc);
+  c.ri = take(sizeof(double2) * (size_t)sc * sc);
+  c.w = take(sizeof(double2) * (size_t)sc * sc);
+  c.rr = take(sizeof(double2) * (size_t)n * chi);
+  c.aux = take(sizeof(double2) * aux_el);
+  c.tau = take(sizeof(double2) * sc);
+  c.taup = take(sizeof(double2) * sc);
+  c.bdws = take(sizeof(double) * bd_d);
+  c.per = o;
+  return c;
+}
+
+// counter-based normal deviates for Om (Box-Muller on a 64-bit mix of the index)
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdULL;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ULL;
+  x ^= x >> 33;
+  return x;
+}
+
+__global__ void k_rs_omega(double2 *om, int n, int s, unsigned long long seed) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * s;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const unsigned long long a = mix64(seed ^ (2 * e + 1)), b = mix64(seed ^ (2 * e + 2) ^ 0x9e3779b97f4a7c15ULL);
+    const double u1 = ((double)(a >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    const double u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
+    const double rad = sqrt(-2.0 * log(u1));
+    om[e] = make_double2(rad * cos(6.283185307179586 * u2), rad * sin(6.283185307179586 * u2));
+  }
+}
+
+// dims[s] = {m, n, s_active, r}: the bond's compacted sizes, the sketch width
+// (0: not on this route) and the triplets wanted
+struct RsDims {
+  int m, n, s, r;
+};
+
+// 1. Xp (m_max x n_max, ld m_max) = X (m x n, ld m) zero-padded
+__global__ void k_rs_pad(const Slot *slots, const RsDims *dims, double2 *ws, size_t per, int m_max, int n_max) {
+  const int p = blockIdx.y;
+  if (dims[p].s == 0) return;
+  const Compact cp = *slots[p].cp;
+  const double2 *X = slots[p].X;
+  double2 *Xp = reinterpret_cast<double2 *>(reinterpret_cast<char *>(ws) + p * per);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)m_max * n_max;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % m_max), j = (int)(e / m_max);
+    Xp[e] = (i < cp.m && j < cp.n) ? X[i + (size_t)cp.m * j] : make_double2(0.0, 0.0);
+  }
+}
+
+// CholQR step on a Gram: G (s x s, ld s, Hermitian, both triangles) = R^H R with
+// R upper triangular (right-looking Cholesky in place on the upper triangle),
+// then Ri = R^-1 (upper).  A pivot at or below `floor` times the largest diagonal
+// (the Gram's own rounding level: its products carry 7 S bits) marks a direction
+// the sketch does not span to that accuracy: its row of R and column of R^-1 are
+// zero, so A R^-1 has a zero column there.  One CTA per bond.
+__global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, size_t per, size_t og, size_t ori,
+                                                 int s, double floor) {
+  const int p = blockIdx.x;
+  if (dims[p].s == 0) return;
+  double2 *G = reinterpret_cast<double2 *>(ws + p * per + og);
+  double2 *Ri = reinterpret_cast<double2 *>(ws + p * per + ori);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ double gmax, piv;
+  __shared__ double red[512];
+  double mx = 0.0;
+  for (int j = tid; j < s; j += nt) mx = fmax(mx, G[j + (size_t)s * j].x);
+  red[tid] = mx;
+  __syncthreads();
+  for (int w = nt / 2; w > 0; w >>= 1) {
+    if (tid < w) red[tid] = fmax(red[tid], red[tid + w]);
+    __syncthreads();
+  }
+  if (tid == 0) gmax = red[0];
+  __syncthreads();
+  const double thresh = gmax * floor;
+  for (int j = 0; j < s; ++j) {
+    if (tid == 0) {
+      const double d = G[j + (size_t)s * j].x;
+      piv = (d > thresh && d > 0.0) ? sqrt(d) : 0.0;
+      G[j + (size_t)s * j] = make_double2(piv, 0.0);
+    }
+    __syncthreads();
+    const double inv = piv > 0.0 ? 1.0 / piv : 0.0;
+    for (int k = j + 1 + tid; k < s; k += nt) {  // row j of R
+      const double2 v = G[j + (size_t)s * k];
+      G[j + (size_t)s * k] = make_double2(v.x * inv, v.y * inv);
+    }
+    __syncthreads();
+    const int t = s - j - 1;
+    for (int e = tid; e < t * t; e += nt) {  // trailing upper triangle: G_kl -= conj(R_jk) R_jl
+      const int k = j + 1 + e % t, l = j + 1 + e / t;
+      if (k > l) continue;
+      const double2 a = G[j + (size_t)s * k], b = G[j + (size_t)s * l];
+      double2 &g = G[k + (size_t)s * l];
+      g.x -= a.x * b.x + a.y * b.y;
+      g.y -= a.x * b.y - a.y * b.x;
+    }
+    __syncthreads();
+  }
+  // Ri = R^-1 (upper), row by row from the bottom: Ri_ii = 1 / R_ii and
+  // Ri_ic = -(sum_{l=i+1..c} R_il Ri_lc) / R_ii; one warp per column, lanes over l
+  // (Ri's columns are contiguous: coalesced), so the O(s^3 / 6) work is spread
+  // over the CTA instead of one thread per column.
+  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  for (int e = tid; e < s * s; e += nt) Ri[e] = make_double2(0.0, 0.0);
+  __syncthreads();
+  for (int i = s - 1; i >= 0; --i) {
+    const double d = G[i + (size_t)s * i].x;
+    const double inv = d > 0.0 ? 1.0 / d : 0.0;
+    for (int c = i + 1 + warp; c < s; c += nw) {
+      double ax = 0.0, ay = 0.0;
+      for (int l = i + 1 + lane; l <= c; l += 32) {
+        const double2 r = G[i + (size_t)s * l], x = Ri[l + (size_t)s * c];
+        ax = fma(r.x, x.x, fma(-r.y, x.y, ax));
+        ay = fma(r.x, x.y, fma(r.y, x.x, ay));
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, o);
+        ay += __shfl_xor_sync(0xffffffffu, ay, o);
+      }
+      if (lane == 0) Ri[i + (size_t)s * c] = make_double2(-ax * inv, -ay * inv);
+    }
+    if (tid == 0) Ri[i + (size_t)s * i] = make_double2(inv, 0.0);
+    __syncthreads();
+  }
+}
+
+// the slot's X (m x r, ld m) = the first m rows of U Sigma (ld m_max); k = r
+__global__ void k_rs_store(Slot *slots, const RsDims *dims, const char *ws, size_t off, size_t per, int m_max,
+                           int r) {
+  const int p = blockIdx.y;
+  if (dims[p].s == 0) return;
+  Slot S = slots[p];
+  const int m = S.cp->m;
+  const double2 *U = reinterpret_cast<const double2 *>(ws + p * per + off);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)m * r;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % m), c = (int)(e / m);
+    S.X[e] = U[i + (size_t)m_max * c];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) S.cp->k = r;
+}
+
+// judge: R = Xp^H (U Sigma) (n_max x r, ld n_max); rho_i = |R_i - sigma_i^2 v_i| / sigma_i
+// with sigma_i = |column i of U Sigma|; bad[p] = 1 if max rho_i > tol ||Theta||.
+// One CTA per bond, one warp per column.
+__global__ void k_rs_judge(const Slot *slots, const RsDims *dims, const char *ws, size_t off_u, size_t off_r,
+                           size_t per, int m_max, int n_max, const double *nrm, double tol, int *bad,
+                           double *worst) {
+  const int p = blockIdx.x;
+  if (dims[p].s == 0) return;
+  const int r = dims[p].r, n = slots[p].cp->n;
+  const double2 *U = reinterpret_cast<const double2 *>(ws + p * per + off_u);
+  const double2 *R = reinterpret_cast<const double2 *>(ws + p * per + off_r);
+  const double2 *V = slots[p].V;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __shared__ double wmax[32];
+  double mx = 0.0;
+  for (int c = warp; c < r; c += nw) {
+    double a = 0.0;
+    for (int i = lane; i < m_max; i += 32) {
+      const double2 u = U[i + (size_t)m_max * c];
+      a = fma(u.x, u.x, fma(u.y, u.y, a));
+    }
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    const double s2 = a;  // sigma^2
+    double e = 0.0;
+    for (int i = lane; i < n; i += 32) {
+      const double2 q = R[i + (size_t)n_max * c], v = V[i + (size_t)n * c];
+      const double dx = q.x - s2 * v.x, dy = q.y - s2 * v.y;
+      e = fma(dx, dx, fma(dy, dy, e));
+    }
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    mx = fmax(mx, s2 > 0.0 ? sqrt(e / s2) : 0.0);
+  }
+  if (lane == 0) wmax[warp] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double w = 0.0;
+    for (int i = 0; i < nw; ++i) w = fmax(w, wmax[i]);
+    const double rel = w / nrm[p];
+    worst[p] = rel;
+    bad[p] = !(rel <= tol);  // NaN counts as bad
+  }
+}
+
+// fallback: the slot's X (m x n, ld m) = Xp again
+__global__ void k_rs_restore(Slot *slots, const int *again, const char *ws, size_t per, int m_max) {
+  const int p = blockIdx.y;
+  if (!again[p]) return;
+  const Slot S = slots[p];
+  const int m = S.cp->m, n = S.cp->n;
+  const double2 *Xp = reinterpret_cast<const double2 *>(ws + p * per);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)m * n;
+       e += (size_t)gridDim.x * blockDim.x)
+    S.X[e] = Xp[(e % m) + (size_t)m_max * (e / m)];
+}
+
+}  // namespace
+
+struct RsState {
+  int n_full, sc, chi, nslots;
+  RsCarve carve;
+  void *ws;          // nslots * carve.per
+  double2 *om;       // n_full x sc
+  Slot *in_slots_d;  // the s x s problems of the bidiagonal route
+  Compact *in_cp_d;
+  int *in_path_d;
+  RsDims *dims_d;
+  int *bad_d;
+  double *worst_d;
+  std::vector<int> in_path_h;
+  // digits of Xp (as the A operand) and of Xp^H, 7 planes, packed once per batch
+  unsigned short *xd0, *xd1;
+  int *xe0, *xe1;
+};
+
+void rsvd_free(tebd_handle *h) {
+  RsState *r = static_cast<RsState *>(h->rs);
+  if (!r) return;
+  cudaFree(r->ws);
+  cudaFree(r->om);
+  cudaFree(r->in_slots_d);
+  cudaFree(r->in_cp_d);
+  cudaFree(r->in_path_d);
+  cudaFree(r->dims_d);
+  cudaFree(r->bad_d);
+  cudaFree(r->worst_d);
+  cudaFree(r->xd0);
+  cudaFree(r->xd1);
+  cudaFree(r->xe0);
+  cudaFree(r->xe1);
+  delete r;
+  h->rs = nullptr;
+}
+
+// 7 digit planes of an n x n operand for every slot
+static size_t rs_digit_bytes(int n, int ns) {
+  return sizeof(unsigned short) * kOzMaxS * (size_t)ns * tc_pad(n, kTcBM) * tc_pad(2 * n, kOzBK);
+}
+
+static int rsvd_alloc(tebd_handle *h, int sc) {
+  RsState *r = static_cast<RsState *>(h->rs);
+  if (r && r->sc >= sc) return TEBD_OK;
+  if (r) {
+    int rc = check_cuda(h, cudaStreamSynchronize(h->stream), "randomized SVD workspace");
+    if (rc) return rc;
+    rsvd_free(h);
+  }
+  r = new (std::nothrow) RsState();
+  if (!r) return set_error(h, TEBD_ERR_OOM, "randomized SVD state");
+  h->rs = r;
+  r->n_full = h->n;
+  r->sc = sc;
+  r->chi = h->chi;
+  r->nslots = h->nslots;
+  r->carve = rs_carve(h->n, sc, h->chi);
+  int rc;
+  const int ns = h->nslots;
+  if ((rc = check_cuda(h, cudaMalloc(&r->ws, r->carve.per * ns), "alloc randomized SVD workspace")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->om, sizeof(double2) * (size_t)h->n * sc), "alloc sketch")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->in_slots_d, sizeof(Slot) * ns), "alloc rsvd slots")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->in_cp_d, sizeof(Compact) * ns), "alloc rsvd slots")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->in_path_d, sizeof(int) * ns), "alloc rsvd slots")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->dims_d, sizeof(RsDims) * ns), "alloc rsvd slots")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->bad_d, sizeof(int) * ns), "alloc rsvd flags")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->worst_d, sizeof(double) * ns), "alloc rsvd flags")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->xd0, rs_digit_bytes(h->n, ns)), "alloc rsvd digits")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->xd1, rs_digit_bytes(h->n, ns)), "alloc rsvd digits")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->xe0, sizeof(int) * ns * (size_t)tc_pad(h->n, kTcBM)), "alloc rsvd digits")) ||
+      (rc = check_cuda(h, cudaMalloc(&r->xe1, sizeof(int) * ns * (size_t)tc_pad(h->n, kTcBM)), "alloc rsvd digits"))) {
+    rsvd_free(h);
+    return rc;
+  }
+  k_rs_omega<<<256, 256, 0, h->stream>>>(r->om, h->n, sc, 0x5eed5eedULL);
+  TEBD_LAUNCHED(h);
+  r->in_path_h.assign(ns, kPathQRJ);
+  return check_cuda(h, cudaGetLastError(), "sketch generation");
+}
+
+// One bidiagonal-route batch on the s x s Grams: problem p's matrix at byte
+// offset `off` of its workspace (ld s), its right vectors to offset `voff`
+// (ld s); kk triplets.
+static int rs_gram_svd(tebd_handle *h, RsState *R, const std::vector<int> &on, int nb, int s, size_t off,
+                       size_t voff, int kk) {
+  std::vector<Slot> sl(nb);
+  std::vector<Compact> cp(nb);
+  char *base = static_cast<char *>(R->ws);
+  for (int p = 0; p < nb; ++p) {
+    Slot &S = sl[p];
+    memset(&S, 0, sizeof(S));
+    char *w = base + p * R->carve.per;
+    S.X = reinterpret_cast<double2 *>(w + off);
+    S.V = reinterpret_cast<double2 *>(w + voff);
+    S.aux = reinterpret_cast<double2 *>(w + R->carve.aux);
+    S.tau = reinterpret_cast<double2 *>(w + R->carve.tau);
+    S.taup = reinterpret_cast<double2 *>(w + R->carve.taup);
+    S.bdws = reinterpret_cast<double *>(w + R->carve.bdws);
+    S.cp = R->in_cp_d + p;
+    cp[p] = {0, 0, 0, s, s, s};
+    R->in_path_h[p] = on[p] ? kPathBidiag : kPathQRJ;
+    if (on[p]) h->stats.gebrd_flops += 16.0 * s * (double)s * s - 16.0 / 3.0 * (double)s * s * s;
+  }
+  int rc;
+  if ((rc = check_cuda(h, cudaMemcpyAsync(R->in_slots_d, sl.data(), sizeof(Slot) * nb, cudaMemcpyHostToDevice,
+                                          h->stream), "upload rsvd slots")) ||
+      (rc = check_cuda(h, cudaMemcpyAsync(R->in_cp_d, cp.data(), sizeof(Compact) * nb, cudaMemcpyHostToDevice,
+                                          h->stream), "upload rsvd slots")) ||
+      (rc = check_cuda(h, cudaMemcpyAsync(R->in_path_d, R->in_path_h.data(), sizeof(int) * nb,
+                                          cudaMemcpyHostToDevice, h->stream), "upload rsvd routes")) ||
+      (rc = check_cuda(h, cudaStreamSynchronize(h->stream), "upload rsvd slots")))  // host vectors go away
+    return rc;
+  BidiagBatch b;
+  b.slots_d = R->in_slots_d;
+  b.path_d = R->in_path_d;
+  b.path_h = R->in_path_h.data();
+  b.nb = nb;
+  b.nmax = s;
+  b.kk = kk;
+  b.dfp = false;
+  b.phase = 0;
+  b.cap = 0;
+  return run_bidiag_batch(h, b);
+}
+
+// The randomized route for the bonds with route[p] == kPathRsvd (set by the
+// caller from the compaction record); on return route[p] is kPathRsvd for the
+// accepted bonds and the full route (kPathBidiag / kPathBidiagT) for the bonds
+// the judge sent back, whose Theta is back in the slot's X.
+int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vector<int> &route,
+             const std::vector<int> &rank, int sketch) {
+  int m_max = 0, n_max = 0, r_max = 0, s = 0;
+  std::vector<RsDims> dims(nb, RsDims{0, 0, 0, 0});
+  std::vector<int> on(nb, 0);
+  for (int p = 0; p < nb; ++p) {
+    if (route[p] != kPathRsvd) continue;
+    on[p] = 1;
+    m_max = std::max(m_max, cps[p].m);
+    n_max = std::max(n_max, cps[p].n);
+    r_max = std::max(r_max, rank[p]);
+    s = std::max(s, std::min(sketch, std::min(cps[p].m, cps[p].n)));
+  }
+  if (!s) return TEBD_OK;
+  s = std::max(s, r_max);
+  int rc = rsvd_alloc(h, std::max(s, h->rs_sketch_cap));
+  if (rc) return rc;
+  h->rs_sketch_cap = std::max(h->rs_sketch_cap, s);
+  RsState *R = static_cast<RsState *>(h->rs);
+  for (int p = 0; p < nb; ++p)  // one rank for the batch: the s x s SVD computes r_max triplets
+    if (on[p]) dims[p] = {cps[p].m, cps[p].n, s, r_max};
+  cudaStream_t st = h->stream;
+  if ((rc = check_cuda(h, cudaMemcpyAsync(R->dims_d, dims.data(), sizeof(RsDims) * nb, cudaMemcpyHostToDevice, st),
+                       "upload rsvd sizes")) ||
+      (rc = check_cuda(h, cudaStreamSynchronize(st), "upload rsvd sizes")))
+    return rc;
+  const size_t per = R->carve.per;
+  char *ws = static_cast<char *>(R->ws);
+  const RsCarve &c = R->carve;
+  const long long pstr = (long long)(per / sizeof(double2));
+  const int dstride = (int)(sizeof(RsDims) / sizeof(int));
+  const int sk = h->rs_slices, fin = kOzMaxS;
+  // out (rows x cols, ld rows, workspace offset oo) = op(A) op(B); A and B are
+  // workspace offsets unless a base pointer is given
+  auto prod = [&](size_t ao, int lda, int at, const double2 *abase, long long astr, size_t bo, int ldb,
+                  const double2 *bbase, long long bstr, int rows, int cols, int k, size_t oo, int slices) -> int {
+    ZProd z = {};
+    z.a = abase ? abase : reinterpret_cast<const double2 *>(ws + ao);
+    z.a_stride = astr;
+    z.lda = lda;
+    z.a_trans = at;
+    z.a_conj = at;
+    z.b = bbase ? bbase : reinterpret_cast<const double2 *>(ws + bo);
+    z.b_stride = bstr;
+    z.ldb = ldb;
+    z.nprob = nb;
+    z.m = rows;
+    z.n = cols;
+    z.k = k;
+    z.form = 100 + slices;
+    z.out = reinterpret_cast<double2 *>(ws + oo);
+    z.out_stride = pstr;
+    z.rs = 1;
+    z.cs = rows;
+    z.n_d = &R->dims_d[0].s;  // 0 off the route: those tiles exit at once
+    z.dim_stride = dstride;
+    z.alpha = 1.0;
+    if (!abase && ao == c.xp) {  // Xp or Xp^H: digits packed once for the batch
+      z.a_dig = at ? R->xd1 : R->xd0;
+      z.a_exp = at ? R->xe1 : R->xe0;
+    }
+    int e = tc_reserve(h, zprod_ws_bytes(z));
+    if (e) return e;
+    e = check_cuda(h, zprod_run(z, h->tc_ws, h->tc_err, st), "randomized SVD product");
+    h->launches += 5;
+    h->stats.rsvd_flops += 8.0 * rows * (double)cols * k * nb;
+    return e;
+  };
+  // CholQR of the rows x s block at `buf` (ld rows), through `tmp`: one pass for
+  // the range finder's intermediate bases (only their span matters), two (CholQR2,
+  // the second with 7 planes) for the final basis P; the result is left in `buf`
+  auto cholqr2 = [&](size_t buf, size_t tmp, int rows, int slices2) -> int {
+    int e;
+    if ((e = prod(buf, rows, 1, nullptr, pstr, buf, rows, nullptr, pstr, s, s, rows, c.g, sk))) return e;
+    k_rs_chol<<<nb, 512, 0, st>>>(R->dims_d, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * sk + 10));
+    TEBD_LAUNCHED(h);
+    if ((e = prod(buf, rows, 0, nullptr, pstr, c.ri, s, nullptr, pstr, rows, s, s, tmp, sk))) return e;
+    if (slices2 != fin)  // one pass: back into buf
+      return check_cuda(h, cudaMemcpy2DAsync(ws + buf, per, ws + tmp, per, sizeof(double2) * (size_t)rows * s, nb,
+                                             cudaMemcpyDeviceToDevice, st),
+                        "CholQR copy");
+    if ((e = prod(tmp, rows, 1, nullptr, pstr, tmp, rows, nullptr, pstr, s, s, rows, c.g, fin))) return e;
+    k_rs_chol<<<nb, 512, 0, st>>>(R->dims_d, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * fin + 10));
+    TEBD_LAUNCHED(h);
+    return prod(tmp, rows, 0, nullptr, pstr, c.ri, s, nullptr, pstr, rows, s, s, buf, fin);
+  };
+  // 1. padded copy
+  k_rs_pad<<<dim3(256, nb), 256, 0, st>>>(h->slots_d, R->dims_d, reinterpret_cast<double2 *>(ws), per, m_max,
+                                           n_max);
+  TEBD_LAUNCHED(h);
+  {
+    const double2 *xp0 = reinterpret_cast<const double2 *>(ws + c.xp);
+    if ((rc = check_cuda(h, oz_pack_a(xp0, pstr, m_max, m_max, n_max, 0, 0, nb, tc_pad(m_max, kTcBM),
+                                      tc_pad(2 * n_max, kOzBK), fin, R->xd0, R->xe0, st),
+                         "pack Xp")) ||
+        (rc = check_cuda(h, oz_pack_a(xp0, pstr, m_max, n_max, m_max, 1, 1, nb, tc_pad(n_max, kTcBM),
+                                      tc_pad(2 * m_max, kOzBK), fin, R->xd1, R->xe1, st),
+                         "pack Xp^H")))
+      return rc;
+    h->launches += 4;
+  }
+  // 2. range finder
+  if ((rc = prod(c.xp, m_max, 0, nullptr, pstr, 0, R->n_full, R->om, 0, m_max, s, n_max, c.a, sk)) ||
+      (rc = cholqr2(c.a, c.b, m_max, sk)))
+    return rc;
+  for (int it = 0; it < h->rs_power; ++it)
+    if ((rc = prod(c.xp, m_max, 1, nullptr, pstr, c.a, m_max, nullptr, pstr, n_max, s, m_max, c.z, sk)) ||
+        (rc = cholqr2(c.z, c.b, n_max, sk)) ||
+        (rc = prod(c.xp, m_max, 0, nullptr, pstr, c.z, n_max, nullptr, pstr, m_max, s, n_max, c.a, sk)) ||
+        (rc = cholqr2(c.a, c.b, m_max, sk)))
+      return rc;
+  if ((rc = prod(c.xp, m_max, 1, nullptr, pstr, c.a, m_max, nullptr, pstr, n_max, s, m_max, c.z, sk)) ||
+      (rc = cholqr2(c.z, c.b, n_max, fin)))
+    return rc;
+  // 3. Rayleigh-Ritz: C = Xp P, M = C^H C, M = W Lambda W^H
+  if ((rc = prod(c.xp, m_max, 0, nullptr, pstr, c.z, n_max, nullptr, pstr, m_max, s, n_max, c.c, fin)) ||
+      (rc = prod(c.c, m_max, 1, nullptr, pstr, c.c, m_max, nullptr, pstr, s, s, m_max, c.g, fin)) ||
+      (rc = rs_gram_svd(h, R, on, nb, s, c.g, c.w, r_max)))
+    return rc;
+  // 4. V = P W -> the slot's V (ld n); U Sigma = C W -> the slot's X (ld m); k = r
+  {
+    ZProd z = {};
+    z.a = reinterpret_cast<const double2 *>(ws + c.z);
+    z.a_stride = pstr;
+    z.lda = n_max;
+    z.b = reinterpret_cast<const double2 *>(ws + c.w);
+    z.b_stride = pstr;
+    z.ldb = s;
+    z.nprob = nb;
+    z.m = n_max;
+    z.n = r_max;
+    z.k = s;
+    z.form = 100 + fin;
+    z.rs = 1;
+    z.cs = 0;  // ld = the bond's n (its m_d entry below)
+    z.m_d = &R->dims_d[0].n;
+    z.n_d = &R->dims_d[0].r;
+    z.dim_stride = dstride;
+    z.alpha = 1.0;
+    z.optr = reinterpret_cast<const unsigned char *>(h->slots_d) + offsetof(Slot, V);
+    z.optr_stride = (int)sizeof(Slot);
+    if ((rc = tc_reserve(h, zprod_ws_bytes(z)))) return rc;
+    if ((rc = check_cuda(h, zprod_run(z, h->tc_ws, h->tc_err, st), "randomized SVD V"))) return rc;
+    h->launches += 5;
+  }
+  if ((rc = prod(c.c, m_max, 0, nullptr, pstr, c.w, s, nullptr, pstr, m_max, r_max, s, c.a, fin))) return rc;
+  k_rs_store<<<dim3(256, nb), 256, 0, st>>>(h->slots_d, R->dims_d, ws, c.a, per, m_max, r_max);
+  TEBD_LAUNCHED(h);
+  // 5. judge: R = Xp^H (U Sigma), residuals of the kept triplets
+  if ((rc = prod(c.xp, m_max, 1, nullptr, pstr, c.a, m_max, nullptr, pstr, n_max, r_max, m_max, c.rr, fin)))
+    return rc;
+  k_rs_judge<<<nb, 256, 0, st>>>(h->slots_d, R->dims_d, ws, c.a, c.rr, per, m_max, n_max, h->nrm, h->rs_tol,
+                                 R->bad_d, R->worst_d);
+  TEBD_LAUNCHED(h);
+  std::vector<int> bad(nb, 0);
+  std::vector<double> worst(nb, 0.0);
+  if ((rc = check_cuda(h, cudaMemcpyAsync(bad.data(), R->bad_d, sizeof(int) * nb, cudaMemcpyDeviceToHost, st),
+                       "read rsvd judge")) ||
+      (rc = check_cuda(h, cudaMemcpyAsync(worst.data(), R->worst_d, sizeof(double) * nb, cudaMemcpyDeviceToHost, st),
+                       "read rsvd judge")) ||
+      (rc = check_cuda(h, cudaStreamSynchronize(st), "randomized SVD")) || (rc = tc_check(h)))
+    return rc;
+  int nagain = 0;
+  for (int p = 0; p < nb; ++p) {
+    if (!on[p]) {
+      bad[p] = 0;
+      continue;
+    }
+    h->stats.rsvd_updates++;
+    h->stats.rsvd_worst_residual = std::max(h->stats.rsvd_worst_residual, worst[p]);
+    if (bad[p]) {
+      ++nagain;
+      h->stats.rsvd_fallbacks++;
+      route[p] = cps[p].m >= cps[p].n ? kPathBidiag : kPathBidiagT;
+    }
+  }
+  if (nagain) {
+    if ((rc = check_cuda(h, cudaMemcpyAsync(R->bad_d, bad.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, st),
+                         "upload rsvd fallback")))
+      return rc;
+    k_rs_restore<<<dim3(256, nb), 256, 0, st>>>(h->slots_d, R->bad_d, ws, per, m_max);
+    TEBD_LAUNCHED(h);
+    if ((rc = check_cuda(h, cudaStreamSynchronize(st), "randomized SVD fallback"))) return rc;
+  }
+  return check_cuda(h, cudaGetLastError(), "randomized SVD");
+}
+
+}  // namespace tebd
+
+using namespace tebd;
+
+extern "C" int tebd_set_rsvd(tebd_handle *h, int oversample, int power_iters, double tol, int slices) {
+  if (!h) return TEBD_ERR_ARG;
+  if (oversample < 0 || power_iters < 0 || power_iters > 4 || !(tol > 0.0 && tol < 1.0) || slices < 3 ||
+      slices > kOzMaxS)
+    return set_error(h, TEBD_ERR_ARG, "rsvd: oversample >= 0, 0 <= power_iters <= 4, 0 < tol < 1, 3 <= slices <= 7");
+  h->rs_oversample = oversample;
+  h->rs_power = power_iters;
+  h->rs_tol = tol;
+  h->rs_slices = slices;
+  return TEBD_OK;
+}

@@ -70,8 +70,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int p = blockIdx.z;
   const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kTcBN;
-  const int mp = b.m_d ? b.m_d[(size_t)p * b.dim_stride] : b.m;
-  const int np = b.n_d ? b.n_d[(size_t)p * b.dim_stride] : b.n;
+  // a problem's own extent, never beyond the batch's (the operands end there)
+  const int mp = b.m_d ? min(b.m_d[(size_t)p * b.dim_stride], b.m) : b.m;
+  const int np = b.n_d ? min(b.n_d[(size_t)p * b.dim_stride], b.n) : b.n;
   if (m0 >= mp || n0 >= 2 * np) return;  // tile outside this problem: uniform over the CTA
   const int nk = b.k_pad / kTcBK;
 
@@ -391,9 +392,14 @@ cudaError_t zprod_run(const ZProd &z, void *ws, int *err_d, cudaStream_t st) {
     const int S = d.planes;
     auto *da = reinterpret_cast<unsigned short *>(pa);
     auto *db = reinterpret_cast<unsigned short *>(pb);
-    if ((e = oz_pack_a(z.a, z.a_stride, z.lda, z.m, z.k, z.a_trans, z.a_conj, z.nprob, d.m_pad, d.k_pad, S, da,
-                       ea, st)) != cudaSuccess ||
-        (e = oz_pack_b(z.b, z.b_stride, z.ldb, z.k, z.n, z.b_trans, z.b_conj, z.nprob, d.n_pad, d.k_pad, S, db,
+    if (z.a_dig) {  // packed by the caller, reused across products
+      da = const_cast<unsigned short *>(z.a_dig);
+      ea = const_cast<int *>(z.a_exp);
+    } else if ((e = oz_pack_a(z.a, z.a_stride, z.lda, z.m, z.k, z.a_trans, z.a_conj, z.nprob, d.m_pad, d.k_pad,
+                              S, da, ea, st)) != cudaSuccess) {
+      return e;
+    }
+    if ((e = oz_pack_b(z.b, z.b_stride, z.ldb, z.k, z.n, z.b_trans, z.b_conj, z.nprob, d.n_pad, d.k_pad, S, db,
                        eb, st)) != cudaSuccess)
       return e;
     OzBatch b = {};

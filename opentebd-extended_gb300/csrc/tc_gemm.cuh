@@ -147,6 +147,10 @@ struct ZProd {
   double alpha;
   const unsigned char *optr;
   int optr_stride;
+  // digit-plane forms: A already packed (oz_pack_a with at least the form's planes,
+  // m_pad = tc_pad(m, 128), k_pad = tc_pad(2 k, 32)) -- A is then not read
+  const unsigned short *a_dig;
+  const int *a_exp;
 };
 inline bool zprod_oz(int form) { return form > 100 && form <= 100 + kOzMaxS; }
 size_t zprod_ws_bytes(const ZProd &z);

@@ -88,8 +88,9 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int p = blockIdx.z;
   const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kOzBN;
-  const int mp = b.m_d ? b.m_d[(size_t)p * b.dim_stride] : b.m;
-  const int np = b.n_d ? b.n_d[(size_t)p * b.dim_stride] : b.n;
+  // a problem's own extent, never beyond the batch's (the operands end there)
+  const int mp = b.m_d ? min(b.m_d[(size_t)p * b.dim_stride], b.m) : b.m;
+  const int np = b.n_d ? min(b.n_d[(size_t)p * b.dim_stride], b.n) : b.n;
   if (m0 >= mp || n0 >= 2 * np) return;  // tile outside this problem: uniform over the CTA
   const int nk = b.k_pad / kOzBK;
   const int nchunks = (nk + kOzChunk - 1) / kOzChunk;

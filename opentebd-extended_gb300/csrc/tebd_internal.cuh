@@ -117,6 +117,7 @@ struct Slot {
 constexpr int kPathQRJ = 0;      // pivoted QR + one-sided Jacobi on R^H (qrj.cu)
 constexpr int kPathBidiag = 1;   // bidiagonalisation + bisection + inverse iteration (bidiag.cu)
 constexpr int kPathBidiagT = 2;  // the same on Theta^H, for a wide compacted Theta (m < n)
+constexpr int kPathRsvd = 3;     // randomized sketch + Rayleigh-Ritz (rsvd.cu), full SVD as fallback
 constexpr int kBidiagMinDim = 64;  // default route switch: min(m, n) of the compacted Theta
 
 }  // namespace tebd
@@ -179,6 +180,13 @@ struct tebd_handle {
   void *tc_ws;             // operand planes / digits, grown on demand
   size_t tc_ws_bytes;
   int *tc_err;             // set by a tensor-core kernel whose pipeline wait expired
+  // randomized SVD route (rsvd.cu, TEBD_SVD_RSVD)
+  void *rs;                // RsState, allocated on first use
+  int rs_oversample;       // sketch columns beyond the kept rank
+  int rs_power;            // power iterations (X^H X applications beyond the first)
+  double rs_tol;           // judge: largest triplet residual / ||Theta||
+  int rs_slices;           // bf16 digit planes of the products (7: FP64 class)
+  int rs_sketch_cap;       // workspace sketch capacity requested so far
 };
 
 namespace tebd {
@@ -227,6 +235,10 @@ int launch_theta_tc(tebd_handle *h, int nb);
 int tc_reserve(tebd_handle *h, size_t bytes);
 int tc_check(tebd_handle *h);  // reads and clears tc_err (synchronises the stream)
 void tc_free(tebd_handle *h);
+// randomized SVD route (rsvd.cu)
+int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vector<int> &route,
+             const std::vector<int> &rank, int sketch);
+void rsvd_free(tebd_handle *h);
 
 }  // namespace tebd
 

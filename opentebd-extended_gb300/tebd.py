@@ -44,6 +44,7 @@ SVD_JACOBI = 2
 SVD_BIDIAG = 3
 SVD_QRJ = 4
 SVD_DF = 5
+SVD_RSVD = 6
 OPTS_VERSION = 1
 
 ERROR_NAMES = {
@@ -69,7 +70,7 @@ EXPORTED_SYMBOLS = (
     "tebd_record_lambdas", "tebd_record_gammas", "tebd_record_labels", "tebd_read_gamma_lambda",
     "tebd_read_gamma_lambda_labels", "tebd_swapping", "tebd_trotter_step_pbc", "tebd_canonical_form_all_nc",
     "tebd_canonical_form", "tebd_canonical_form_all", "tebd_set_conserv", "tebd_set_rank_bound",
-    "tebd_zgemm_tc", "tebd_set_theta_form",
+    "tebd_zgemm_tc", "tebd_set_theta_form", "tebd_set_rsvd",
 )
 
 
@@ -117,6 +118,10 @@ class Stats(ctypes.Structure):
         ("gebrd_flops", ctypes.c_double),
         ("gebrd_ms", ctypes.c_double),
         ("gebrd_launches", ctypes.c_longlong),
+        ("rsvd_updates", ctypes.c_longlong),
+        ("rsvd_fallbacks", ctypes.c_longlong),
+        ("rsvd_flops", ctypes.c_double),
+        ("rsvd_worst_residual", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -181,6 +186,7 @@ def load_library(path: str = LIB_PATH):
     L.tebd_set_conserv.argtypes = [vp, ip]
     L.tebd_set_rank_bound.argtypes = [vp, ctypes.c_double]
     L.tebd_set_theta_form.argtypes = [vp, ctypes.c_int]
+    L.tebd_set_rsvd.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
     L.tebd_canonical_form.argtypes = [vp, ctypes.c_int]
     L.tebd_canonical_form_all.argtypes = [vp]
     cp = ctypes.c_char_p
@@ -246,6 +252,12 @@ class Chain:
         """Theta formation: 0 CUDA cores (default), 3 = 3xTF32 on the tensor cores,
         100 + S = S bf16 digit planes on the tensor cores (S = 7: FP64 class)."""
         self._check(self._lib.tebd_set_theta_form(self.h, int(form)))
+
+    def set_rsvd(self, oversample=64, power_iters=2, tol=1e-5, slices=5):
+        """Randomized route of TEBD_SVD_RSVD: sketch width kept rank + oversample,
+        power iterations, judge tolerance (largest triplet residual / ||Theta||)
+        and the digit planes of its tensor-core products."""
+        self._check(self._lib.tebd_set_rsvd(self.h, int(oversample), int(power_iters), float(tol), int(slices)))
 
     def set_conserv(self, conserv):
         """Internal degrees of freedom for the NC routines: ``conserv`` = Conserv%vi
