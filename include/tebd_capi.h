@@ -205,6 +205,38 @@ int tebd_set_rank_bound(tebd_handle *h, double bound);
  * class).  The learned model may set the sketch per batch instead. */
 int tebd_set_rsvd(tebd_handle *h, int oversample, int power_iters, double tol, int slices);
 
+/* The learned part of the learned-rank form (no reference counterpart): a small
+ * FP32 network, 67 -> 128 -> 128 -> 8 with ReLU, trained on the GPU by the
+ * library's own forward/backward/Adam kernels.  Inputs (per bond, 67 floats):
+ * log10(lambda_k / lambda_0) of the bond's Lambda before the update at ranks
+ * k = floor(j chi / 64), j = 0..63 (floored at -16), then log10 |U - I|_F,
+ * log10 |offdiag(U)|_F (floored at -16) and d / 8 of the gate U.  Outputs (8):
+ * log10(sigma_k / sigma_0) of the normalised Theta at k / chi = 0.75, 1, 1.125,
+ * 1.25, 1.5, 1.75, 2, 2.5.  Samples are stored one after another (x[67 j + i]).
+ * Parameters: one float vector W1 (128 x 67, row-major), b1, W2 (128 x 128), b2,
+ * W3 (8 x 128), b3.  Loss: mean squared error over the outputs.
+ * Attached to a TEBD_SVD_RSVD handle, the model's predictions set, per batch,
+ * the randomized route's oversampling and power count (the cheapest pair whose
+ * predicted (sigma_{r+p} / sigma_r)^(2q+2) is at most `target`) and send bonds
+ * with no such pair straight to the full SVD; the judge still checks every bond
+ * the sketch decomposes. */
+typedef struct tebd_mlp tebd_mlp;
+int tebd_mlp_create(int device, unsigned long long seed, tebd_mlp **out);
+int tebd_mlp_destroy(tebd_mlp *m);
+int tebd_mlp_param_count(void);
+const char *tebd_mlp_last_error(tebd_mlp *m);
+int tebd_mlp_get_params(tebd_mlp *m, float *params);
+int tebd_mlp_set_params(tebd_mlp *m, const float *params);
+/* host buffers; n samples */
+int tebd_mlp_forward(tebd_mlp *m, int n, const float *x, float *y);
+int tebd_mlp_loss_grad(tebd_mlp *m, int n, const float *x, const float *t, double *loss, float *grad);
+/* Adam (lr, beta 0.9 / 0.999, eps 1e-8) over `epochs` passes of minibatches of
+ * `batch` samples in order; *loss: mean minibatch loss of the last epoch */
+int tebd_mlp_train(tebd_mlp *m, int n, const float *x, const float *t, int epochs, int batch, float lr,
+                   double *loss);
+/* attach (m != NULL) or detach the model; target in (0, 1) */
+int tebd_set_rsvd_model(tebd_handle *h, tebd_mlp *m, double target);
+
 /* Theta formation (FormTheta, local_operations_module.f90:184-211) on the tensor
  * cores, dense handles (no counterpart in the reference, which forms Theta in
  * FP64 loops).  form 0: CUDA cores (FP64, or double-float with TEBD_SVD_DF), the
@@ -269,6 +301,7 @@ typedef struct tebd_stats {
   double rsvd_flops;           /* algorithmic flops (8 m n k per complex product) of the
                                   randomized route's tensor-core products                 */
   double rsvd_worst_residual;  /* largest triplet residual / ||Theta|| the judge saw        */
+  long long rsvd_skipped;      /* bonds the learned model sent straight to the full SVD     */
 } tebd_stats;
 int tebd_set_profiling(tebd_handle *h, int on);
 int tebd_get_stats(tebd_handle *h, tebd_stats *stats);

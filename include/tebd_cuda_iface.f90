@@ -21,6 +21,7 @@ TYPE, BIND(C) :: tebd_stats
   INTEGER(C_LONG_LONG) :: gebrd_launches
   INTEGER(C_LONG_LONG) :: rsvd_updates, rsvd_fallbacks
   REAL(C_DOUBLE) :: rsvd_flops, rsvd_worst_residual
+  INTEGER(C_LONG_LONG) :: rsvd_skipped
 END TYPE
 INTERFACE
   SUBROUTINE tebd_default_opts(o) BIND(C, NAME='tebd_default_opts')
@@ -296,6 +297,59 @@ INTERFACE
     TYPE(C_PTR), VALUE :: h
     INTEGER(C_INT), VALUE :: oversample, power_iters, slices
     REAL(C_DOUBLE), VALUE :: tol
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_mlp_create(device, seed, m) BIND(C, NAME='tebd_mlp_create')
+    IMPORT :: C_INT, C_LONG_LONG, C_PTR
+    INTEGER(C_INT), VALUE :: device
+    INTEGER(C_LONG_LONG), VALUE :: seed
+    TYPE(C_PTR) :: m
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_mlp_destroy(m) BIND(C, NAME='tebd_mlp_destroy')
+    IMPORT :: C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: m
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_mlp_param_count() BIND(C, NAME='tebd_mlp_param_count')
+    IMPORT :: C_INT
+  END FUNCTION
+  TYPE(C_PTR) FUNCTION tebd_mlp_last_error(m) BIND(C, NAME='tebd_mlp_last_error')
+    IMPORT :: C_PTR
+    TYPE(C_PTR), VALUE :: m
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_mlp_get_params(m, params) BIND(C, NAME='tebd_mlp_get_params')
+    IMPORT :: C_FLOAT, C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: m
+    REAL(C_FLOAT) :: params(*)
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_mlp_set_params(m, params) BIND(C, NAME='tebd_mlp_set_params')
+    IMPORT :: C_FLOAT, C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: m
+    REAL(C_FLOAT) :: params(*)
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_mlp_forward(m, n, x, y) BIND(C, NAME='tebd_mlp_forward')
+    IMPORT :: C_FLOAT, C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: m
+    INTEGER(C_INT), VALUE :: n
+    REAL(C_FLOAT) :: x(*), y(*)
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_mlp_loss_grad(m, n, x, t, loss, grad) BIND(C, NAME='tebd_mlp_loss_grad')
+    IMPORT :: C_DOUBLE, C_FLOAT, C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: m
+    INTEGER(C_INT), VALUE :: n
+    REAL(C_FLOAT) :: x(*), t(*), grad(*)
+    REAL(C_DOUBLE) :: loss
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_mlp_train(m, n, x, t, epochs, batch, lr, loss) BIND(C, NAME='tebd_mlp_train')
+    IMPORT :: C_DOUBLE, C_FLOAT, C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: m
+    INTEGER(C_INT), VALUE :: n, epochs, batch
+    REAL(C_FLOAT) :: x(*), t(*)
+    REAL(C_FLOAT), VALUE :: lr
+    REAL(C_DOUBLE) :: loss
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_set_rsvd_model(h, m, target) BIND(C, NAME='tebd_set_rsvd_model')
+    IMPORT :: C_DOUBLE, C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: h, m
+    REAL(C_DOUBLE), VALUE :: target
   END FUNCTION
 END INTERFACE
 END MODULE tebd_cuda_iface

@@ -5,7 +5,7 @@ The directory name is not a Python identifier; load it with
 """
 from . import hamiltonians  # noqa: F401
 from .tebd import (  # noqa: F401
-    Chain, TebdError, TrotterStep, TwoSiteOp, TwoSiteOpNC, load_library,
+    Chain, Mlp, TebdError, TrotterStep, TwoSiteOp, TwoSiteOpNC, load_library,
     OneSiteExpVal, TotalEnergy, LocalEnergy, InnerProduct, ChainEntropy,
     MODE_DENSE, MODE_NC, SVD_FP64, SVD_JACOBI, SVD_BIDIAG, SVD_QRJ, SVD_DF, SVD_RSVD, EXPORTED_SYMBOLS, measure_fp64_peak,
 )

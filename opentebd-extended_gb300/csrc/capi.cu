@@ -415,6 +415,69 @@ extern "C" int tebd_get_sweeps(tebd_handle *h, int link, int *sweeps) {
               "get sweeps");
 }
 
+// The learned model's choice for the randomized route of one batch: per bond
+// the predicted log10 sigma_k / sigma_0 at k / chi = kMlpRanks (interpolated
+// linearly, extended past the last point along its last segment); a pair (p, q)
+// is feasible for a bond when (2q + 2) log10(sigma_{chi+p} / sigma_chi) <=
+// log10(target), and costs (chi + p)(2q + 4) -- the sketch's product columns over
+// its passes.  Each bond takes its cheapest feasible pair; bonds with none take
+// the full SVD (allow = 0); the batch runs with the largest p and q chosen.
+static int rsvd_model_choice(tebd_handle *h, int nb, const double *const *gates, int *over, int *power,
+                             std::vector<char> &allow) {
+  const int d2 = h->d * h->d;
+  std::vector<float> gt(3 * (size_t)nb), pred((size_t)kMlpOut * nb);
+  for (int s = 0; s < nb; ++s) {
+    const double *g = gates[s];
+    double off = 0.0, dev = 0.0;
+    for (int c = 0; c < d2; ++c)
+      for (int r = 0; r < d2; ++r) {
+        const double re = g[2 * (r + (size_t)d2 * c)], im = g[2 * (r + (size_t)d2 * c) + 1];
+        const double a2 = re * re + im * im;
+        if (r != c) off += a2;
+        dev += r == c ? (re - 1.0) * (re - 1.0) + im * im : a2;
+      }
+    gt[3 * s] = (float)(dev > 0.0 ? std::max(-16.0, 0.5 * log10(dev)) : -16.0);
+    gt[3 * s + 1] = (float)(off > 0.0 ? std::max(-16.0, 0.5 * log10(off)) : -16.0);
+    gt[3 * s + 2] = (float)h->d / 8.f;
+  }
+  int rc = mlp_features_forward(h->rs_model, h->lam, h->links_d, gt.data(), h->chi, nb, h->stream, pred.data());
+  if (rc) return set_error(h, rc, std::string("rsvd model: ") + tebd_mlp_last_error(h->rs_model));
+  auto at = [&](const float *y, double rho) {
+    int j = 0;
+    while (j < kMlpOut - 2 && rho > kMlpRanks[j + 1]) ++j;
+    const double t = (rho - kMlpRanks[j]) / (kMlpRanks[j + 1] - kMlpRanks[j]);
+    return (double)y[j] + t * ((double)y[j + 1] - (double)y[j]);
+  };
+  static const int kP[] = {16, 32, 48, 64, 96, 128};
+  const double lt = log10(h->rs_target);
+  int pmax = 0, qmax = 0;
+  for (int s = 0; s < nb; ++s) {
+    const float *y = pred.data() + (size_t)kMlpOut * s;
+    const double y1 = at(y, 1.0);
+    double best = 1e300;
+    int bp = -1, bq = -1;
+    for (int p : kP)
+      for (int q = 0; q <= 3; ++q) {
+        const double lr = at(y, (double)(h->chi + p) / h->chi) - y1;
+        if (!(lr < 0.0) || (2.0 * q + 2.0) * lr > lt) continue;
+        const double cost = (double)(h->chi + p) * (2 * q + 4);
+        if (cost < best) {
+          best = cost;
+          bp = p;
+          bq = q;
+        }
+      }
+    allow[s] = bp >= 0;
+    if (bp >= 0) {
+      pmax = std::max(pmax, bp);
+      qmax = std::max(qmax, bq);
+    }
+  }
+  *over = pmax ? pmax : h->rs_oversample;
+  *power = pmax ? qmax : h->rs_power;
+  return TEBD_OK;
+}
+
 // One batch of at most nslots non-overlapping bonds (complex gates).
 static int run_batch(tebd_handle *h, int nb, const int *links, const double *const *gates,
                      double *truncerr) {
@@ -453,15 +516,20 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
       std::vector<int> rank(nb, 0);
       int nrs = 0;
       if (h->opts.svd_mode == TEBD_SVD_RSVD && !h->unnormalized) {
-        const int sketch = h->chi + h->rs_oversample;
+        int over = h->rs_oversample, power = h->rs_power;
+        std::vector<char> allow(nb, 1);
+        if (h->rs_model && (rc = rsvd_model_choice(h, nb, gates, &over, &power, allow))) return rc;
+        const int sketch = h->chi + over;
         for (int s = 0; s < nb; ++s) {
           const int mn = std::min(cps[s].m, cps[s].n);
           rank[s] = std::min(h->chi, mn);
-          h->path_h[s] = (mn >= sketch + 16 && std::max(cps[s].m, cps[s].n) <= kBidiagMaxDim) ? kPathRsvd
-                                                                                            : kPathQRJ;
+          h->path_h[s] = (allow[s] && mn >= sketch + 16 && std::max(cps[s].m, cps[s].n) <= kBidiagMaxDim)
+                             ? kPathRsvd
+                             : kPathQRJ;
           nrs += h->path_h[s] == kPathRsvd;
         }
-        if (nrs && (rc = run_rsvd(h, nb, cps, h->path_h, rank, sketch))) return rc;
+        h->stats.rsvd_skipped += std::count(allow.begin(), allow.end(), 0);
+        if (nrs && (rc = run_rsvd(h, nb, cps, h->path_h, rank, sketch, power))) return rc;
       }
       for (int s = 0; s < nb; ++s) {
         if (nrs && h->path_h[s] != kPathQRJ) {  // randomized route, or its fallback to the full SVD

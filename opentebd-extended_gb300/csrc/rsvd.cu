@@ -398,7 +398,7 @@ static int rs_gram_svd(tebd_handle *h, RsState *R, const std::vector<int> &on, i
 // accepted bonds and the full route (kPathBidiag / kPathBidiagT) for the bonds
 // the judge sent back, whose Theta is back in the slot's X.
 int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vector<int> &route,
-             const std::vector<int> &rank, int sketch) {
+             const std::vector<int> &rank, int sketch, int power) {
   int m_max = 0, n_max = 0, r_max = 0, s = 0;
   std::vector<RsDims> dims(nb, RsDims{0, 0, 0, 0});
   std::vector<int> on(nb, 0);
@@ -502,7 +502,7 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
   if ((rc = prod(c.xp, m_max, 0, nullptr, pstr, 0, R->n_full, R->om, 0, m_max, s, n_max, c.a, sk)) ||
       (rc = cholqr2(c.a, c.b, m_max, sk)))
     return rc;
-  for (int it = 0; it < h->rs_power; ++it)
+  for (int it = 0; it < power; ++it)
     if ((rc = prod(c.xp, m_max, 1, nullptr, pstr, c.a, m_max, nullptr, pstr, n_max, s, m_max, c.z, sk)) ||
         (rc = cholqr2(c.z, c.b, n_max, sk)) ||
         (rc = prod(c.xp, m_max, 0, nullptr, pstr, c.z, n_max, nullptr, pstr, m_max, s, n_max, c.a, sk)) ||

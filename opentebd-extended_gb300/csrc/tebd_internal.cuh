@@ -120,6 +120,10 @@ constexpr int kPathBidiagT = 2;  // the same on Theta^H, for a wide compacted Th
 constexpr int kPathRsvd = 3;     // randomized sketch + Rayleigh-Ritz (rsvd.cu), full SVD as fallback
 constexpr int kBidiagMinDim = 64;  // default route switch: min(m, n) of the compacted Theta
 
+// learned model (mlp.cu): sizes and the relative ranks k / chi of its outputs
+constexpr int kMlpIn = 67, kMlpHidden = 128, kMlpOut = 8;
+extern const double kMlpRanks[kMlpOut];
+
 }  // namespace tebd
 
 struct tebd_handle {
@@ -187,6 +191,8 @@ struct tebd_handle {
   double rs_tol;           // judge: largest triplet residual / ||Theta||
   int rs_slices;           // bf16 digit planes of the products (7: FP64 class)
   int rs_sketch_cap;       // workspace sketch capacity requested so far
+  tebd_mlp *rs_model;      // learned model choosing the sketch per batch (mlp.cu), or null
+  double rs_target;        // the model's bound on (sigma_{r+p} / sigma_r)^(2q+2)
 };
 
 namespace tebd {
@@ -237,8 +243,12 @@ int tc_check(tebd_handle *h);  // reads and clears tc_err (synchronises the stre
 void tc_free(tebd_handle *h);
 // randomized SVD route (rsvd.cu)
 int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vector<int> &route,
-             const std::vector<int> &rank, int sketch);
+             const std::vector<int> &rank, int sketch, int power);
 void rsvd_free(tebd_handle *h);
+// model inference for the bonds of a batch: features from Lambda(link) on the
+// device and 3 host gate terms per bond; kMlpOut predictions per bond to the host
+int mlp_features_forward(tebd_mlp *M, const double *lam, const int *links, const float *gate_terms_host, int chi,
+                         int nb, cudaStream_t st, float *out_host);
 
 }  // namespace tebd
 

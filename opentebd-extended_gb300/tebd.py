@@ -71,6 +71,8 @@ EXPORTED_SYMBOLS = (
     "tebd_read_gamma_lambda_labels", "tebd_swapping", "tebd_trotter_step_pbc", "tebd_canonical_form_all_nc",
     "tebd_canonical_form", "tebd_canonical_form_all", "tebd_set_conserv", "tebd_set_rank_bound",
     "tebd_zgemm_tc", "tebd_set_theta_form", "tebd_set_rsvd",
+    "tebd_mlp_create", "tebd_mlp_destroy", "tebd_mlp_param_count", "tebd_mlp_last_error", "tebd_mlp_get_params",
+    "tebd_mlp_set_params", "tebd_mlp_forward", "tebd_mlp_loss_grad", "tebd_mlp_train", "tebd_set_rsvd_model",
 )
 
 
@@ -122,6 +124,7 @@ class Stats(ctypes.Structure):
         ("rsvd_fallbacks", ctypes.c_longlong),
         ("rsvd_flops", ctypes.c_double),
         ("rsvd_worst_residual", ctypes.c_double),
+        ("rsvd_skipped", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -187,6 +190,18 @@ def load_library(path: str = LIB_PATH):
     L.tebd_set_rank_bound.argtypes = [vp, ctypes.c_double]
     L.tebd_set_theta_form.argtypes = [vp, ctypes.c_int]
     L.tebd_set_rsvd.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.tebd_mlp_create.argtypes = [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(vp)]
+    L.tebd_mlp_destroy.argtypes = [vp]
+    L.tebd_mlp_param_count.argtypes = []
+    L.tebd_mlp_last_error.argtypes = [vp]
+    L.tebd_mlp_last_error.restype = ctypes.c_char_p
+    L.tebd_mlp_get_params.argtypes = [vp, fp]
+    L.tebd_mlp_set_params.argtypes = [vp, fp]
+    L.tebd_mlp_forward.argtypes = [vp, ctypes.c_int, fp, fp]
+    L.tebd_mlp_loss_grad.argtypes = [vp, ctypes.c_int, fp, fp, dp, fp]
+    L.tebd_mlp_train.argtypes = [vp, ctypes.c_int, fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_float, dp]
+    L.tebd_set_rsvd_model.argtypes = [vp, vp, ctypes.c_double]
     L.tebd_canonical_form.argtypes = [vp, ctypes.c_int]
     L.tebd_canonical_form_all.argtypes = [vp]
     cp = ctypes.c_char_p
@@ -258,6 +273,12 @@ class Chain:
         power iterations, judge tolerance (largest triplet residual / ||Theta||)
         and the digit planes of its tensor-core products."""
         self._check(self._lib.tebd_set_rsvd(self.h, int(oversample), int(power_iters), float(tol), int(slices)))
+
+    def set_rsvd_model(self, model, target=1e-6):
+        """Attach a trained Mlp (None detaches): per batch it sets the randomized
+        route's oversampling and power count, or sends bonds to the full SVD."""
+        self._check(self._lib.tebd_set_rsvd_model(self.h, model.h if model is not None else None, float(target)))
+        self._model = model  # keep it alive while attached
 
     def set_conserv(self, conserv):
         """Internal degrees of freedom for the NC routines: ``conserv`` = Conserv%vi
@@ -586,3 +607,72 @@ def InnerProduct(chain_left: Chain, chain_right: Chain) -> complex:
 def ChainEntropy(link, chain: Chain) -> float:
     """ChainEntropy(link, Lambdas)."""
     return float(chain.chain_entropy()[link - 1])
+
+
+class Mlp:
+    """The learned model of the randomized route (tebd_mlp_*): 67 -> 128 -> 128 -> 8,
+    FP32, trained on the GPU by the library's kernels.  x: (n, 67), targets (n, 8)."""
+
+    N_IN, N_OUT = 67, 8
+
+    def __init__(self, device=0, seed=0):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self._lib.tebd_mlp_create(device, seed, ctypes.byref(h))
+        if rc != TEBD_OK:
+            raise TebdError(rc, "tebd_mlp_create failed")
+        self.h = h
+        self.n_params = self._lib.tebd_mlp_param_count()
+
+    def _check(self, rc):
+        if rc != TEBD_OK:
+            raise TebdError(rc, self._lib.tebd_mlp_last_error(self.h).decode())
+
+    @staticmethod
+    def _f(a, cols):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        if a.ndim != 2 or a.shape[1] != cols:
+            raise ValueError("expected (n, %d) array" % cols)
+        return a
+
+    def params(self):
+        p = np.zeros(self.n_params, np.float32)
+        self._check(self._lib.tebd_mlp_get_params(self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        self._check(self._lib.tebd_mlp_set_params(self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def forward(self, x):
+        x = self._f(x, self.N_IN)
+        y = np.zeros((len(x), self.N_OUT), np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        self._check(self._lib.tebd_mlp_forward(self.h, len(x), x.ctypes.data_as(fp), y.ctypes.data_as(fp)))
+        return y
+
+    def loss_grad(self, x, t):
+        x, t = self._f(x, self.N_IN), self._f(t, self.N_OUT)
+        g = np.zeros(self.n_params, np.float32)
+        loss = ctypes.c_double(0.0)
+        fp = ctypes.POINTER(ctypes.c_float)
+        self._check(self._lib.tebd_mlp_loss_grad(self.h, len(x), x.ctypes.data_as(fp), t.ctypes.data_as(fp),
+                                                 ctypes.byref(loss), g.ctypes.data_as(fp)))
+        return loss.value, g
+
+    def train(self, x, t, epochs=200, batch=256, lr=1e-3):
+        x, t = self._f(x, self.N_IN), self._f(t, self.N_OUT)
+        loss = ctypes.c_double(0.0)
+        fp = ctypes.POINTER(ctypes.c_float)
+        self._check(self._lib.tebd_mlp_train(self.h, len(x), x.ctypes.data_as(fp), t.ctypes.data_as(fp), epochs,
+                                             batch, float(lr), ctypes.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.tebd_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -1,0 +1,127 @@
+"""The learned part of the learned-rank form: the model's hand-written kernels
+against the CPU oracle, its training on spectra the method produces, and what it
+gains the randomized route.
+
+* forward and gradient (tebd_mlp_forward / tebd_mlp_loss_grad, FP32 on the GPU)
+  against oracle/mlp_oracle.py (float64): outputs within 1e-4 relative, loss
+  within 1e-5 relative, gradient within 1e-3 relative in norm and per element
+  within 1e-3 of the largest gradient entry;
+* training (tebd_mlp_train, Adam) on logged spectra lowers the loss tenfold and
+  predicts held-out spectra (log10 of singular-value ratios) better than their
+  mean;
+* A/B: the same Trotter steps of a saturated Bose-Hubbard chain through the
+  randomized route with the fixed sketch (p = 64, q = 2) and with a trained model
+  choosing it: the model's run spends fewer tensor-core flops on the sketch, and
+  both agree with the plain FP64 route on every two-site density matrix within
+  1e-8.
+"""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as MO
+from oracle import observables as obs
+
+pytestmark = pytest.mark.gpu
+
+
+def _rand(seed, n):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((n, MO.N_IN)).astype(np.float32)
+    t = rng.standard_normal((n, MO.N_OUT)).astype(np.float32)
+    p = (0.2 * rng.standard_normal(MO.N_PARAMS)).astype(np.float32)
+    return x, t, p
+
+
+def test_mlp_forward_matches_cpu_oracle(pkg):
+    x, _, p = _rand(1, 257)
+    m = pkg.Mlp(seed=3)
+    m.set_params(p)
+    y = m.forward(x)
+    yr, _ = MO.forward(p, x)
+    assert np.max(np.abs(y - yr)) <= 1e-4 * max(1.0, np.max(np.abs(yr)))
+    m.close()
+
+
+def test_mlp_gradient_matches_cpu_oracle(pkg):
+    x, t, p = _rand(2, 300)
+    m = pkg.Mlp(seed=4)
+    m.set_params(p)
+    loss, g = m.loss_grad(x, t)
+    lr, gr = MO.loss_grad(p, x, t)
+    assert abs(loss - lr) <= 1e-5 * lr
+    assert np.linalg.norm(g - gr) <= 1e-3 * np.linalg.norm(gr)
+    assert np.max(np.abs(g - gr)) <= 1e-3 * np.max(np.abs(gr))
+    m.close()
+
+
+def _bh_chain(pkg, L, d, chi, seed):
+    H = pkg.hamiltonians
+    carray = np.zeros((d, L), complex)
+    carray[1, :] = 1.0
+    gam, lam = H.perturbed_product_state(carray, chi, 1e-3, seed)
+    return gam, lam
+
+
+def _logged(pkg, seeds, L=12, d=5, chi=24, dt=0.05, steps=25):
+    from importlib import import_module
+
+    learned = import_module(pkg.__name__ + ".learned")
+    H = pkg.hamiltonians
+    gates = H.construct_propagators(H.bose_hubbard(L, d, 1.0, 2.0), dt, 2)
+    xs, ts = [], []
+    for s in seeds:
+        gam, lam = _bh_chain(pkg, L, d, chi, s)
+        x, t = learned.log_run(pkg, gam, lam, gates, steps)
+        xs.append(x)
+        ts.append(t)
+    return np.concatenate(xs), np.concatenate(ts)
+
+
+def test_mlp_training_on_logged_spectra(pkg):
+    x, t = _logged(pkg, [11, 12])
+    xv, tv = _logged(pkg, [13])
+    assert len(x) > 100 and len(xv) > 20
+    m = pkg.Mlp(seed=5)
+    l0, _ = m.loss_grad(x, t)
+    loss = m.train(x, t, epochs=300, batch=128, lr=2e-3)
+    assert loss < 0.1 * l0, (loss, l0)
+    err_model = np.mean((m.forward(xv) - tv) ** 2)
+    err_mean = np.mean((t.mean(0) - tv) ** 2)
+    assert err_model < err_mean, (err_model, err_mean)
+    m.close()
+
+
+def test_learned_model_gains_over_fixed_sketch(pkg):
+    H = pkg.hamiltonians
+    x, t = _logged(pkg, [21, 22], L=12, d=5, chi=48, steps=30)
+    m = pkg.Mlp(seed=6)
+    m.train(x, t, epochs=300, batch=128, lr=2e-3)
+    L, d, chi, dt = 12, 5, 48, 0.05
+    gates = H.construct_propagators(H.bose_hubbard(L, d, 1.0, 2.0), dt, 2)
+    gam, lam = _bh_chain(pkg, L, d, chi, 23)
+    with pkg.Chain(L, d, chi) as c:  # to saturation in plain FP64
+        c.set_state(gam, lam)
+        for _ in range(30):
+            c.trotter_step(gates, 2)
+        gam, lam = c.get_state()
+    res = {}
+    for name, mode, model in (("fp64", pkg.SVD_FP64, None), ("fixed", pkg.SVD_RSVD, None),
+                              ("model", pkg.SVD_RSVD, m)):
+        with pkg.Chain(L, d, chi, svd_mode=mode) as c:
+            c.set_state(gam, lam)
+            if model is not None:
+                c.set_rsvd_model(model, 1e-6)
+            for _ in range(3):
+                c.trotter_step(gates, 2)
+            res[name] = (c.get_state(), c.stats())
+    (g0, l0), _ = res["fp64"]
+    for name in ("fixed", "model"):
+        (g1, l1), st = res[name]
+        for k in range(1, L):
+            a = obs.two_site_rho(l0[k - 1], g0[k - 1], l0[k], g0[k], l0[k + 1])
+            b = obs.two_site_rho(l1[k - 1], g1[k - 1], l1[k], g1[k], l1[k + 1])
+            assert np.max(np.abs(a - b)) < 1e-8, (name, k)
+    fixed, model = res["fixed"][1], res["model"][1]
+    assert fixed["rsvd_updates"] > 0
+    assert model["rsvd_flops"] < fixed["rsvd_flops"], (model["rsvd_flops"], fixed["rsvd_flops"])
+    m.close()
