@@ -245,6 +245,108 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# the mixed form's trained model and the saturated-bond legs
+# ---------------------------------------------------------------------------
+MODEL_PATH = os.path.join(ROOT, "opentebd-extended_gb300", "data", "rsvd_model.npz")
+MODEL_TARGET = 1e-8
+
+
+def load_model(pkg, device):
+    """The randomized route's model trained by the package's learned.py on spectra
+    of the method's own runs (the parameters committed beside it)."""
+    m = pkg.Mlp(device=device)
+    m.set_params(np.load(MODEL_PATH)["params"])
+    return m
+
+
+def measured_peak(key):
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))[key]), "MEASURED_PEAKS.json " + key
+    except (OSError, ValueError, KeyError, TypeError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}[key], "fallback figure (no MEASURED_PEAKS.json)"
+
+
+def saturated_state(H):
+    """Every Lambda full (lambda_k ~ exp(-k/16), normalised) and complex Gaussian
+    Gammas (seed 5): each odd bond of the L=64, d=5, chi=128 chain has a full
+    640 x 640 Theta -- the cost regime of the configured run after step ~50."""
+    rng = np.random.default_rng(5)
+    gam = [np.asfortranarray(rng.standard_normal((CHI, D, CHI)) + 1j * rng.standard_normal((CHI, D, CHI)))
+           for _ in range(L)]
+    lam = []
+    for _ in range(L + 1):
+        l = np.exp(-np.arange(CHI) / 16.0)
+        lam.append(l / np.linalg.norm(l))
+    return gam, lam
+
+
+def saturated_legs(pkg, device, args, fp64_peak, steps=3):
+    """The 32 odd bonds of the saturated chain, updated `steps` times (one batched
+    sweep each), in plain FP64 and in the mixed form, profiled: updates/s from CUDA
+    events on each chain's stream, and the roofline of each form's dominant kernel
+    from that leg's own launch timings (k_gebrd on the FP64 pipe; the tensor-core
+    product kernels against the measured bf16 peak)."""
+    import torch
+
+    H = pkg.hamiltonians
+    gam, lam = saturated_state(H)
+    gate = H.matrix_exponential(H.bose_hubbard(L, D, J, U, MU)[1], DT)
+    links = list(range(1, L, 2))
+    bf16_peak, bf16_src = measured_peak("bf16_tflops")
+    out = {"workload": "saturated_bonds_L64_d5_chi128 (32 bonds of a 640 x 640 Theta per step)", "steps": steps}
+    finals = {}
+    for name in ("fp64", "mixed"):
+        c = pkg.Chain(L, D, CHI, device=device, svd_mode=SVD_MODES["fp64" if name == "fp64" else "rsvd"])
+        model = None
+        if name == "mixed":
+            c.set_theta_form(107)
+            model = load_model(pkg, device)
+            c.set_rsvd_model(model, MODEL_TARGET)
+        c.set_state(gam, lam)
+        st_ = torch.cuda.ExternalStream(c.stream(), device=device)
+        c.apply_bonds(links, [gate] * len(links))  # warm-up (workspaces, kernels)
+        c.set_state(gam, lam)
+        c.reset_stats()
+        c.set_profiling(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st_)
+        for _ in range(steps):
+            c.apply_bonds(links, [gate] * len(links))
+        e1.record(st_)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        st = c.stats()
+        finals[name] = [c.two_site_rho(k) for k in links]  # device observable of each updated bond
+        leg_ = {"ms_per_step": ms / steps, "value": len(links) * steps / (ms / 1e3), "unit": "updates/s"}
+        if st["gebrd_ms"] > 0:
+            a = st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12
+            leg_["roofline_k_gebrd"] = {"bound": "fp64", "achieved": a, "peak": fp64_peak, "unit": "TFLOP/s",
+                                        "frac": a / fp64_peak, "share_of_leg": st["gebrd_ms"] / ms,
+                                        "algorithmic": "16 M N^2 - 16 N^3/3 per bidiagonalised matrix"}
+        if st["tc_ms"] > 0:
+            a = st["tc_mma_flops"] / (st["tc_ms"] / 1e3) / 1e12
+            leg_["roofline_tensor_products"] = {
+                "kernels": "k_tc_oz (bf16 digit-plane products)", "bound": "tensor", "achieved": a,
+                "peak": bf16_peak, "unit": "TFLOP/s", "frac": a / bf16_peak, "peak_source": bf16_src,
+                "launches": st["tc_launches"], "avg_launch_ms": st["tc_ms"] / max(1, st["tc_launches"]),
+                "share_of_leg": st["tc_ms"] / ms,
+                "algorithmic": "digit pairs x 2 x m_pad x n_pad x k_pad per product (bf16 multiply-adds issued)",
+                "fp64_class_flops_per_s": st["rsvd_flops"] / (st["tc_ms"] / 1e3) / 1e12}
+            leg_["rsvd"] = {"updates": st["rsvd_updates"], "fallbacks": st["rsvd_fallbacks"],
+                            "skipped_by_model": st["rsvd_skipped"], "worst_residual": st["rsvd_worst_residual"]}
+        out[name] = leg_
+        c.close()
+        if model is not None:
+            model.close()
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    out["max_abs_err_rho2_vs_fp64"] = float(max(np.max(np.abs(a - b)) for a, b in zip(finals["fp64"],
+                                                                                         finals["mixed"])))
+    return out
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_ours(args):
@@ -344,18 +446,25 @@ def run_ours(args):
     Hb = H.bose_hubbard(L, D, J, U, MU)
     ref_obs = (chain.one_site_expval(num), chain.local_energy(Hb), chain.chain_entropy())
 
-    def leg(svd_mode, bound=0.0):
+    def leg(svd_mode, bound=0.0, mixed=False):
         """The same K steps from the initial state on a second chain: updates/s from
         CUDA events on its stream, and final-state observable errors against the
-        plain FP64 run."""
+        plain FP64 run.  mixed: the mixed form (Theta in 7 digit planes on the
+        tensor cores, the trained model on the randomized route), profiled."""
         pc = pkg.Chain(L, D, CHI, device=local, svd_mode=svd_mode)
         pc.set_rank_bound(bound)
+        model = None
+        if mixed:
+            pc.set_theta_form(107)
+            model = load_model(pkg, local)
+            pc.set_rsvd_model(model, MODEL_TARGET)
         pc.set_state(gam, lam)
         for _ in range(args.warmup):
             pc.trotter_step(Udt, ORDER)
         pc.set_state(gam, lam)
         pstream = torch.cuda.ExternalStream(pc.stream(), device=local)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pc.reset_stats()
         barrier()
         e0.record(pstream)
         te = 0.0
@@ -364,23 +473,37 @@ def run_ours(args):
         e1.record(pstream)
         barrier()
         pms = maxall(e0.elapsed_time(e1))
+        pst = pc.stats()
         o = (pc.one_site_expval(num), pc.local_energy(Hb), pc.chain_entropy())
         ranks = [int(np.sum(x > 0)) for x in pc.get_state()[1][1:-1]]
         pc.close()
+        if model is not None:
+            model.close()
         pv = whole_job_rate(world, UPDATES_PER_STEP * args.steps, pms)
         err = {"n_i": float(np.max(np.abs(o[0] - ref_obs[0]))),
                "bond_energy": float(np.max(np.abs(o[1] - ref_obs[1]))),
                "entropy": float(np.max(np.abs(o[2] - ref_obs[2])))}
-        return {"value": pv, "unit": "updates/s", "ms_per_step": pms / args.steps,
-                "speedup_vs_plain_fp64": pv / value, "max_abs_err_vs_plain_fp64": err,
-                "within_error_bound": max(err.values()) <= 1e-8, "error_bound": 1e-8,
-                "total_truncerr": te, "final_mean_rank": float(np.mean(ranks))}
+        out = {"value": pv, "unit": "updates/s", "ms_per_step": pms / args.steps,
+               "speedup_vs_plain_fp64": pv / value, "max_abs_err_vs_plain_fp64": err,
+               "within_error_bound": max(err.values()) <= 1e-8, "error_bound": 1e-8,
+               "total_truncerr": te, "final_mean_rank": float(np.mean(ranks))}
+        if svd_mode == SVD_MODES["rsvd"]:
+            out["rsvd"] = {"updates": pst["rsvd_updates"], "fallbacks": pst["rsvd_fallbacks"],
+                           "skipped_by_model": pst["rsvd_skipped"], "worst_residual": pst["rsvd_worst_residual"]}
+        return out
 
     prec = None
     if args.svd == "fp64" and not args.no_precision:
         prec = {"svd": "TEBD_SVD_DF: bidiagonal route's trailing-matrix passes, trailing updates and "
                        "back-transformation in double-float on the FP32 pipe; the rest FP64"}
         prec.update(leg(SVD_MODES["df"]))
+    mixed = None
+    if args.svd == "fp64" and not args.no_precision:
+        mixed = {"form": "TEBD_SVD_RSVD + tebd_set_theta_form(107) + trained model (target %g): Theta and the "
+                         "randomized route's products on the tensor cores (bf16 digit planes, FP64 class), FP64 "
+                         "Cholesky / s x s SVD, full FP64 SVD for the bonds the model or the judge sends "
+                         "back" % MODEL_TARGET}
+        mixed.update(leg(SVD_MODES["rsvd"], mixed=True))
     rank_form = None
     if args.svd == "fp64" and args.rank_bound:
         rank_form = []
@@ -449,6 +572,8 @@ def run_ours(args):
                                      os.path.join(ROOT, "MEASURED_PEAKS.json")),
         "cpu_baseline": cpu,
         "precision_form": prec,
+        "mixed_form": mixed,
+        "saturated": saturated_legs(pkg, local, args, fp64_peak) if not args.no_precision else None,
         **({"rank_form": {"what": "kept-rank form: per-update discarded-weight bound "
                                   "(tebd_set_rank_bound), Lambda beyond the kept rank exactly zero",
                           "legs": rank_form}} if rank_form else {}),

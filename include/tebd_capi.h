@@ -85,9 +85,9 @@ extern "C" {
                                      much larger than the kept rank r take a randomized
                                      sketch of width r + p with FP64-class products on
                                      the tensor cores and a Rayleigh-Ritz SVD (FP64);
-                                     the full SVD of TEBD_SVD_FP64 is the fallback when
-                                     a kept triplet's residual exceeds the tolerance
-                                     (tebd_set_rsvd); the other bonds as TEBD_SVD_FP64 */
+                                     the full SVD is the fallback when a kept triplet's
+                                     residual exceeds the tolerance (tebd_set_rsvd); the
+                                     fallback and the other bonds as TEBD_SVD_DF         */
 
 #define TEBD_OPTS_VERSION 1
 
@@ -200,9 +200,13 @@ int tebd_set_rank_bound(tebd_handle *h, double bound);
  * rho = |Theta^H u - sigma v| is at most tol * ||Theta|| (default 1e-5), else its
  * full SVD is computed -- an accepted triplet's singular value is then within
  * ~rho^2 / gap and its vectors within ~rho / gap of the exact ones; slices: bf16
- * digit planes of the range finder's tensor-core products (3..7, default 5, ~2^-35:
- * a subspace needs no more); the Rayleigh-Ritz products always use 7 (FP64
- * class).  The learned model may set the sketch per batch instead. */
+ * digit planes of the range finder's tensor-core products (3..7, default 7, FP64
+ * class); the Rayleigh-Ritz products always use 7.  The route takes only
+ * saturated bonds (all chi Schmidt values of the bond in use, spanning at most
+ * six decades: the sketch is orthonormalised through Gram matrices, which
+ * resolve directions down to ~1e-7 of the largest) with a compacted Theta at
+ * least chi + p + 16 on its smaller side.  The learned model may set the sketch
+ * per batch instead. */
 int tebd_set_rsvd(tebd_handle *h, int oversample, int power_iters, double tol, int slices);
 
 /* The learned part of the learned-rank form (no reference counterpart): a small
@@ -302,6 +306,11 @@ typedef struct tebd_stats {
                                   randomized route's tensor-core products                 */
   double rsvd_worst_residual;  /* largest triplet residual / ||Theta|| the judge saw        */
   long long rsvd_skipped;      /* bonds the learned model sent straight to the full SVD     */
+  double tc_ms;                /* device time of the tensor-core product kernels (profiling on;
+                                  the operand packing excluded)                           */
+  long long tc_launches;       /* tensor-core product kernels timed                       */
+  double tc_mma_flops;         /* flops those kernels issued on the tensor cores (2 per
+                                  multiply-add, bf16 or TF32 operands, padding included)  */
 } tebd_stats;
 int tebd_set_profiling(tebd_handle *h, int on);
 int tebd_get_stats(tebd_handle *h, tebd_stats *stats);

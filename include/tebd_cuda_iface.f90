@@ -22,6 +22,9 @@ TYPE, BIND(C) :: tebd_stats
   INTEGER(C_LONG_LONG) :: rsvd_updates, rsvd_fallbacks
   REAL(C_DOUBLE) :: rsvd_flops, rsvd_worst_residual
   INTEGER(C_LONG_LONG) :: rsvd_skipped
+  REAL(C_DOUBLE) :: tc_ms
+  INTEGER(C_LONG_LONG) :: tc_launches
+  REAL(C_DOUBLE) :: tc_mma_flops
 END TYPE
 INTERFACE
   SUBROUTINE tebd_default_opts(o) BIND(C, NAME='tebd_default_opts')

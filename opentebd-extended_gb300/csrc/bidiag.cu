@@ -1802,7 +1802,8 @@ int run_bidiag(tebd_handle *h, int nb, int nmax) {
   b.nb = nb;
   b.nmax = nmax;
   b.kk = h->chi;
-  b.dfp = h->opts.svd_mode == TEBD_SVD_DF;
+  // the precision form, and the learned-rank form's bonds off the randomized route
+  b.dfp = h->opts.svd_mode == TEBD_SVD_DF || h->opts.svd_mode == TEBD_SVD_RSVD;
   b.phase = 0;
   b.cap = 0;
   return run_bidiag_batch(h, b);

@@ -144,7 +144,7 @@ extern "C" int tebd_create(int L, int d, int chi, int mode, const tebd_opts *opt
     h->rs_oversample = 64;
     h->rs_power = 2;
     h->rs_tol = 1e-5;
-    h->rs_slices = 5;
+    h->rs_slices = 7;
   }
   if (!h) return TEBD_ERR_OOM;
   h->L = L;
@@ -415,6 +415,17 @@ extern "C" int tebd_get_sweeps(tebd_handle *h, int link, int *sweeps) {
               "get sweeps");
 }
 
+// A bond the randomized route may take: saturated (all chi of its Lambda in use)
+// with Schmidt values spanning at most kRsvdSpan (the sketch is orthonormalised
+// through Grams, which resolve directions down to ~1e-7 of the largest), a
+// compacted Theta with room for a sketch beyond the kept rank, and within the
+// bidiagonal route's size limit (its fallback).
+constexpr float kRsvdSpan = 1e-6f;
+static bool rsvd_candidate(const tebd_handle *h, const Compact &c) {
+  const int mn = std::min(c.m, c.n);
+  return c.r1 == h->chi && c.span >= kRsvdSpan && mn >= h->chi + 32 && std::max(c.m, c.n) <= kBidiagMaxDim;
+}
+
 // The learned model's choice for the randomized route of one batch: per bond
 // the predicted log10 sigma_k / sigma_0 at k / chi = kMlpRanks (interpolated
 // linearly, extended past the last point along its last segment); a pair (p, q)
@@ -518,12 +529,15 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
       if (h->opts.svd_mode == TEBD_SVD_RSVD && !h->unnormalized) {
         int over = h->rs_oversample, power = h->rs_power;
         std::vector<char> allow(nb, 1);
-        if (h->rs_model && (rc = rsvd_model_choice(h, nb, gates, &over, &power, allow))) return rc;
+        bool any = false;
+        for (int s = 0; s < nb; ++s) any |= rsvd_candidate(h, cps[s]);
+        if (any && h->rs_model && (rc = rsvd_model_choice(h, nb, gates, &over, &power, allow))) return rc;
         const int sketch = h->chi + over;
         for (int s = 0; s < nb; ++s) {
           const int mn = std::min(cps[s].m, cps[s].n);
           rank[s] = std::min(h->chi, mn);
-          h->path_h[s] = (allow[s] && mn >= sketch + 16 && std::max(cps[s].m, cps[s].n) <= kBidiagMaxDim)
+          // the sketch is at most 1024 wide (its Cholesky stages one row of R in shared memory)
+          h->path_h[s] = (allow[s] && rsvd_candidate(h, cps[s]) && mn >= sketch + 16 && sketch <= 1024)
                              ? kPathRsvd
                              : kPathQRJ;
           nrs += h->path_h[s] == kPathRsvd;
@@ -579,6 +593,7 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
   if (h->profiling) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]) == cudaSuccess) h->stats.batch_ms += ms;
+    tc_collect(h);
   }
   h->stats.updates += nb;
   if ((rc = jacobi_collect(h))) return rc;

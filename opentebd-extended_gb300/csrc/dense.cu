@@ -57,6 +57,15 @@ __global__ void __launch_bounds__(96) k_compact(const double *__restrict__ lam, 
     c.m = d * cnt[0];
     c.n = d * cnt[2];
     c.k = c.n;
+    const double *l1 = lam + (size_t)link * chi;
+    double lo = 0.0, hi = 0.0;
+    for (int a = 0; a < chi; ++a)
+      if (l1[a] != 0.0) {
+        const double v = fabs(l1[a]);
+        lo = (lo == 0.0 || v < lo) ? v : lo;
+        hi = v > hi ? v : hi;
+      }
+    c.span = hi > 0.0 ? (float)(lo / hi) : 0.f;
     *slots[s].cp = c;
     jp[s].m = c.m;
     jp[s].n = c.n;
@@ -529,7 +538,7 @@ int launch_dense_prepare(tebd_handle *h, int nb, bool /*real_gate: converted on 
   int tc = -1;  // tensor-core Theta (theta_tc.cu); -1: formed on the CUDA cores below
   if (h->theta_form != 0 && (tc = launch_theta_tc(h, nb)) > 0) return tc;
   if (tc == 0) {
-  } else if (h->opts.svd_mode == TEBD_SVD_DF)
+  } else if (h->opts.svd_mode == TEBD_SVD_DF || h->opts.svd_mode == TEBD_SVD_RSVD)
     k_theta_form_df<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
                                                                             h->slots_d, chi, d);
   else

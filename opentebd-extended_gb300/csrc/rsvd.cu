@@ -6,9 +6,8 @@
 //
 // Per bond (X = the gated, unnormalised Theta, m x n; r triplets wanted, sketch
 // width s = r + p).  Every product below runs on the tensor cores as an
-// error-free digit-plane product (tc_ozaki.cu): the range finder with S_sk
-// planes (default 5, ~2^-35: a subspace needs no more), everything from the
-// final basis on with 7 planes (FP64 class).  The only FP64 CUDA-core work is
+// error-free digit-plane product (tc_ozaki.cu) with 7 planes (FP64 class; the
+// range finder's plane count is settable, tebd_set_rsvd).  The only FP64 CUDA-core work is
 // O(s^3): the Cholesky factors of s x s Grams and one s x s SVD.
 //   1. Xp = X zero-padded to the batch's m_max x n_max (kept: the fallback
 //      restarts from it);
@@ -122,7 +121,10 @@ __global__ void k_rs_pad(const Slot *slots, const RsDims *dims, double2 *ws, siz
 // then Ri = R^-1 (upper).  A pivot at or below `floor` times the largest diagonal
 // (the Gram's own rounding level: its products carry 7 S bits) marks a direction
 // the sketch does not span to that accuracy: its row of R and column of R^-1 are
-// zero, so A R^-1 has a zero column there.  One CTA per bond.
+// zero, so A R^-1 has a zero column there.  One CTA per bond; row j of R is staged
+// in shared memory at step j, and the trailing update runs one warp per column
+// with the lanes down the column (contiguous in memory).
+constexpr int kCholMaxS = 1024;
 __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, size_t per, size_t og, size_t ori,
                                                  int s, double floor) {
   const int p = blockIdx.x;
@@ -130,8 +132,10 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
   double2 *G = reinterpret_cast<double2 *>(ws + p * per + og);
   double2 *Ri = reinterpret_cast<double2 *>(ws + p * per + ori);
   const int tid = threadIdx.x, nt = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   __shared__ double gmax, piv;
   __shared__ double red[512];
+  __shared__ double2 row[kCholMaxS];
   double mx = 0.0;
   for (int j = tid; j < s; j += nt) mx = fmax(mx, G[j + (size_t)s * j].x);
   red[tid] = mx;
@@ -151,38 +155,43 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
     }
     __syncthreads();
     const double inv = piv > 0.0 ? 1.0 / piv : 0.0;
-    for (int k = j + 1 + tid; k < s; k += nt) {  // row j of R
+    for (int k = j + 1 + tid; k < s; k += nt) {  // row j of R, kept in shared memory too
       const double2 v = G[j + (size_t)s * k];
-      G[j + (size_t)s * k] = make_double2(v.x * inv, v.y * inv);
+      const double2 r = make_double2(v.x * inv, v.y * inv);
+      G[j + (size_t)s * k] = r;
+      row[k] = r;
     }
     __syncthreads();
-    const int t = s - j - 1;
-    for (int e = tid; e < t * t; e += nt) {  // trailing upper triangle: G_kl -= conj(R_jk) R_jl
-      const int k = j + 1 + e % t, l = j + 1 + e / t;
-      if (k > l) continue;
-      const double2 a = G[j + (size_t)s * k], b = G[j + (size_t)s * l];
-      double2 &g = G[k + (size_t)s * l];
-      g.x -= a.x * b.x + a.y * b.y;
-      g.y -= a.x * b.y - a.y * b.x;
+    for (int l = j + 1 + warp; l < s; l += nw) {  // G_kl -= conj(R_jk) R_jl, j < k <= l
+      const double2 b = row[l];
+      double2 *col = G + (size_t)s * l;
+      for (int k = j + 1 + lane; k <= l; k += 32) {
+        const double2 a = row[k];
+        double2 g = col[k];
+        g.x -= a.x * b.x + a.y * b.y;
+        g.y -= a.x * b.y - a.y * b.x;
+        col[k] = g;
+      }
     }
     __syncthreads();
   }
   // Ri = R^-1 (upper), row by row from the bottom: Ri_ii = 1 / R_ii and
-  // Ri_ic = -(sum_{l=i+1..c} R_il Ri_lc) / R_ii; one warp per column, lanes over l
-  // (Ri's columns are contiguous: coalesced), so the O(s^3 / 6) work is spread
-  // over the CTA instead of one thread per column.
-  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  // Ri_ic = -(sum_{l=i+1..c} R_il Ri_lc) / R_ii; row i of R is staged in shared
+  // memory, one warp per column c with the lanes over l (Ri's columns contiguous).
   for (int e = tid; e < s * s; e += nt) Ri[e] = make_double2(0.0, 0.0);
   __syncthreads();
   for (int i = s - 1; i >= 0; --i) {
-    const double d = G[i + (size_t)s * i].x;
+    for (int l = i + tid; l < s; l += nt) row[l] = G[i + (size_t)s * l];
+    __syncthreads();
+    const double d = row[i].x;
     const double inv = d > 0.0 ? 1.0 / d : 0.0;
     for (int c = i + 1 + warp; c < s; c += nw) {
       double ax = 0.0, ay = 0.0;
+      const double2 *x = Ri + (size_t)s * c;
       for (int l = i + 1 + lane; l <= c; l += 32) {
-        const double2 r = G[i + (size_t)s * l], x = Ri[l + (size_t)s * c];
-        ax = fma(r.x, x.x, fma(-r.y, x.y, ax));
-        ay = fma(r.x, x.y, fma(r.y, x.x, ay));
+        const double2 r = row[l], xl = x[l];
+        ax = fma(r.x, xl.x, fma(-r.y, xl.y, ax));
+        ay = fma(r.x, xl.y, fma(r.y, xl.x, ay));
       }
       for (int o = 16; o > 0; o >>= 1) {
         ax += __shfl_xor_sync(0xffffffffu, ax, o);
@@ -412,6 +421,7 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
   }
   if (!s) return TEBD_OK;
   s = std::max(s, r_max);
+  const int nact = (int)std::count(on.begin(), on.end(), 1);  // bonds on the route
   int rc = rsvd_alloc(h, std::max(s, h->rs_sketch_cap));
   if (rc) return rc;
   h->rs_sketch_cap = std::max(h->rs_sketch_cap, s);
@@ -460,26 +470,28 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
     }
     int e = tc_reserve(h, zprod_ws_bytes(z));
     if (e) return e;
+    tc_events(h, zprod_mma_flops(z, nact), &z.ev0, &z.ev1);
     e = check_cuda(h, zprod_run(z, h->tc_ws, h->tc_err, st), "randomized SVD product");
     h->launches += 5;
-    h->stats.rsvd_flops += 8.0 * rows * (double)cols * k * nb;
+    h->stats.rsvd_flops += 8.0 * rows * (double)cols * k * nact;
     return e;
   };
   // CholQR of the rows x s block at `buf` (ld rows), through `tmp`: one pass for
   // the range finder's intermediate bases (only their span matters), two (CholQR2,
-  // the second with 7 planes) for the final basis P; the result is left in `buf`
-  auto cholqr2 = [&](size_t buf, size_t tmp, int rows, int slices2) -> int {
+  // the second with 7 planes) for the final basis P; the result is left in `buf`.
+  // The sketch's width s is at most kCholMaxS (the Cholesky stages one row of R).
+  auto cholqr2 = [&](size_t buf, size_t tmp, int rows, bool twice) -> int {
     int e;
     if ((e = prod(buf, rows, 1, nullptr, pstr, buf, rows, nullptr, pstr, s, s, rows, c.g, sk))) return e;
-    k_rs_chol<<<nb, 512, 0, st>>>(R->dims_d, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * sk + 10));
+    k_rs_chol<<<nb, 512, 0, st>>>(R->dims_d, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * sk + 9));
     TEBD_LAUNCHED(h);
     if ((e = prod(buf, rows, 0, nullptr, pstr, c.ri, s, nullptr, pstr, rows, s, s, tmp, sk))) return e;
-    if (slices2 != fin)  // one pass: back into buf
+    if (!twice)  // one pass: back into buf
       return check_cuda(h, cudaMemcpy2DAsync(ws + buf, per, ws + tmp, per, sizeof(double2) * (size_t)rows * s, nb,
                                              cudaMemcpyDeviceToDevice, st),
                         "CholQR copy");
     if ((e = prod(tmp, rows, 1, nullptr, pstr, tmp, rows, nullptr, pstr, s, s, rows, c.g, fin))) return e;
-    k_rs_chol<<<nb, 512, 0, st>>>(R->dims_d, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * fin + 10));
+    k_rs_chol<<<nb, 512, 0, st>>>(R->dims_d, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * fin + 9));
     TEBD_LAUNCHED(h);
     return prod(tmp, rows, 0, nullptr, pstr, c.ri, s, nullptr, pstr, rows, s, s, buf, fin);
   };
@@ -500,16 +512,16 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
   }
   // 2. range finder
   if ((rc = prod(c.xp, m_max, 0, nullptr, pstr, 0, R->n_full, R->om, 0, m_max, s, n_max, c.a, sk)) ||
-      (rc = cholqr2(c.a, c.b, m_max, sk)))
+      (rc = cholqr2(c.a, c.b, m_max, false)))
     return rc;
   for (int it = 0; it < power; ++it)
     if ((rc = prod(c.xp, m_max, 1, nullptr, pstr, c.a, m_max, nullptr, pstr, n_max, s, m_max, c.z, sk)) ||
-        (rc = cholqr2(c.z, c.b, n_max, sk)) ||
+        (rc = cholqr2(c.z, c.b, n_max, false)) ||
         (rc = prod(c.xp, m_max, 0, nullptr, pstr, c.z, n_max, nullptr, pstr, m_max, s, n_max, c.a, sk)) ||
-        (rc = cholqr2(c.a, c.b, m_max, sk)))
+        (rc = cholqr2(c.a, c.b, m_max, false)))
       return rc;
   if ((rc = prod(c.xp, m_max, 1, nullptr, pstr, c.a, m_max, nullptr, pstr, n_max, s, m_max, c.z, sk)) ||
-      (rc = cholqr2(c.z, c.b, n_max, fin)))
+      (rc = cholqr2(c.z, c.b, n_max, true)))
     return rc;
   // 3. Rayleigh-Ritz: C = Xp P, M = C^H C, M = W Lambda W^H
   if ((rc = prod(c.xp, m_max, 0, nullptr, pstr, c.z, n_max, nullptr, pstr, m_max, s, n_max, c.c, fin)) ||
@@ -539,6 +551,7 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
     z.optr = reinterpret_cast<const unsigned char *>(h->slots_d) + offsetof(Slot, V);
     z.optr_stride = (int)sizeof(Slot);
     if ((rc = tc_reserve(h, zprod_ws_bytes(z)))) return rc;
+    tc_events(h, zprod_mma_flops(z, nact), &z.ev0, &z.ev1);
     if ((rc = check_cuda(h, zprod_run(z, h->tc_ws, h->tc_err, st), "randomized SVD V"))) return rc;
     h->launches += 5;
   }

@@ -367,6 +367,12 @@ static ZDims zdims(const ZProd &z) {
   return d;
 }
 
+double zprod_mma_flops(const ZProd &z, int active) {
+  const ZDims d = zdims(z);
+  const double pairs = zprod_oz(z.form) ? d.planes * (d.planes + 1) / 2.0 : (z.form == kTc3xTF32 ? 3.0 : 1.0);
+  return pairs * 2.0 * d.m_pad * (double)d.n_pad * d.k_pad * active;
+}
+
 size_t zprod_ws_bytes(const ZProd &z) {
   const ZDims d = zdims(z);
   const size_t el = zprod_oz(z.form) ? 2 : 4;
@@ -425,7 +431,10 @@ cudaError_t zprod_run(const ZProd &z, void *ws, int *err_d, cudaStream_t st) {
     b.alpha = z.alpha;
     b.optr = z.optr;
     b.optr_stride = z.optr_stride;
-    return oz_gemm_launch(b, err_d, st);
+    if (z.ev0) cudaEventRecord(z.ev0, st);
+    e = oz_gemm_launch(b, err_d, st);
+    if (z.ev1) cudaEventRecord(z.ev1, st);
+    return e;
   }
   float *fa = reinterpret_cast<float *>(pa), *fb = reinterpret_cast<float *>(pb);
   if ((e = tc_pack_a(z.a, z.a_stride, z.lda, z.m, z.k, z.a_trans, z.a_conj, z.nprob, d.m_pad, d.k_pad, z.form,
@@ -454,7 +463,10 @@ cudaError_t zprod_run(const ZProd &z, void *ws, int *err_d, cudaStream_t st) {
   b.alpha = z.alpha;
   b.optr = z.optr;
   b.optr_stride = z.optr_stride;
-  return tc_gemm_launch(b, err_d, st);
+  if (z.ev0) cudaEventRecord(z.ev0, st);
+  e = tc_gemm_launch(b, err_d, st);
+  if (z.ev1) cudaEventRecord(z.ev1, st);
+  return e;
 }
 
 }  // namespace tebd

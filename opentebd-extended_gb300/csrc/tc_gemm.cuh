@@ -151,9 +151,14 @@ struct ZProd {
   // m_pad = tc_pad(m, 128), k_pad = tc_pad(2 k, 32)) -- A is then not read
   const unsigned short *a_dig;
   const int *a_exp;
+  // optional events recorded around the product kernel alone (profiling)
+  cudaEvent_t ev0, ev1;
 };
 inline bool zprod_oz(int form) { return form > 100 && form <= 100 + kOzMaxS; }
 size_t zprod_ws_bytes(const ZProd &z);
+// tensor-core multiply-adds the product kernel issues, as flops (2 per
+// multiply-add): planes pairs x 2 x m_pad x n_pad x k_pad x `active` problems
+double zprod_mma_flops(const ZProd &z, int active);
 // ws: zprod_ws_bytes(z) bytes of device memory (256-byte aligned).
 cudaError_t zprod_run(const ZProd &z, void *ws, int *err_d, cudaStream_t st);
 

@@ -91,6 +91,7 @@ struct Compact {
   int r0, r1, r2;  // kept counts of Lambda0, Lambda1, Lambda2
   int m, n;        // d*r0 rows, d*r2 columns
   int k;           // singular triplets computed (numerical rank for the QR path, else n)
+  float span;      // smallest / largest nonzero Lambda1 (the bond's own Schmidt values)
 };
 
 struct Slot {
@@ -191,6 +192,10 @@ struct tebd_handle {
   double rs_tol;           // judge: largest triplet residual / ||Theta||
   int rs_slices;           // bf16 digit planes of the products (7: FP64 class)
   int rs_sketch_cap;       // workspace sketch capacity requested so far
+  // profiling: event pairs around the tensor-core product kernels of a batch
+  std::vector<cudaEvent_t> tc_ev;
+  std::vector<double> tc_ev_flops;
+  int tc_ev_used;
   tebd_mlp *rs_model;      // learned model choosing the sketch per batch (mlp.cu), or null
   double rs_target;        // the model's bound on (sigma_{r+p} / sigma_r)^(2q+2)
 };
@@ -241,6 +246,11 @@ int launch_theta_tc(tebd_handle *h, int nb);
 int tc_reserve(tebd_handle *h, size_t bytes);
 int tc_check(tebd_handle *h);  // reads and clears tc_err (synchronises the stream)
 void tc_free(tebd_handle *h);
+// profiling of the tensor-core product kernels: a fresh event pair for one launch
+// issuing `flops` tensor-core flops (null events when profiling is off), and the
+// collection of a batch's pairs into the stats once the stream is synchronised
+void tc_events(tebd_handle *h, double flops, cudaEvent_t *e0, cudaEvent_t *e1);
+void tc_collect(tebd_handle *h);
 // randomized SVD route (rsvd.cu)
 int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vector<int> &route,
              const std::vector<int> &rank, int sketch, int power);

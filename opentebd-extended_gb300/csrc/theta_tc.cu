@@ -36,7 +36,42 @@ int tc_reserve(tebd_handle *h, size_t bytes) {
   return TEBD_OK;
 }
 
+void tc_events(tebd_handle *h, double flops, cudaEvent_t *e0, cudaEvent_t *e1) {
+  *e0 = *e1 = nullptr;
+  if (!h->profiling) return;
+  const size_t need = 2 * (size_t)(h->tc_ev_used + 1);
+  while (h->tc_ev.size() < need) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return;
+    }
+    h->tc_ev.push_back(e);
+  }
+  h->tc_ev_flops.resize(h->tc_ev.size() / 2);
+  *e0 = h->tc_ev[2 * h->tc_ev_used];
+  *e1 = h->tc_ev[2 * h->tc_ev_used + 1];
+  h->tc_ev_flops[h->tc_ev_used] = flops;
+  ++h->tc_ev_used;
+}
+
+void tc_collect(tebd_handle *h) {
+  for (int i = 0; i < h->tc_ev_used; ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->tc_ev[2 * i], h->tc_ev[2 * i + 1]) == cudaSuccess) {
+      h->stats.tc_ms += ms;
+      h->stats.tc_launches++;
+      h->stats.tc_mma_flops += h->tc_ev_flops[i];
+    }
+  }
+  (void)cudaGetLastError();
+  h->tc_ev_used = 0;
+}
+
 void tc_free(tebd_handle *h) {
+  for (cudaEvent_t e : h->tc_ev) cudaEventDestroy(e);
+  h->tc_ev.clear();
+  h->tc_ev_used = 0;
   cudaFree(h->tc_ws);
   cudaFree(h->tc_err);
   h->tc_ws = nullptr;
@@ -116,7 +151,9 @@ int launch_theta_tc(tebd_handle *h, int nb) {
     n_max = std::max(n_max, c.n);
     r1_max = std::max(r1_max, c.r1);
   }
-  if (m_max == 0 || n_max == 0 || r1_max == 0) return -1;
+  // small products (early, low-rank updates) stay on the CUDA cores: packing and
+  // the extra synchronisation cost more than the tiled FP64 kernel there
+  if (m_max == 0 || n_max == 0 || r1_max == 0 || (double)m_max * n_max * r1_max < (double)(1 << 21)) return -1;
   const Slot &s0 = h->slots[0];
   const long long aux_stride = nb > 1 ? (long long)(h->slots[1].aux - s0.aux) : 0;
   const size_t total = (size_t)m_max * r1_max + (size_t)r1_max * n_max;
@@ -145,6 +182,7 @@ int launch_theta_tc(tebd_handle *h, int nb) {
   z.optr = reinterpret_cast<const unsigned char *>(h->slots_d) + offsetof(Slot, X);
   z.optr_stride = (int)sizeof(Slot);
   if ((rc = tc_reserve(h, zprod_ws_bytes(z)))) return rc;
+  tc_events(h, zprod_mma_flops(z, nb), &z.ev0, &z.ev1);
   if ((rc = check_cuda(h, zprod_run(z, h->tc_ws, h->tc_err, h->stream), "tensor-core Theta"))) return rc;
   h->launches += zprod_oz(z.form) ? 5 : 3;  // packs (+ exponent passes) and the product
   return TEBD_OK;

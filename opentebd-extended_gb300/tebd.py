@@ -125,6 +125,9 @@ class Stats(ctypes.Structure):
         ("rsvd_flops", ctypes.c_double),
         ("rsvd_worst_residual", ctypes.c_double),
         ("rsvd_skipped", ctypes.c_longlong),
+        ("tc_ms", ctypes.c_double),
+        ("tc_launches", ctypes.c_longlong),
+        ("tc_mma_flops", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -268,7 +271,7 @@ class Chain:
         100 + S = S bf16 digit planes on the tensor cores (S = 7: FP64 class)."""
         self._check(self._lib.tebd_set_theta_form(self.h, int(form)))
 
-    def set_rsvd(self, oversample=64, power_iters=2, tol=1e-5, slices=5):
+    def set_rsvd(self, oversample=64, power_iters=2, tol=1e-5, slices=7):
         """Randomized route of TEBD_SVD_RSVD: sketch width kept rank + oversample,
         power iterations, judge tolerance (largest triplet residual / ||Theta||)
         and the digit planes of its tensor-core products."""

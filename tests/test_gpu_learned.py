@@ -10,10 +10,11 @@ gains the randomized route.
   predicts held-out spectra (log10 of singular-value ratios) better than their
   mean;
 * A/B: the same Trotter steps of a saturated Bose-Hubbard chain through the
-  randomized route with the fixed sketch (p = 64, q = 2) and with a trained model
-  choosing it: the model's run spends fewer tensor-core flops on the sketch, and
-  both agree with the plain FP64 route on every two-site density matrix within
-  1e-8.
+  randomized route with a trained model choosing the sketch, against a
+  conservative fixed sketch (p = 128, q = 3) and a cheap one (p = 16, q = 0): the
+  model keeps the conservative sketch's agreement with plain FP64 (two-site
+  density matrices within 1e-8) for fewer tensor-core flops, and sends no more
+  bonds to the full SVD than the cheap sketch.
 """
 import numpy as np
 import pytest
@@ -92,6 +93,12 @@ def test_mlp_training_on_logged_spectra(pkg):
 
 
 def test_learned_model_gains_over_fixed_sketch(pkg):
+    """The model against two fixed sketches on the same saturated steps: a
+    conservative one (p = 128, q = 3) that every bond passes, and a cheap one
+    (p = 16, q = 0).  With the model the route keeps the conservative sketch's
+    accuracy (two-site density matrices within 1e-8 of plain FP64) for fewer
+    tensor-core flops, and sends no more bonds to the full SVD than the cheap
+    sketch does."""
     H = pkg.hamiltonians
     x, t = _logged(pkg, [21, 22], L=12, d=5, chi=48, steps=30)
     m = pkg.Mlp(seed=6)
@@ -105,23 +112,29 @@ def test_learned_model_gains_over_fixed_sketch(pkg):
             c.trotter_step(gates, 2)
         gam, lam = c.get_state()
     res = {}
-    for name, mode, model in (("fp64", pkg.SVD_FP64, None), ("fixed", pkg.SVD_RSVD, None),
-                              ("model", pkg.SVD_RSVD, m)):
+    for name, mode, sketch, model in (("fp64", pkg.SVD_FP64, None, None),
+                                      ("conservative", pkg.SVD_RSVD, (128, 3), None),
+                                      ("cheap", pkg.SVD_RSVD, (16, 0), None),
+                                      ("model", pkg.SVD_RSVD, None, m)):
         with pkg.Chain(L, d, chi, svd_mode=mode) as c:
             c.set_state(gam, lam)
+            if sketch is not None:
+                c.set_rsvd(oversample=sketch[0], power_iters=sketch[1])
             if model is not None:
                 c.set_rsvd_model(model, 1e-6)
             for _ in range(3):
                 c.trotter_step(gates, 2)
-            res[name] = (c.get_state(), c.stats())
+            g, l = c.get_state()
+            res[name] = ((g, l), c.stats())
     (g0, l0), _ = res["fp64"]
-    for name in ("fixed", "model"):
+    for name in ("conservative", "model"):
         (g1, l1), st = res[name]
+        assert st["rsvd_updates"] > 0, name
         for k in range(1, L):
             a = obs.two_site_rho(l0[k - 1], g0[k - 1], l0[k], g0[k], l0[k + 1])
             b = obs.two_site_rho(l1[k - 1], g1[k - 1], l1[k], g1[k], l1[k + 1])
             assert np.max(np.abs(a - b)) < 1e-8, (name, k)
-    fixed, model = res["fixed"][1], res["model"][1]
-    assert fixed["rsvd_updates"] > 0
-    assert model["rsvd_flops"] < fixed["rsvd_flops"], (model["rsvd_flops"], fixed["rsvd_flops"])
+    cons, cheap, model = res["conservative"][1], res["cheap"][1], res["model"][1]
+    assert model["rsvd_flops"] < cons["rsvd_flops"], (model["rsvd_flops"], cons["rsvd_flops"])
+    assert model["rsvd_fallbacks"] <= cheap["rsvd_fallbacks"], (model, cheap)
     m.close()
