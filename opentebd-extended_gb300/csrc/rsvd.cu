@@ -35,6 +35,7 @@
 
 #include <algorithm>
 
+#include "df.cuh"
 #include "tc_gemm.cuh"
 
 namespace tebd {
@@ -121,23 +122,52 @@ __global__ void k_rs_pad(const Slot *slots, const RsDims *dims, double2 *ws, siz
 // then Ri = R^-1 (upper).  A pivot at or below `floor` times the largest diagonal
 // (the Gram's own rounding level: its products carry 7 S bits) marks a direction
 // the sketch does not span to that accuracy: its row of R and column of R^-1 are
-// zero, so A R^-1 has a zero column there.  One CTA per bond; row j of R is staged
-// in shared memory at step j, and the trailing update runs one warp per column
-// with the lanes down the column (contiguous in memory).
+// zero, so A R^-1 has a zero column there.  One CTA per bond.  The O(s^3) work
+// runs in double-float on the FP32 pipe (pairs of floats, 48-bit significands:
+// the FP64 pipe gives one SM ~7 GFLOP/s, too little for s^3 / 2 complex
+// multiply-adds per call); only the s pivots and their reciprocals are FP64.
+// G and Ri hold float4 (re_hi, re_lo, im_hi, im_lo) while the kernel runs -- the
+// same 16 bytes as a double2 -- and Ri is converted back to FP64 at the end.
+// Row j of R is staged in shared memory at step j; the trailing update runs one
+// warp per column with the lanes down the column (contiguous in memory).
 constexpr int kCholMaxS = 1024;
+
+__device__ __forceinline__ float4 df_scale(float4 v, float sh, float sl) {  // v * (sh + sl)
+  float4 r;
+  float p = __fmul_rn(v.x, sh), e = fmaf(v.x, sh, -p);
+  e = fmaf(v.x, sl, e);
+  e = fmaf(v.y, sh, e);
+  r.x = __fadd_rn(p, e);
+  r.y = __fadd_rn(e, -__fadd_rn(r.x, -p));
+  p = __fmul_rn(v.z, sh);
+  e = fmaf(v.z, sh, -p);
+  e = fmaf(v.z, sl, e);
+  e = fmaf(v.w, sh, e);
+  r.z = __fadd_rn(p, e);
+  r.w = __fadd_rn(e, -__fadd_rn(r.z, -p));
+  return r;
+}
+
+__device__ __forceinline__ void df_split(double x, float &h, float &l) {
+  h = (float)x;
+  l = (float)(x - (double)h);
+}
+
 __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, size_t per, size_t og, size_t ori,
                                                  int s, double floor) {
   const int p = blockIdx.x;
   if (dims[p].s == 0) return;
-  double2 *G = reinterpret_cast<double2 *>(ws + p * per + og);
-  double2 *Ri = reinterpret_cast<double2 *>(ws + p * per + ori);
+  double2 *Gd = reinterpret_cast<double2 *>(ws + p * per + og);
+  float4 *G = reinterpret_cast<float4 *>(Gd);
+  float4 *Ri = reinterpret_cast<float4 *>(ws + p * per + ori);
   const int tid = threadIdx.x, nt = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-  __shared__ double gmax, piv;
+  __shared__ double gmax;
+  __shared__ float ph, pl;  // the reciprocal pivot of the step, double-float
   __shared__ double red[512];
-  __shared__ double2 row[kCholMaxS];
+  __shared__ float4 row[kCholMaxS];
   double mx = 0.0;
-  for (int j = tid; j < s; j += nt) mx = fmax(mx, G[j + (size_t)s * j].x);
+  for (int j = tid; j < s; j += nt) mx = fmax(mx, Gd[j + (size_t)s * j].x);
   red[tid] = mx;
   __syncthreads();
   for (int w = nt / 2; w > 0; w >>= 1) {
@@ -146,30 +176,36 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
   }
   if (tid == 0) gmax = red[0];
   __syncthreads();
+  for (size_t e = tid; e < (size_t)s * s; e += nt) G[e] = dfs(Gd[e]);  // in place: element e read, then written
+  __syncthreads();
   const double thresh = gmax * floor;
   for (int j = 0; j < s; ++j) {
     if (tid == 0) {
-      const double d = G[j + (size_t)s * j].x;
-      piv = (d > thresh && d > 0.0) ? sqrt(d) : 0.0;
-      G[j + (size_t)s * j] = make_double2(piv, 0.0);
+      const float4 g = G[j + (size_t)s * j];
+      const double d = (double)g.x + (double)g.y;
+      const double piv = (d > thresh && d > 0.0) ? sqrt(d) : 0.0;
+      float h, l;
+      df_split(piv, h, l);
+      G[j + (size_t)s * j] = make_float4(h, l, 0.f, 0.f);
+      df_split(piv > 0.0 ? 1.0 / piv : 0.0, h, l);
+      ph = h;
+      pl = l;
     }
     __syncthreads();
-    const double inv = piv > 0.0 ? 1.0 / piv : 0.0;
+    const float ih = ph, il = pl;
     for (int k = j + 1 + tid; k < s; k += nt) {  // row j of R, kept in shared memory too
-      const double2 v = G[j + (size_t)s * k];
-      const double2 r = make_double2(v.x * inv, v.y * inv);
+      const float4 r = df_scale(G[j + (size_t)s * k], ih, il);
       G[j + (size_t)s * k] = r;
       row[k] = r;
     }
     __syncthreads();
     for (int l = j + 1 + warp; l < s; l += nw) {  // G_kl -= conj(R_jk) R_jl, j < k <= l
-      const double2 b = row[l];
-      double2 *col = G + (size_t)s * l;
+      const float4 b = row[l];
+      float4 *col = G + (size_t)s * l;
       for (int k = j + 1 + lane; k <= l; k += 32) {
-        const double2 a = row[k];
-        double2 g = col[k];
-        g.x -= a.x * b.x + a.y * b.y;
-        g.y -= a.x * b.y - a.y * b.x;
+        const float4 a = row[k];
+        float4 g = col[k];
+        df_cmac_ca(g.x, g.y, g.z, g.w, make_float4(-a.x, -a.y, -a.z, -a.w), b);
         col[k] = g;
       }
     }
@@ -178,30 +214,36 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
   // Ri = R^-1 (upper), row by row from the bottom: Ri_ii = 1 / R_ii and
   // Ri_ic = -(sum_{l=i+1..c} R_il Ri_lc) / R_ii; row i of R is staged in shared
   // memory, one warp per column c with the lanes over l (Ri's columns contiguous).
-  for (int e = tid; e < s * s; e += nt) Ri[e] = make_double2(0.0, 0.0);
+  for (size_t e = tid; e < (size_t)s * s; e += nt) Ri[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   __syncthreads();
   for (int i = s - 1; i >= 0; --i) {
     for (int l = i + tid; l < s; l += nt) row[l] = G[i + (size_t)s * l];
-    __syncthreads();
-    const double d = row[i].x;
-    const double inv = d > 0.0 ? 1.0 / d : 0.0;
-    for (int c = i + 1 + warp; c < s; c += nw) {
-      double ax = 0.0, ay = 0.0;
-      const double2 *x = Ri + (size_t)s * c;
-      for (int l = i + 1 + lane; l <= c; l += 32) {
-        const double2 r = row[l], xl = x[l];
-        ax = fma(r.x, xl.x, fma(-r.y, xl.y, ax));
-        ay = fma(r.x, xl.y, fma(r.y, xl.x, ay));
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        ax += __shfl_xor_sync(0xffffffffu, ax, o);
-        ay += __shfl_xor_sync(0xffffffffu, ay, o);
-      }
-      if (lane == 0) Ri[i + (size_t)s * c] = make_double2(-ax * inv, -ay * inv);
+    if (tid == 0) {
+      const double d = (double)G[i + (size_t)s * i].x + (double)G[i + (size_t)s * i].y;
+      float h, l2;
+      df_split(d > 0.0 ? 1.0 / d : 0.0, h, l2);
+      ph = h;
+      pl = l2;
     }
-    if (tid == 0) Ri[i + (size_t)s * i] = make_double2(inv, 0.0);
+    __syncthreads();
+    const float ih = ph, il = pl;
+    for (int c = i + 1 + warp; c < s; c += nw) {
+      float rh = 0.f, rl = 0.f, jh = 0.f, jl = 0.f;
+      const float4 *x = Ri + (size_t)s * c;
+      for (int l = i + 1 + lane; l <= c; l += 32) df_cmac(rh, rl, jh, jl, row[l], x[l]);
+      for (int o = 16; o > 0; o >>= 1) {  // double-float sums across the warp
+        const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, jh, o), d2 = __shfl_xor_sync(0xffffffffu, jl, o);
+        df_mac(rh, rl, a, b, 1.f, 0.f);
+        df_mac(jh, jl, c2, d2, 1.f, 0.f);
+      }
+      if (lane == 0) Ri[i + (size_t)s * c] = df_scale(make_float4(-rh, -rl, -jh, -jl), ih, il);
+    }
+    if (tid == 0) Ri[i + (size_t)s * i] = make_float4(ih, il, 0.f, 0.f);
     __syncthreads();
   }
+  double2 *Rd = reinterpret_cast<double2 *>(Ri);
+  for (size_t e = tid; e < (size_t)s * s; e += nt) Rd[e] = dfd(Ri[e]);  // back to FP64, in place
 }
 
 // the slot's X (m x r, ld m) = the first m rows of U Sigma (ld m_max); k = r
@@ -396,7 +438,7 @@ static int rs_gram_svd(tebd_handle *h, RsState *R, const std::vector<int> &on, i
   b.nb = nb;
   b.nmax = s;
   b.kk = kk;
-  b.dfp = false;
+  b.dfp = true;  // double-float passes: the s x s Gram's eigenvectors need no more
   b.phase = 0;
   b.cap = 0;
   return run_bidiag_batch(h, b);

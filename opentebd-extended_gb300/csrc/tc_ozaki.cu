@@ -356,6 +356,55 @@ __global__ void __launch_bounds__(256) k_oz_pack(const double2 *src, long long p
   }
 }
 
+// Digits of an operand whose K index is contiguous in memory (A read transposed,
+// element (i, k) at src[k + ld i]; B read as stored, element (k, j) at
+// src[k + ld j]): one warp per row of the packed operand, two passes over that
+// row (largest magnitude, then the digits), coalesced reads and writes, no
+// atomics.  Rows beyond the source extent and K beyond it are packed as zeros.
+template <bool kB>
+__global__ void __launch_bounds__(256) k_oz_pack_rows(const double2 *src, long long pstride, int ld, int r_ext,
+                                                      int c_ext, int conj, int nprob, int rows_pad, int k_pad,
+                                                      int S, unsigned short *dig, int *exps) {
+  const int p = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nrow = kB ? rows_pad / 2 : rows_pad;
+  const int r = blockIdx.x * 8 + warp;
+  if (r >= nrow) return;
+  const bool live = r < r_ext;
+  const double2 *row = src + (size_t)p * pstride + (size_t)ld * r;
+  double mx = 0.0;
+  if (live)
+    for (int k = lane; k < c_ext; k += 32) {
+      const double2 v = row[k];
+      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+    }
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int e = mx > 0.0 ? oz_exp(mx) : (int)0x80808080;
+  if (lane == 0) exps[(size_t)p * nrow + r] = e;
+  const size_t plane = (size_t)nprob * rows_pad * k_pad;
+  for (int k = lane; 2 * k < k_pad; k += 32) {
+    double2 v = make_double2(0.0, 0.0);
+    if (live && k < c_ext) v = row[k];
+    if (conj) v.y = -v.y;
+    unsigned short dr[kOzMaxS], di[kOzMaxS];
+    oz_digits(v.x, e, S, dr);
+    oz_digits(v.y, e, S, di);
+    if (!kB) {
+      unsigned short *o = dig + ((size_t)p * rows_pad + r) * k_pad + 2 * k;
+      for (int q = 0; q < S; ++q)
+        *reinterpret_cast<uint32_t *>(o + q * plane) = (uint32_t)dr[q] | ((uint32_t)di[q] << 16);
+    } else {
+      unsigned short *o0 = dig + ((size_t)p * rows_pad + 2 * r) * k_pad + 2 * k;
+      unsigned short *o1 = o0 + k_pad;
+      for (int q = 0; q < S; ++q) {
+        const unsigned short ni = di[q] ^ 0x8000u;
+        *reinterpret_cast<uint32_t *>(o0 + q * plane) = (uint32_t)dr[q] | ((uint32_t)ni << 16);
+        *reinterpret_cast<uint32_t *>(o1 + q * plane) = (uint32_t)di[q] | ((uint32_t)dr[q] << 16);
+      }
+    }
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 oz_encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
@@ -405,6 +454,11 @@ cudaError_t oz_gemm_launch(const OzBatch &b, int *err_d, cudaStream_t st) {
 cudaError_t oz_pack_a(const double2 *src, long long pstride, int ld, int rows, int cols, int trans, int conj,
                       int nprob, int m_pad, int k_pad, int slices, unsigned short *dig, int *exps,
                       cudaStream_t st) {
+  if (trans) {  // rows contiguous: one warp per row, one kernel
+    k_oz_pack_rows<false><<<dim3((m_pad + 7) / 8, nprob), 256, 0, st>>>(src, pstride, ld, rows, cols, conj, nprob,
+                                                                         m_pad, k_pad, slices, dig, exps);
+    return cudaPeekAtLastError();
+  }
   cudaError_t e = cudaMemsetAsync(exps, 0x80, sizeof(int) * (size_t)nprob * m_pad, st);
   if (e != cudaSuccess) return e;
   dim3 grid((m_pad + 31) / 32, (k_pad / 2 + 31) / 32, nprob);
@@ -418,6 +472,11 @@ cudaError_t oz_pack_a(const double2 *src, long long pstride, int ld, int rows, i
 cudaError_t oz_pack_b(const double2 *src, long long pstride, int ld, int krows, int ncols, int trans, int conj,
                       int nprob, int n_pad, int k_pad, int slices, unsigned short *dig, int *exps,
                       cudaStream_t st) {
+  if (!trans) {  // columns contiguous: one warp per complex column, one kernel
+    k_oz_pack_rows<true><<<dim3((n_pad / 2 + 7) / 8, nprob), 256, 0, st>>>(src, pstride, ld, ncols, krows, conj,
+                                                                            nprob, n_pad, k_pad, slices, dig, exps);
+    return cudaPeekAtLastError();
+  }
   cudaError_t e = cudaMemsetAsync(exps, 0x80, sizeof(int) * (size_t)nprob * (n_pad / 2), st);
   if (e != cudaSuccess) return e;
   dim3 grid((n_pad / 2 + 31) / 32, (k_pad / 2 + 31) / 32, nprob);
