@@ -267,37 +267,39 @@ def measured_peak(key):
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}[key], "fallback figure (no MEASURED_PEAKS.json)"
 
 
-def saturated_state(H):
-    """Every Lambda full (lambda_k ~ exp(-k/16), normalised) and complex Gaussian
-    Gammas (seed 5): each odd bond of the L=64, d=5, chi=128 chain has a full
-    640 x 640 Theta -- the cost regime of the configured run after step ~50."""
+def saturated_state(Ls=L, chi=CHI, decay=16.0):
+    """Every Lambda full (lambda_k ~ exp(-k/decay), normalised) and complex Gaussian
+    Gammas (seed 5): each odd bond of the d=5 chain has a full (5 chi) x (5 chi)
+    Theta -- at L=64, chi=128 the cost regime of the configured run after step ~50."""
     rng = np.random.default_rng(5)
-    gam = [np.asfortranarray(rng.standard_normal((CHI, D, CHI)) + 1j * rng.standard_normal((CHI, D, CHI)))
-           for _ in range(L)]
+    gam = [np.asfortranarray(rng.standard_normal((chi, D, chi)) + 1j * rng.standard_normal((chi, D, chi)))
+           for _ in range(Ls)]
     lam = []
-    for _ in range(L + 1):
-        l = np.exp(-np.arange(CHI) / 16.0)
+    for _ in range(Ls + 1):
+        l = np.exp(-np.arange(chi) / decay)
         lam.append(l / np.linalg.norm(l))
     return gam, lam
 
 
-def saturated_legs(pkg, device, args, fp64_peak, steps=3):
-    """The 32 odd bonds of the saturated chain, updated `steps` times (one batched
-    sweep each), in plain FP64 and in the mixed form, profiled: updates/s from CUDA
-    events on each chain's stream, and the roofline of each form's dominant kernel
-    from that leg's own launch timings (k_gebrd on the FP64 pipe; the tensor-core
+def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=16.0):
+    """The odd bonds of a saturated chain, updated `steps` times (one batched sweep
+    each), in plain FP64 and in the mixed form, profiled: updates/s from CUDA events
+    on each chain's stream, and the roofline of each form's dominant kernel from
+    that leg's own launch timings (k_gebrd on the FP64 pipe; the tensor-core
     product kernels against the measured bf16 peak)."""
     import torch
 
     H = pkg.hamiltonians
-    gam, lam = saturated_state(H)
-    gate = H.matrix_exponential(H.bose_hubbard(L, D, J, U, MU)[1], DT)
-    links = list(range(1, L, 2))
+    gam, lam = saturated_state(Ls, chi, decay)
+    gate = H.matrix_exponential(H.bose_hubbard(Ls, D, J, U, MU)[1], DT)
+    links = list(range(1, Ls, 2))
     bf16_peak, bf16_src = measured_peak("bf16_tflops")
-    out = {"workload": "saturated_bonds_L64_d5_chi128 (32 bonds of a 640 x 640 Theta per step)", "steps": steps}
+    n = D * chi
+    out = {"workload": "saturated_bonds_L%d_d5_chi%d (%d bonds of a %d x %d Theta per step, lambda_k ~ exp(-k/%g))"
+                       % (Ls, chi, len(links), n, n, decay), "steps": steps}
     finals = {}
     for name in ("fp64", "mixed"):
-        c = pkg.Chain(L, D, CHI, device=device, svd_mode=SVD_MODES["fp64" if name == "fp64" else "rsvd"])
+        c = pkg.Chain(Ls, D, chi, device=device, svd_mode=SVD_MODES["fp64" if name == "fp64" else "rsvd"])
         model = None
         if name == "mixed":
             c.set_theta_form(107)
@@ -574,6 +576,8 @@ def run_ours(args):
         "precision_form": prec,
         "mixed_form": mixed,
         "saturated": saturated_legs(pkg, local, args, fp64_peak) if not args.no_precision else None,
+        "saturated_chi512": (saturated_legs(pkg, local, args, fp64_peak, steps=1, Ls=32, chi=512, decay=64.0)
+                             if not args.no_precision and not args.no_chi512 else None),
         **({"rank_form": {"what": "kept-rank form: per-update discarded-weight bound "
                                   "(tebd_set_rank_bound), Lambda beyond the kept rank exactly zero",
                           "legs": rank_form}} if rank_form else {}),
@@ -800,7 +804,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--svd", default="fp64", choices=sorted(SVD_MODES))
     ap.add_argument("--save-obs", default=None, help="write final <n_i>, bond energies, Lambdas (npz)")
-    ap.add_argument("--no-precision", action="store_true", help="skip the precision-form leg")
+    ap.add_argument("--no-precision", action="store_true", help="skip the precision, mixed and saturated legs")
+    ap.add_argument("--no-chi512", action="store_true", help="skip the chi=512 saturated leg")
     ap.add_argument("--rank-bound", type=float, nargs="*", default=None,
                     help="extra legs of the kept-rank form at these discarded-weight bounds (FP64 and "
                          "double-float), with speedup and observable errors against the plain run")

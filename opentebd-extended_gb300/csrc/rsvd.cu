@@ -153,19 +153,24 @@ __device__ __forceinline__ void df_split(double x, float &h, float &l) {
   l = (float)(x - (double)h);
 }
 
+// Blocked form (panels of PB rows of R, PB = 16 up to s = 512, else 8): the panel
+// rows are factored in shared memory and the trailing triangle takes one rank-PB
+// update per panel; the inverse runs block rows from the bottom, each a product
+// with the rows already inverted (one pass) and a triangular solve inside the
+// block.  Dynamic shared memory: PB x s float4.
 __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, size_t per, size_t og, size_t ori,
-                                                 int s, double floor) {
+                                                 int s, double floor, int PB) {
   const int p = blockIdx.x;
   if (dims[p].s == 0) return;
+  extern __shared__ float4 P[];  // PB x s: panel rows, P[t * s + c]
   double2 *Gd = reinterpret_cast<double2 *>(ws + p * per + og);
   float4 *G = reinterpret_cast<float4 *>(Gd);
   float4 *Ri = reinterpret_cast<float4 *>(ws + p * per + ori);
   const int tid = threadIdx.x, nt = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   __shared__ double gmax;
-  __shared__ float ph, pl;  // the reciprocal pivot of the step, double-float
+  __shared__ float ph[16], pl[16];  // reciprocal pivots of the panel, double-float
   __shared__ double red[512];
-  __shared__ float4 row[kCholMaxS];
   double mx = 0.0;
   for (int j = tid; j < s; j += nt) mx = fmax(mx, Gd[j + (size_t)s * j].x);
   red[tid] = mx;
@@ -176,70 +181,114 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
   }
   if (tid == 0) gmax = red[0];
   __syncthreads();
-  for (size_t e = tid; e < (size_t)s * s; e += nt) G[e] = dfs(Gd[e]);  // in place: element e read, then written
+  for (size_t e = tid; e < (size_t)s * s; e += nt) G[e] = dfs(Gd[e]);  // in place
   __syncthreads();
   const double thresh = gmax * floor;
-  for (int j = 0; j < s; ++j) {
-    if (tid == 0) {
-      const float4 g = G[j + (size_t)s * j];
-      const double d = (double)g.x + (double)g.y;
-      const double piv = (d > thresh && d > 0.0) ? sqrt(d) : 0.0;
-      float h, l;
-      df_split(piv, h, l);
-      G[j + (size_t)s * j] = make_float4(h, l, 0.f, 0.f);
-      df_split(piv > 0.0 ? 1.0 / piv : 0.0, h, l);
-      ph = h;
-      pl = l;
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int j0 = 0; j0 < s; j0 += PB) {
+    const int jb = min(PB, s - j0);
+    // 1. panel rows j0..j0+jb-1, columns j0..s-1
+    for (int e = tid; e < jb * (s - j0); e += nt) {
+      const int t = e % jb, c = j0 + e / jb;
+      P[t * s + c] = G[(j0 + t) + (size_t)s * c];
     }
     __syncthreads();
-    const float ih = ph, il = pl;
-    for (int k = j + 1 + tid; k < s; k += nt) {  // row j of R, kept in shared memory too
-      const float4 r = df_scale(G[j + (size_t)s * k], ih, il);
-      G[j + (size_t)s * k] = r;
-      row[k] = r;
-    }
-    __syncthreads();
-    for (int l = j + 1 + warp; l < s; l += nw) {  // G_kl -= conj(R_jk) R_jl, j < k <= l
-      const float4 b = row[l];
-      float4 *col = G + (size_t)s * l;
-      for (int k = j + 1 + lane; k <= l; k += 32) {
-        const float4 a = row[k];
-        float4 g = col[k];
+    // 2. factor the panel in shared memory
+    for (int t = 0; t < jb; ++t) {
+      const int j = j0 + t;
+      if (tid == 0) {
+        const float4 g = P[t * s + j];
+        const double d = (double)g.x + (double)g.y;
+        const double pv = (d > thresh && d > 0.0) ? sqrt(d) : 0.0;
+        float h, l;
+        df_split(pv, h, l);
+        P[t * s + j] = make_float4(h, l, 0.f, 0.f);
+        df_split(pv > 0.0 ? 1.0 / pv : 0.0, h, l);
+        ph[t] = h;
+        pl[t] = l;
+      }
+      __syncthreads();
+      for (int c = j + 1 + tid; c < s; c += nt) P[t * s + c] = df_scale(P[t * s + c], ph[t], pl[t]);
+      __syncthreads();
+      for (int e = tid; e < (jb - t - 1) * (s - j - 1); e += nt) {  // rows below t inside the panel
+        const int u = t + 1 + e % (jb - t - 1), c = j + 1 + e / (jb - t - 1);
+        if (c < j0 + u) continue;  // only the upper triangle
+        const float4 a = P[t * s + j0 + u], b = P[t * s + c];
+        float4 g = P[u * s + c];
         df_cmac_ca(g.x, g.y, g.z, g.w, make_float4(-a.x, -a.y, -a.z, -a.w), b);
+        P[u * s + c] = g;
+      }
+      __syncthreads();
+    }
+    // 3. the panel's rows of R back to G
+    for (int e = tid; e < jb * (s - j0); e += nt) {
+      const int t = e % jb, c = j0 + e / jb;
+      G[(j0 + t) + (size_t)s * c] = c >= j0 + t ? P[t * s + c] : zero;
+    }
+    // 4. trailing triangle: G_kl -= sum_t conj(R_tk) R_tl, j0+jb <= k <= l
+    for (int l = j0 + jb + warp; l < s; l += nw) {
+      float4 *col = G + (size_t)s * l;
+      for (int k = j0 + jb + lane; k <= l; k += 32) {
+        float4 g = col[k];
+        for (int t = 0; t < jb; ++t) {
+          const float4 a = P[t * s + k];
+          df_cmac_ca(g.x, g.y, g.z, g.w, make_float4(-a.x, -a.y, -a.z, -a.w), P[t * s + l]);
+        }
         col[k] = g;
       }
     }
     __syncthreads();
   }
-  // Ri = R^-1 (upper), row by row from the bottom: Ri_ii = 1 / R_ii and
-  // Ri_ic = -(sum_{l=i+1..c} R_il Ri_lc) / R_ii; row i of R is staged in shared
-  // memory, one warp per column c with the lanes over l (Ri's columns contiguous).
-  for (size_t e = tid; e < (size_t)s * s; e += nt) Ri[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+  // Ri = R^-1 (upper), block rows B = [b0, b0+jb) from the bottom:
+  //   T(B, c) = sum_{l >= b0+jb} R(B, l) Ri(l, c)      (one pass over the rows done)
+  //   Ri(B, c) = R(B, B)^-1 (delta(B, c) - T(B, c))    (triangular solve in the block)
+  for (size_t e = tid; e < (size_t)s * s; e += nt) Ri[e] = zero;
   __syncthreads();
-  for (int i = s - 1; i >= 0; --i) {
-    for (int l = i + tid; l < s; l += nt) row[l] = G[i + (size_t)s * l];
-    if (tid == 0) {
-      const double d = (double)G[i + (size_t)s * i].x + (double)G[i + (size_t)s * i].y;
-      float h, l2;
-      df_split(d > 0.0 ? 1.0 / d : 0.0, h, l2);
-      ph = h;
-      pl = l2;
+  const int nblk = (s + PB - 1) / PB;
+  for (int bi = nblk - 1; bi >= 0; --bi) {
+    const int b0 = bi * PB, jb = min(PB, s - b0);
+    for (int e = tid; e < jb * (s - b0); e += nt) {  // R(B, b0..s-1)
+      const int t = e % jb, c = b0 + e / jb;
+      P[t * s + c] = G[(b0 + t) + (size_t)s * c];
     }
     __syncthreads();
-    const float ih = ph, il = pl;
-    for (int c = i + 1 + warp; c < s; c += nw) {
-      float rh = 0.f, rl = 0.f, jh = 0.f, jl = 0.f;
+    // T into Ri(B, c), one warp per column c, lanes over l
+    for (int c = b0 + jb + warp; c < s; c += nw) {
       const float4 *x = Ri + (size_t)s * c;
-      for (int l = i + 1 + lane; l <= c; l += 32) df_cmac(rh, rl, jh, jl, row[l], x[l]);
-      for (int o = 16; o > 0; o >>= 1) {  // double-float sums across the warp
-        const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
-        const float c2 = __shfl_xor_sync(0xffffffffu, jh, o), d2 = __shfl_xor_sync(0xffffffffu, jl, o);
-        df_mac(rh, rl, a, b, 1.f, 0.f);
-        df_mac(jh, jl, c2, d2, 1.f, 0.f);
+      for (int t = 0; t < jb; ++t) {
+        float rh = 0.f, rl = 0.f, jh = 0.f, jl = 0.f;
+        for (int l = b0 + jb + lane; l <= c; l += 32) df_cmac(rh, rl, jh, jl, P[t * s + l], x[l]);
+        for (int o = 16; o > 0; o >>= 1) {
+          const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
+          const float c2 = __shfl_xor_sync(0xffffffffu, jh, o), d2 = __shfl_xor_sync(0xffffffffu, jl, o);
+          df_mac(rh, rl, a, b, 1.f, 0.f);
+          df_mac(jh, jl, c2, d2, 1.f, 0.f);
+        }
+        if (lane == 0) Ri[(b0 + t) + (size_t)s * c] = make_float4(rh, rl, jh, jl);
       }
-      if (lane == 0) Ri[i + (size_t)s * c] = df_scale(make_float4(-rh, -rl, -jh, -jl), ih, il);
     }
-    if (tid == 0) Ri[i + (size_t)s * i] = make_float4(ih, il, 0.f, 0.f);
+    __syncthreads();
+    // triangular solve in the block, one thread per column c >= b0
+    for (int c = b0 + tid; c < s; c += nt) {
+      float4 xs[16];
+      for (int t = jb - 1; t >= 0; --t) {
+        float4 acc = (b0 + t == c) ? make_float4(1.f, 0.f, 0.f, 0.f) : zero;
+        if (c >= b0 + jb) {
+          const float4 q = Ri[(b0 + t) + (size_t)s * c];
+          acc = make_float4(-q.x, -q.y, -q.z, -q.w);
+        }
+        for (int u = t + 1; u < jb; ++u) {
+          const float4 r = P[t * s + b0 + u];
+          df_cmac(acc.x, acc.y, acc.z, acc.w, make_float4(-r.x, -r.y, -r.z, -r.w), xs[u]);
+        }
+        const float4 rd = P[t * s + b0 + t];
+        const double d = (double)rd.x + (double)rd.y;
+        float h, l;
+        df_split(d > 0.0 ? 1.0 / d : 0.0, h, l);
+        xs[t] = (b0 + t <= c) ? df_scale(acc, h, l) : zero;
+      }
+      for (int t = 0; t < jb; ++t) Ri[(b0 + t) + (size_t)s * c] = xs[t];
+    }
     __syncthreads();
   }
   double2 *Rd = reinterpret_cast<double2 *>(Ri);
@@ -518,6 +567,16 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
     h->stats.rsvd_flops += 8.0 * rows * (double)cols * k * nact;
     return e;
   };
+  auto rs_chol = [&](int nbk, char *w, size_t pr, size_t og, size_t ori, int ss, double fl) -> int {
+    const int PB = ss <= 512 ? 16 : 8;
+    const size_t smem = sizeof(float4) * (size_t)PB * ss;
+    int e2 = check_cuda(h, cudaFuncSetAttribute(k_rs_chol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "Cholesky shared memory");
+    if (e2) return e2;
+    k_rs_chol<<<nbk, 512, smem, st>>>(R->dims_d, w, pr, og, ori, ss, fl, PB);
+    TEBD_LAUNCHED(h);
+    return check_cuda(h, cudaPeekAtLastError(), "Cholesky launch");
+  };
   // CholQR of the rows x s block at `buf` (ld rows), through `tmp`: one pass for
   // the range finder's intermediate bases (only their span matters), two (CholQR2,
   // the second with 7 planes) for the final basis P; the result is left in `buf`.
@@ -525,16 +584,14 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
   auto cholqr2 = [&](size_t buf, size_t tmp, int rows, bool twice) -> int {
     int e;
     if ((e = prod(buf, rows, 1, nullptr, pstr, buf, rows, nullptr, pstr, s, s, rows, c.g, sk))) return e;
-    k_rs_chol<<<nb, 512, 0, st>>>(R->dims_d, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * sk + 9));
-    TEBD_LAUNCHED(h);
+    if ((e = rs_chol(nb, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * sk + 9)))) return e;
     if ((e = prod(buf, rows, 0, nullptr, pstr, c.ri, s, nullptr, pstr, rows, s, s, tmp, sk))) return e;
     if (!twice)  // one pass: back into buf
       return check_cuda(h, cudaMemcpy2DAsync(ws + buf, per, ws + tmp, per, sizeof(double2) * (size_t)rows * s, nb,
                                              cudaMemcpyDeviceToDevice, st),
                         "CholQR copy");
     if ((e = prod(tmp, rows, 1, nullptr, pstr, tmp, rows, nullptr, pstr, s, s, rows, c.g, fin))) return e;
-    k_rs_chol<<<nb, 512, 0, st>>>(R->dims_d, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * fin + 9));
-    TEBD_LAUNCHED(h);
+    if ((e = rs_chol(nb, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * fin + 9)))) return e;
     return prod(tmp, rows, 0, nullptr, pstr, c.ri, s, nullptr, pstr, rows, s, s, buf, fin);
   };
   // 1. padded copy

@@ -254,12 +254,16 @@ __device__ __forceinline__ void oz_digits(double x, int e, int S, unsigned short
     for (int s = 0; s < S; ++s) d[s] = 0;
     return;
   }
-  double t = ldexp(x, -e);  // |t| < 1
+  // q = rint(x 2^(7S - e)), |q| <= 2^(7S) (|x| < 2^e): one scaling by a power of two
+  // and one conversion; then balanced 7-bit digits by integer shifts, rounding to
+  // nearest at every step: D_0 in [-128, 128], D_s in [-64, 64] after it, and
+  // x - 2^e sum_s D_s 2^(-7(s+1)) = 2^(e - 7S) (x 2^(7S-e) - q), at most 2^(e-7S-1)
+  long long q = __double2ll_rn(ldexp(x, 7 * S - e));
   for (int s = 0; s < S; ++s) {
-    const double y = t * 128.0;
-    const double q = rint(y);
-    d[s] = __bfloat16_as_ushort(__float2bfloat16_rn((float)q));  // |q| <= 128: exact
-    t = y - q;                                                    // exact, |t| <= 1/2
+    const int sh = 7 * (S - 1 - s);
+    const long long D = sh ? ((q + (1LL << (sh - 1))) >> sh) : q;
+    q -= D << sh;
+    d[s] = __bfloat16_as_ushort(__float2bfloat16_rn((float)D));  // |D| <= 128: exact
   }
 }
 
