@@ -281,22 +281,38 @@ def saturated_state(Ls=L, chi=CHI, decay=16.0):
     return gam, lam
 
 
-def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=16.0):
+def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=16.0, prepare=True):
     """The odd bonds of a saturated chain, updated `steps` times (one batched sweep
     each), in plain FP64 and in the mixed form, profiled: updates/s from CUDA events
     on each chain's stream, and the roofline of each form's dominant kernel from
     that leg's own launch timings (k_gebrd on the FP64 pipe; the tensor-core
-    product kernels against the measured bf16 peak)."""
+    product kernels against the measured bf16 peak).
+
+    prepare: the legs start from the random state after one sweep of the same
+    bonds (double-float form).  Every update of a Trotter run meets a state whose
+    Schmidt rank across the bond is at most chi (the bond was truncated at its
+    last update, and the gates since then act on other bonds), so that Theta's
+    spectrum beyond chi comes from the one gate; the prepared state has that
+    property.  Without it each Theta of the random state is full rank and the
+    sweep discards a large weight -- a harder case than any step of a run."""
     import torch
 
     H = pkg.hamiltonians
     gam, lam = saturated_state(Ls, chi, decay)
     gate = H.matrix_exponential(H.bose_hubbard(Ls, D, J, U, MU)[1], DT)
     links = list(range(1, Ls, 2))
+    if prepare:
+        with pkg.Chain(Ls, D, chi, device=device, svd_mode=SVD_MODES["df"]) as c:
+            c.set_state(gam, lam)
+            c.apply_bonds(links, [gate] * len(links))
+            gam, lam = c.get_state()
     bf16_peak, bf16_src = measured_peak("bf16_tflops")
     n = D * chi
     out = {"workload": "saturated_bonds_L%d_d5_chi%d (%d bonds of a %d x %d Theta per step, lambda_k ~ exp(-k/%g))"
-                       % (Ls, chi, len(links), n, n, decay), "steps": steps}
+                       % (Ls, chi, len(links), n, n, decay), "steps": steps,
+           "start": ("random state after one sweep of the same bonds (Schmidt rank chi across each bond, "
+                     "as at every update of a run)" if prepare else
+                     "random state: full-rank Theta, large discarded weight (harder than any step of a run)")}
     finals = {}
     for name in ("fp64", "mixed"):
         c = pkg.Chain(Ls, D, chi, device=device, svd_mode=SVD_MODES["fp64" if name == "fp64" else "rsvd"])
@@ -320,7 +336,9 @@ def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=1
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         st = c.stats()
-        finals[name] = [c.two_site_rho(k) for k in links]  # device observable of each updated bond
+        num = np.diag(np.arange(D, dtype=float))
+        finals[name] = ([c.two_site_rho(k) for k in links],  # device observables of the updated bonds
+                        c.one_site_expval(num), c.local_energy(H.bose_hubbard(Ls, D, J, U, MU)))
         leg_ = {"ms_per_step": ms / steps, "value": len(links) * steps / (ms / 1e3), "unit": "updates/s"}
         if st["gebrd_ms"] > 0:
             a = st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12
@@ -343,8 +361,11 @@ def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=1
         if model is not None:
             model.close()
     out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
-    out["max_abs_err_rho2_vs_fp64"] = float(max(np.max(np.abs(a - b)) for a, b in zip(finals["fp64"],
-                                                                                         finals["mixed"])))
+    (r0, n0, e0), (r1, n1, e1) = finals["fp64"], finals["mixed"]
+    out["max_abs_err_rho2_vs_fp64"] = float(max(np.max(np.abs(a - b)) for a, b in zip(r0, r1)))
+    out["max_abs_err_vs_plain_fp64"] = {"n_i": float(np.max(np.abs(n1 - n0))),
+                                        "bond_energy": float(np.max(np.abs(e1 - e0)))}
+    out["within_error_bound"] = max(out["max_abs_err_vs_plain_fp64"].values()) <= 1e-8
     return out
 
 
@@ -576,6 +597,8 @@ def run_ours(args):
         "precision_form": prec,
         "mixed_form": mixed,
         "saturated": saturated_legs(pkg, local, args, fp64_peak) if not args.no_precision else None,
+        "saturated_random_start": (saturated_legs(pkg, local, args, fp64_peak, prepare=False)
+                                   if not args.no_precision else None),
         "saturated_chi512": (saturated_legs(pkg, local, args, fp64_peak, steps=1, Ls=32, chi=512, decay=64.0)
                              if not args.no_precision and not args.no_chi512 else None),
         **({"rank_form": {"what": "kept-rank form: per-update discarded-weight bound "
@@ -765,6 +788,10 @@ def run_saturated(args):
     links = list(range(1, L, 2))
     chain = pkg.Chain(L, D, CHI, svd_mode=SVD_MODES[args.svd])
     chain.set_theta_form(args.theta_form)
+    model = None
+    if args.svd == "rsvd":  # the mixed form's model sizes the sketches, as in the headline run's legs
+        model = load_model(pkg, 0)
+        chain.set_rsvd_model(model, MODEL_TARGET)
     chain.set_state(gam, lam)
     stream = torch.cuda.ExternalStream(chain.stream())
     for _ in range(args.warmup):
@@ -792,6 +819,8 @@ def run_saturated(args):
                     "worst_residual": st["rsvd_worst_residual"], "tc_flops": st["rsvd_flops"]}}
     print(json.dumps(out), flush=True)
     chain.close()
+    if model is not None:
+        model.close()
 
 
 def main():

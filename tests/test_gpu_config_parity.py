@@ -1,0 +1,129 @@
+"""Parity with the oracle at the sizes of the configured runs.
+
+* Bose-Hubbard L=64, d=5, chi=128, dt=0.005, 2nd order, from the seeded
+  perturbed Mott state: Trotter steps 1..20 (the bench's timed window, 1900 bond
+  updates) in plain FP64 on the GPU and in the oracle;
+* Fermi-Hubbard L=64, d=4, chi=256, Forest-Ruth at dt=0.01, from the seeded
+  random MPS made canonical on the device: two steps (442 updates of
+  1024 x 1024 Thetas);
+* number-conserving Bose-Hubbard L=128, d=5, chi=512, U_i ~ U[1,3] (seed 3),
+  dt=0.01, 2nd order, from the Mott state: three steps (573 updates), labels
+  compared exactly.
+
+The oracle runs each sweep's bonds on all host cores (oracle/pool.py).  Compared:
+the summed truncation error, every Lambda, <n_i>, every bond energy and the
+overlap of the two final states (normalised by their norms where the chain
+carries a large discarded weight).  Bond energies and the overlap of the chi >= 256
+chains are evaluated by the library's device observables (pinned to the numpy
+restatements in test_gpu_observables.py) on both final states; the rest in
+numpy.  The tolerance is written beside each comparison and reported with the
+measured deviation when it fails.
+"""
+import numpy as np
+import pytest
+
+from oracle import observables as obs
+from oracle.pool import SweepPool
+
+pytestmark = pytest.mark.gpu
+
+
+def _report(dev, tol):
+    bad = {k: v for k, v in dev.items() if not v <= tol[k]}
+    assert not bad, {"deviation": dev, "tolerance": tol}
+
+
+def _lam_dev(la, lb):
+    return float(max(np.max(np.abs(a - b)) for a, b in zip(la, lb)))
+
+
+def test_bose_hubbard_chi128_steps_1_20(pkg):
+    H = pkg.hamiltonians
+    L, d, chi, dt, steps = 64, 5, 128, 0.005, 20
+    carray = np.zeros((d, L), complex)
+    carray[1, :] = 1.0
+    gam, lam = H.perturbed_product_state(carray, chi, 1e-3, 1)
+    Hb = H.bose_hubbard(L, d, 1.0, 2.0, 0.0)
+    U = H.construct_propagators(Hb, dt, 2)
+    num = np.diag(np.arange(d, dtype=float))
+    with pkg.Chain(L, d, chi) as c:
+        c.set_state(gam, lam)
+        te = sum(c.trotter_step(U, 2) for _ in range(steps))
+        g1, l1 = c.get_state()
+        e1 = c.local_energy(Hb)
+    with SweepPool() as P:
+        rte = sum(P.trotter_step(gam, lam, U, 2) for _ in range(steps))
+    dev = {"truncerr": abs(te - rte), "lambda": _lam_dev(l1, lam),
+           "n_i": float(np.max(np.abs(obs.one_site_expval(g1, l1, num) - obs.one_site_expval(gam, lam, num)))),
+           "bond_energy": float(np.max(np.abs(e1 - obs.bond_energy(gam, lam, Hb)))),
+           "overlap": abs(abs(obs.inner_product(gam, lam, g1, l1)) - 1.0)}
+    _report(dev, {"truncerr": 1e-10, "lambda": 1e-10, "n_i": 1e-10, "bond_energy": 1e-10, "overlap": 1e-10})
+
+
+def _device_obs(pkg, L, d, chi, gam, lam, Hb, other, **kw):
+    """Bond energies of the oracle's final state and its normalised overlap with
+    the chain `other`, |<o|c>| / sqrt(<o|o> <c|c>): after a truncation the Vidal
+    form is no longer exactly canonical, so the transfer-matrix norm of either
+    state differs from 1 at the level of the discarded weight."""
+    with pkg.Chain(L, d, chi, **kw) as c:
+        if isinstance(gam, tuple):
+            c.set_state(*gam)
+        else:
+            c.set_state(gam, lam)
+        e = c.local_energy(Hb)
+        ov = abs(c.inner_product(other)) / np.sqrt(abs(c.inner_product(c)) * abs(other.inner_product(other)))
+    return e, ov
+
+
+def test_fermi_hubbard_chi256_forest_ruth_two_steps(pkg):
+    H = pkg.hamiltonians
+    L, d, chi, dt, steps = 64, 4, 256, 0.01, 2
+    rng = np.random.default_rng(2)
+    gam = [np.asfortranarray(rng.standard_normal((chi, d, chi)) + 1j * rng.standard_normal((chi, d, chi)))
+           for _ in range(L)]
+    lam = [np.full(chi, 1.0 / np.sqrt(chi)) for _ in range(L + 1)]
+    lam[0] = np.eye(chi)[0]
+    lam[L] = np.eye(chi)[0]
+    Hb = H.fermi_hubbard(L, 1.0, 4.0)
+    U = H.construct_propagators(Hb, dt, 5)
+    _, _, _, nop, _, _ = H.fermi_ops()
+    with pkg.Chain(L, d, chi) as c:
+        c.set_state(gam, lam)
+        c.canonical_form_all()
+        gam, lam = c.get_state()
+        te = sum(c.trotter_step(U, 5) for _ in range(steps))
+        g1, l1 = c.get_state()
+        e1 = c.local_energy(Hb)
+        with SweepPool() as P:
+            rte = sum(P.trotter_step(gam, lam, U, 5) for _ in range(steps))
+        e0, ov = _device_obs(pkg, L, d, chi, gam, lam, Hb, c)
+    dev = {"truncerr": abs(te - rte) / max(1.0, abs(rte)), "lambda": _lam_dev(l1, lam),
+           "n_i": float(np.max(np.abs(obs.one_site_expval(g1, l1, nop) - obs.one_site_expval(gam, lam, nop)))),
+           "bond_energy": float(np.max(np.abs(e1 - e0))), "overlap": abs(abs(ov) - 1.0)}
+    _report(dev, {"truncerr": 1e-10, "lambda": 1e-10, "n_i": 1e-10, "bond_energy": 1e-10, "overlap": 1e-10})
+
+
+def test_nc_bose_hubbard_chi512_three_steps(pkg):
+    H = pkg.hamiltonians
+    L, d, chi, N, dt, steps = 128, 5, 512, 128, 0.01, 3
+    gam, lam, ll, lr = H.initial_set_nc(L, d, chi, N)
+    Hb = H.bose_hubbard(L, d, 1.0, np.random.default_rng(3).uniform(1.0, 3.0, L))
+    U = H.construct_propagators(Hb, dt, 2)
+    num = np.diag(np.arange(d, dtype=float))
+    with pkg.Chain(L, d, chi, mode=pkg.MODE_NC, tot_num=N) as c:
+        c.set_state(gam, lam, ll, lr)
+        te = sum(c.trotter_step(U, 2) for _ in range(steps))
+        g1, l1, ll1, lr1 = c.get_state()
+        e1 = c.local_energy(Hb)
+        with SweepPool() as P:
+            rte = sum(P.trotter_step_nc(gam, lam, ll, lr, U, N, d - 1, 2) for _ in range(steps))
+        e0, ov = _device_obs(pkg, L, d, chi, (gam, lam, ll, lr), None, Hb, c, mode=pkg.MODE_NC, tot_num=N)
+    for link, (a, b) in enumerate(zip(ll1, ll), start=1):
+        assert np.array_equal(a, b), ("label_left", link)
+    for link, (a, b) in enumerate(zip(lr1, lr), start=1):
+        assert np.array_equal(a, b), ("label_right", link)
+    assert max(int(np.sum(x > 0)) for x in l1) > 4  # several charge blocks per bond by now
+    dev = {"truncerr": abs(te - rte), "lambda": _lam_dev(l1, lam),
+           "n_i": float(np.max(np.abs(obs.one_site_expval(g1, l1, num) - obs.one_site_expval(gam, lam, num)))),
+           "bond_energy": float(np.max(np.abs(e1 - e0))), "overlap": abs(abs(ov) - 1.0)}
+    _report(dev, {"truncerr": 1e-10, "lambda": 1e-10, "n_i": 1e-10, "bond_energy": 1e-10, "overlap": 1e-10})
