@@ -49,10 +49,10 @@ constexpr uint32_t kIdescBF16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)
                                 ((uint32_t)(kTcBM >> 4) << 24);
 constexpr int kExpZero = -2000;  // exponents below this mark an all-zero row
 
-int oz_stages(int S) {
-  const int per = S * (int)(kOzTileA + kOzTileB);
-  const int st = (220 * 1024) / per;
-  return st > kOzMaxStages ? kOzMaxStages : st;
+__host__ __device__ constexpr int oz_stages(int S) {
+  return (220 * 1024) / (S * (int)(kOzTileA + kOzTileB)) > kOzMaxStages
+             ? kOzMaxStages
+             : (220 * 1024) / (S * (int)(kOzTileA + kOzTileB));
 }
 size_t oz_smem(int S) { return 1024 + (size_t)oz_stages(S) * S * (kOzTileA + kOzTileB) + 512; }
 
@@ -68,13 +68,50 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
 }
 
+// 32 lanes x 16 columns of TMEM into r[0..15] without waiting; the caller waits
+// once for several loads (tmem_wait) before it reads any of them.
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+      "%14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+// Wait for this thread's TMEM loads; the empty asm statements that "modify" the
+// registers afterwards keep every use of them behind the wait.
+template <int N>
+__device__ __forceinline__ void tmem_wait(uint32_t (&r)[N]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < N; ++i) asm volatile("" : "+r"(r[i]));
+}
+
+// All MMAs of one K block (two K-steps of 16) for every digit pair of a stage:
+// da, db are the descriptors of slice 0 of A and B in the stage; slice q starts
+// q tiles further, a K-step 32 bytes further (descriptor units of 16 bytes).
+// The first MMA into a group in a chunk (K-step 0 of its first K block, pair
+// (0, g)) overwrites the accumulator.
+template <int S>
+__device__ __forceinline__ void oz_issue(uint32_t tmem, uint64_t da, uint64_t db, bool first) {
+#pragma unroll
+  for (int kk = 0; kk < kOzBK / 16; ++kk)
+#pragma unroll
+    for (int sa = 0; sa < S; ++sa)
+#pragma unroll
+      for (int sb = 0; sa + sb < S; ++sb)
+        mma_bf16(tmem + (uint32_t)((sa + sb) * kOzBN), da + (uint64_t)((sa * kOzTileA + kk * 32) >> 4),
+                 db + (uint64_t)((sb * kOzTileB + kk * 32) >> 4), (first && kk == 0 && sa == 0) ? 0u : 1u);
+}
+
+template <int S>
 __global__ void __launch_bounds__(kOzThreads, 1)
     k_tc_oz(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzBatch b,
-            int stages, int *err) {
+            int *err) {
+  constexpr int stages = oz_stages(S);
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem =
       reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  const int S = b.slices;
   unsigned char *sA = smem;                                  // [stage][slice] kOzTileA
   unsigned char *sB = sA + (size_t)stages * S * kOzTileA;    // [stage][slice] kOzTileB
   uint64_t *full = reinterpret_cast<uint64_t *>(sB + (size_t)stages * S * kOzTileB);
@@ -130,8 +167,10 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         break;
       }
       mbar_expect_tx(&full[s], bytes);
+#pragma unroll
       for (int q = 0; q < S; ++q)
         tma_load_3d(sA + (size_t)(s * S + q) * kOzTileA, &tmA, &full[s], kb * kOzBK, m0, q * b.nprob + p);
+#pragma unroll
       for (int q = 0; q < S; ++q)
         tma_load_3d(sB + (size_t)(s * S + q) * kOzTileB, &tmB, &full[s], kb * kOzBK, n0, q * b.nprob + p);
       issued = kb + 1;
@@ -144,7 +183,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   if (warp == 5) {
     // ---- MMA issuer ----
     if (lane != 0) goto finish;
-    uint32_t written = 0;
+    const uint64_t da0 = sw64_desc(su32(sA)), db0 = sw64_desc(su32(sB));
     for (int kb = 0; kb < nk; ++kb) {
       const int c = kb / kOzChunk, kc = kb % kOzChunk;
       const int s = kb % stages;
@@ -153,25 +192,14 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         atomicExch(err, 1);
         break;
       }
-      if (kc == 0) written = 0;
       if (!mbar_wait(&full[s], (kb / stages) & 1, abort)) {
         *abort = 1;
         atomicExch(err, 1);
         break;
       }
       tc_after();
-      const uint32_t a0 = su32(sA + (size_t)s * S * kOzTileA);
-      const uint32_t b0 = su32(sB + (size_t)s * S * kOzTileB);
-      for (int kk = 0; kk < kOzBK / 16; ++kk) {
-        const uint32_t off = kk * 32;  // 16 bf16 = 32 bytes per K-step
-        for (int sa = 0; sa < S; ++sa)
-          for (int sb = 0; sa + sb < S; ++sb) {
-            const int g = sa + sb;
-            mma_bf16(tmem + (uint32_t)(g * kOzBN), sw64_desc(a0 + sa * kOzTileA + off),
-                     sw64_desc(b0 + sb * kOzTileB + off), (written >> g) & 1u);
-            written |= 1u << g;
-          }
-      }
+      oz_issue<S>(tmem, da0 + (uint64_t)((s * S * kOzTileA) >> 4), db0 + (uint64_t)((s * S * kOzTileB) >> 4),
+                  kc == 0);
       mma_commit(&empty[s]);
       if (kc == kOzChunk - 1 || kb == nk - 1) mma_commit(cfull);
     }
@@ -180,10 +208,16 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   }
 
   {
-  // ---- epilogue (warps 0-3): exact chunk sums into FP64 ----
-  double acc[kOzBN];
+  // ---- epilogue (warps 0-3): exact chunk sums into 64-bit integers ----
+  // acc = sum_g G_g 2^(7 (S-1-g) - R) over the chunks, in units of
+  // 2^(R - 7 (S+1)): R keeps the sum inside 63 bits (|G_0| < 2^23 per chunk);
+  // groups shifted right by it are rounded, 2^-60 below the total at most.
+  int lg = 0;
+  while ((1 << lg) < nchunks) ++lg;
+  const int R = max(0, 25 + lg + 7 * (S - 1) - 63);
+  long long acc[kOzBN];
 #pragma unroll
-  for (int i = 0; i < kOzBN; ++i) acc[i] = 0.0;
+  for (int i = 0; i < kOzBN; ++i) acc[i] = 0;
   bool ok = true;
   const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
   for (int c = 0; c < nchunks; ++c) {
@@ -192,14 +226,24 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       break;
     }
     tc_after();
+#pragma unroll 1
     for (int g = 0; g < S; ++g) {
-      const double sc = ldexp(1.0, -7 * (g + 2));
+      const int sh = 7 * (S - 1 - g) - R;
 #pragma unroll
-      for (int c0 = 0; c0 < kOzBN; c0 += 16) {
-        float v[16];
-        tmem_ld16(lane_base + (uint32_t)(g * kOzBN + c0), v);
+      for (int h = 0; h < kOzBN; h += 32) {
+        uint32_t r[32];
+        tmem_ld16_async(lane_base + (uint32_t)(g * kOzBN + h), r);
+        tmem_ld16_async(lane_base + (uint32_t)(g * kOzBN + h + 16), r + 16);
+        tmem_wait(r);
+        if (sh >= 0) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) acc[c0 + i] = fma(sc, (double)v[i], acc[c0 + i]);
+          for (int i = 0; i < 32; ++i) acc[h + i] += (long long)__float2int_rn(__uint_as_float(r[i])) << sh;
+        } else {
+          const long long half = 1LL << (-sh - 1);
+#pragma unroll
+          for (int i = 0; i < 32; ++i)
+            acc[h + i] += ((long long)__float2int_rn(__uint_as_float(r[i])) + half) >> (-sh);
+        }
       }
     }
     tc_before();
@@ -216,6 +260,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                             : b.out + (size_t)p * b.out_stride;
       const int ea = b.a_exp[(size_t)p * b.m_pad + row];
       const long long cs = b.cs ? b.cs : mp;  // cs == 0: column stride = this problem's row count
+      const int eu = R - 7 * (S + 1);          // exponent of the accumulator's unit
 #pragma unroll
       for (int t = 0; t < kOzBN / 2; ++t) {
         const int j = n0 / 2 + t;
@@ -223,7 +268,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
           const int eb = b.b_exp[(size_t)p * (b.n_pad / 2) + j];
           double2 r = make_double2(0.0, 0.0);
           if (ea > kExpZero && eb > kExpZero)
-            r = make_double2(b.alpha * ldexp(acc[2 * t], ea + eb), b.alpha * ldexp(acc[2 * t + 1], ea + eb));
+            r = make_double2(b.alpha * ldexp((double)acc[2 * t], ea + eb + eu),
+                             b.alpha * ldexp((double)acc[2 * t + 1], ea + eb + eu));
           double2 *o = out + (long long)row * b.rs + (long long)j * cs;
           if (b.accumulate) {
             const double2 q = *o;
@@ -448,11 +494,22 @@ cudaError_t oz_gemm_launch(const OzBatch &b, int *err_d, cudaStream_t st) {
       !oz_map(&mb, b.b_dig, b.k_pad, b.n_pad, b.slices * b.nprob, kOzBN))
     return cudaErrorInvalidValue;
   const size_t smem = oz_smem(b.slices);
-  cudaError_t e = cudaFuncSetAttribute(k_tc_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
   dim3 grid(b.m_pad / kTcBM, b.n_pad / kOzBN, b.nprob);
-  k_tc_oz<<<grid, kOzThreads, smem, st>>>(ma, mb, b, oz_stages(b.slices), err_d);
-  return cudaPeekAtLastError();
+  auto go = [&](auto kern) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kOzThreads, smem, st>>>(ma, mb, b, err_d);
+    return cudaPeekAtLastError();
+  };
+  switch (b.slices) {
+    case 1: return go(k_tc_oz<1>);
+    case 2: return go(k_tc_oz<2>);
+    case 3: return go(k_tc_oz<3>);
+    case 4: return go(k_tc_oz<4>);
+    case 5: return go(k_tc_oz<5>);
+    case 6: return go(k_tc_oz<6>);
+    default: return go(k_tc_oz<7>);
+  }
 }
 
 cudaError_t oz_pack_a(const double2 *src, long long pstride, int ld, int rows, int cols, int trans, int conj,
