@@ -281,7 +281,8 @@ def saturated_state(Ls=L, chi=CHI, decay=16.0):
     return gam, lam
 
 
-def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=16.0, prepare=True):
+def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=16.0, prepare=True,
+                   tune=("fp64", "mixed")):
     """The odd bonds of a saturated chain, updated `steps` times (one batched sweep
     each), in plain FP64 and in the mixed form, profiled: updates/s from CUDA events
     on each chain's stream, and the roofline of each form's dominant kernel from
@@ -294,7 +295,10 @@ def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=1
     last update, and the gates since then act on other bonds), so that Theta's
     spectrum beyond chi comes from the one gate; the prepared state has that
     property.  Without it each Theta of the random state is full rank and the
-    sweep discards a large weight -- a harder case than any step of a run."""
+    sweep discards a large weight -- a harder case than any step of a run.
+
+    tune: the legs whose chain runs the autotuner (tebd_autotune) on the batch
+    before it is timed; its default and tuned batch times are reported."""
     import torch
 
     H = pkg.hamiltonians
@@ -325,6 +329,10 @@ def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=1
         st_ = torch.cuda.ExternalStream(c.stream(), device=device)
         c.apply_bonds(links, [gate] * len(links))  # warm-up (workspaces, kernels)
         c.set_state(gam, lam)
+        tuned = None
+        if name in tune:  # untimed: the chain is left as it was
+            b_ms, t_ms = c.autotune(links, [gate] * len(links))
+            tuned = {"default_batch_ms": b_ms, "tuned_batch_ms": t_ms}
         c.reset_stats()
         c.set_profiling(True)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -339,7 +347,8 @@ def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=1
         num = np.diag(np.arange(D, dtype=float))
         finals[name] = ([c.two_site_rho(k) for k in links],  # device observables of the updated bonds
                         c.one_site_expval(num), c.local_energy(H.bose_hubbard(Ls, D, J, U, MU)))
-        leg_ = {"ms_per_step": ms / steps, "value": len(links) * steps / (ms / 1e3), "unit": "updates/s"}
+        leg_ = {"ms_per_step": ms / steps, "value": len(links) * steps / (ms / 1e3), "unit": "updates/s",
+                "autotune": tuned}
         if st["gebrd_ms"] > 0:
             a = st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12
             leg_["roofline_k_gebrd"] = {"bound": "fp64", "achieved": a, "peak": fp64_peak, "unit": "TFLOP/s",
@@ -597,10 +606,12 @@ def run_ours(args):
         "precision_form": prec,
         "mixed_form": mixed,
         "saturated": saturated_legs(pkg, local, args, fp64_peak) if not args.no_precision else None,
-        "saturated_random_start": (saturated_legs(pkg, local, args, fp64_peak, prepare=False)
+        "saturated_random_start": (saturated_legs(pkg, local, args, fp64_peak, prepare=False, tune=())
                                    if not args.no_precision else None),
-        "saturated_chi512": (saturated_legs(pkg, local, args, fp64_peak, steps=1, Ls=32, chi=512, decay=64.0)
+        "saturated_chi512": (saturated_legs(pkg, local, args, fp64_peak, steps=1, Ls=32, chi=512, decay=64.0,
+                                            tune=("mixed",))
                              if not args.no_precision and not args.no_chi512 else None),
+        "autotune_table": pkg.get_tuning(local) if not args.no_precision else None,
         **({"rank_form": {"what": "kept-rank form: per-update discarded-weight bound "
                                   "(tebd_set_rank_bound), Lambda beyond the kept rank exactly zero",
                           "legs": rank_form}} if rank_form else {}),
@@ -763,11 +774,14 @@ def run_fermi(args):
 
 # ---------------------------------------------------------------------------
 # saturated-bond batch (extra line, not the headline): the cost regime that
-# dominates the configured run after step ~50.  The same chain shape (L=64, d=5,
-# chi=128) with every Lambda full (lambda_k ~ exp(-k/16), normalised) and complex
-# Gaussian Gammas (seed 5): each of the 32 odd bonds has a full 640 x 640 Theta.
-# One step = one batched TwoSiteOp sweep over the 32 odd bonds with the
-# Bose-Hubbard bond gate exp(-i dt h) (dt = 0.005).
+# dominates the configured run after step ~50.  The chain (default L=64, d=5,
+# chi=128; --sat-L, --sat-chi, --sat-decay) with every Lambda full
+# (lambda_k ~ exp(-k/decay), normalised) and complex Gaussian Gammas (seed 5),
+# after one sweep of the odd bonds in the double-float form (--random-start
+# skips it): each odd bond has a full (d chi) x (d chi) Theta.  One step = one
+# batched TwoSiteOp sweep over the odd bonds with the Bose-Hubbard bond gate
+# exp(-i dt h) (dt = 0.005).  --svd rsvd loads the trained model as the mixed
+# form does.
 # ---------------------------------------------------------------------------
 def run_saturated(args):
     import torch
@@ -777,16 +791,16 @@ def run_saturated(args):
     ge.build()
     pkg = ge.load_package()
     H = pkg.hamiltonians
-    rng = np.random.default_rng(5)
-    gam = [np.asfortranarray(rng.standard_normal((CHI, D, CHI)) + 1j * rng.standard_normal((CHI, D, CHI)))
-           for _ in range(L)]
-    lam = []
-    for _ in range(L + 1):
-        l = np.exp(-np.arange(CHI) / 16.0)
-        lam.append(l / np.linalg.norm(l))
-    gate = H.matrix_exponential(H.bose_hubbard(L, D, J, U, MU)[1], DT)
-    links = list(range(1, L, 2))
-    chain = pkg.Chain(L, D, CHI, svd_mode=SVD_MODES[args.svd])
+    Ls, chi = args.sat_L, args.sat_chi
+    gam, lam = saturated_state(Ls, chi, args.sat_decay)
+    gate = H.matrix_exponential(H.bose_hubbard(Ls, D, J, U, MU)[1], DT)
+    links = list(range(1, Ls, 2))
+    if not args.random_start:
+        with pkg.Chain(Ls, D, chi, svd_mode=SVD_MODES["df"]) as c:
+            c.set_state(gam, lam)
+            c.apply_bonds(links, [gate] * len(links))
+            gam, lam = c.get_state()
+    chain = pkg.Chain(Ls, D, chi, svd_mode=SVD_MODES[args.svd])
     chain.set_theta_form(args.theta_form)
     model = None
     if args.svd == "rsvd":  # the mixed form's model sizes the sketches, as in the headline run's legs
@@ -796,6 +810,7 @@ def run_saturated(args):
     stream = torch.cuda.ExternalStream(chain.stream())
     for _ in range(args.warmup):
         chain.apply_bonds(links, [gate] * len(links))
+    chain.set_state(gam, lam)
     chain.reset_stats()
     chain.set_profiling(True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -807,14 +822,16 @@ def run_saturated(args):
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     st = chain.stats()
-    out = {"metric": "two-site updates/sec, saturated bonds (640 x 640 Theta)",
+    n = D * chi
+    out = {"metric": "two-site updates/sec, saturated bonds (%d x %d Theta)" % (n, n),
            "value": len(links) * args.steps / (ms / 1e3), "unit": "updates/s", "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps,
-           "config": {"workload": "saturated_bonds_L64_d5_chi128", "bonds_per_step": len(links),
-                      "theta_form": args.theta_form},
+           "config": {"workload": "saturated_bonds_L%d_d5_chi%d" % (Ls, chi), "bonds_per_step": len(links),
+                      "theta_form": args.theta_form, "decay": args.sat_decay,
+                      "start": "random" if args.random_start else "random + one double-float sweep"},
            "gebrd_tflops": st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12 if st["gebrd_ms"] > 0 else None,
            "gebrd_share": st["gebrd_ms"] / ms, "bidiag_share": st["bidiag_ms"] / ms,
-           "gpu_launches": st["kernel_launches"],
+           "tc_share": st["tc_ms"] / ms, "gpu_launches": st["kernel_launches"],
            "rsvd": {"updates": st["rsvd_updates"], "fallbacks": st["rsvd_fallbacks"],
                     "worst_residual": st["rsvd_worst_residual"], "tc_flops": st["rsvd_flops"]}}
     print(json.dumps(out), flush=True)
@@ -823,13 +840,174 @@ def run_saturated(args):
         model.close()
 
 
+# ---------------------------------------------------------------------------
+# learned-rank configuration (extra line, not the headline): spin-1 Heisenberg
+# chain L=128, J=1, Delta=1, single-ion anisotropy D_i ~ U[-0.5, 0.5] (seed 4),
+# from a seeded random MPS at chi=64 (complex Gaussian Gammas, seed 4, made
+# canonical on the device) growing to chi_max=1024; 2nd order, dt=0.01; kept
+# rank: discarded weight <= 1e-10 per update (tebd_set_rank_bound).  The same
+# steps run in plain FP64 and in the learned-rank form (randomized route sized
+# by the trained model, Theta on the tensor cores, the full SVD as fallback and
+# judge); per-step times and the final observables are compared.  Ranks reach
+# 1024 (3072 x 3072 Thetas) in the second step; a saturated plain-FP64 step takes
+# minutes, so --spin1-steps (default 2) bounds the run.
+# ---------------------------------------------------------------------------
+S1_L, S1_D, S1_CHI0, S1_CHI, S1_DT, S1_BOUND = 128, 3, 64, 1024, 0.01, 1e-10
+
+
+def spin1_state(pkg):
+    rng = np.random.default_rng(4)
+    g = [np.asfortranarray(rng.standard_normal((S1_CHI0, S1_D, S1_CHI0)) +
+                           1j * rng.standard_normal((S1_CHI0, S1_D, S1_CHI0))) for _ in range(S1_L)]
+    lm = [np.full(S1_CHI0, 1.0 / np.sqrt(S1_CHI0)) for _ in range(S1_L + 1)]
+    lm[0] = np.eye(S1_CHI0)[0]
+    lm[S1_L] = np.eye(S1_CHI0)[0]
+    with pkg.Chain(S1_L, S1_D, S1_CHI0) as c:
+        c.set_state(g, lm)
+        c.canonical_form_all()
+        g, lm = c.get_state()
+    gam, lam = [], []
+    for x in g:  # embedded in chi_max storage: the rest exactly zero
+        y = np.zeros((S1_CHI, S1_D, S1_CHI), complex, order="F")
+        y[:S1_CHI0, :, :S1_CHI0] = x
+        gam.append(y)
+    for x in lm:
+        y = np.zeros(S1_CHI)
+        y[:S1_CHI0] = x
+        lam.append(y)
+    return gam, lam
+
+
+def run_spin1(args):
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    pkg = ge.load_package()
+    H = pkg.hamiltonians
+    Di = np.random.default_rng(4).uniform(-0.5, 0.5, S1_L)
+    Hb = H.spin1_xxz_anisotropy(S1_L, 1.0, 1.0, Di)
+    Udt = H.construct_propagators(Hb, S1_DT, 2)
+    gam, lam = spin1_state(pkg)
+    sz = H.spin_ops(1.0)[2]
+    per_step = (S1_L // 2) * 2 + (S1_L - 1) // 2
+    legs = {}
+    for name in ("fp64", "learned"):
+        c = pkg.Chain(S1_L, S1_D, S1_CHI, svd_mode=SVD_MODES["fp64" if name == "fp64" else "rsvd"])
+        c.set_rank_bound(S1_BOUND)
+        model = None
+        if name == "learned":
+            c.set_theta_form(107)
+            model = load_model(pkg, 0)
+            c.set_rsvd_model(model, MODEL_TARGET)
+        c.set_state(gam, lam)
+        c.reset_stats()
+        c.set_profiling(True)
+        stream = torch.cuda.ExternalStream(c.stream())
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.spin1_steps + 1)]
+        torch.cuda.synchronize()
+        evs[0].record(stream)
+        ranks = []
+        for k in range(args.spin1_steps):
+            c.trotter_step(Udt, 2)
+            evs[k + 1].record(stream)
+            ranks.append(int(max(np.sum(c.get_lambda(l) > 0) for l in range(2, S1_L + 1))))
+        torch.cuda.synchronize()
+        step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.spin1_steps)]
+        st = c.stats()
+        legs[name] = {"step_ms": step_ms, "max_rank_after_step": ranks,
+                      "obs": (c.one_site_expval(sz), c.local_energy(Hb), c.chain_entropy()),
+                      "rsvd": {"updates": st["rsvd_updates"], "fallbacks": st["rsvd_fallbacks"],
+                               "skipped_by_model": st["rsvd_skipped"],
+                               "worst_residual": st["rsvd_worst_residual"]},
+                      "tc_share": st["tc_ms"] / max(sum(step_ms), 1e-9)}
+        c.close()
+        if model is not None:
+            model.close()
+    f, m = legs["fp64"], legs["learned"]
+    v = per_step * args.spin1_steps / (sum(f["step_ms"]) / 1e3)
+    mv = per_step * args.spin1_steps / (sum(m["step_ms"]) / 1e3)
+    err = {"sz_i": float(np.max(np.abs(m["obs"][0] - f["obs"][0]))),
+           "bond_energy": float(np.max(np.abs(m["obs"][1] - f["obs"][1]))),
+           "entropy": float(np.max(np.abs(m["obs"][2] - f["obs"][2])))}
+    out = {"metric": "two-site updates/sec, spin-1 chi 64 -> 1024 (learned-rank form vs plain FP64)",
+           "value": mv, "unit": "updates/s", "steps": args.spin1_steps,
+           "config": {"workload": "spin1_anisotropy_L128_d3_chi64_to_1024", "L": S1_L, "d": S1_D,
+                      "chi0": S1_CHI0, "chi_max": S1_CHI, "dt": S1_DT, "trotter_order": 2, "J": 1.0, "Delta": 1.0,
+                      "D_i": "uniform[-0.5,0.5] seed 4", "rank_bound": S1_BOUND,
+                      "initial": "random MPS chi=64 (seed 4) made canonical with CanonicalFormAll"},
+           "plain_fp64": {"value": v, "unit": "updates/s", "step_ms": f["step_ms"],
+                          "max_rank_after_step": f["max_rank_after_step"]},
+           "learned": {"value": mv, "unit": "updates/s", "step_ms": m["step_ms"],
+                       "max_rank_after_step": m["max_rank_after_step"], "rsvd": m["rsvd"],
+                       "tensor_product_share": m["tc_share"]},
+           "speedup_vs_plain_fp64": mv / v, "max_abs_err_vs_plain_fp64": err, "error_bound": 1e-8,
+           "within_error_bound": max(err.values()) <= 1e-8}
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# tensor-core product micro-benchmark (extra line): one batched complex product
+# C_p = A_p B_p through the C ABI (tebd_zgemm_tc) at the randomized route's
+# shapes, operands from a seeded normal generator on the device, checked against
+# torch's complex128 product; --zgemm-shape NBxMxNxK, --zgemm-form 107 (7 bf16
+# digit planes), 3 (3xTF32) or 1 (1xTF32).
+# ---------------------------------------------------------------------------
+def run_zgemm(args):
+    import torch
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    pkg = ge.load_package()
+    lib = pkg.load_library()
+    nb, m, n, k = (int(x) for x in args.zgemm_shape.split("x"))
+    g = torch.Generator(device="cuda").manual_seed(0)
+    A = torch.randn((nb, k, m), dtype=torch.complex128, device="cuda", generator=g)
+    B = torch.randn((nb, n, k), dtype=torch.complex128, device="cuda", generator=g)
+    C = torch.zeros((nb, n, m), dtype=torch.complex128, device="cuda")
+
+    def call():
+        rc = lib.tebd_zgemm_tc(nb, m, n, k, A.data_ptr(), k * m, m, B.data_ptr(), n * k, k, C.data_ptr(), n * m, m,
+                               args.zgemm_form, None)
+        if rc:
+            raise RuntimeError("tebd_zgemm_tc failed: %d" % rc)
+
+    for _ in range(max(1, args.warmup)):
+        call()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    ref = torch.einsum("bkm,bnk->bnm", A, B)
+    err = ((C - ref).abs().max() / ref.abs().max()).item()
+    f = args.zgemm_form
+    mp, np_ = -(-m // 128) * 128, -(-2 * n // (64 if f > 100 else 128)) * (64 if f > 100 else 128)
+    kp = -(-2 * k // 32) * 32
+    pairs = (f - 100) * (f - 99) // 2 if f > 100 else 3 if f == 3 else 1
+    mma = pairs * 2.0 * mp * np_ * kp * nb
+    print(json.dumps({"metric": "batched complex product through tebd_zgemm_tc (operand packing included)",
+                      "shape": args.zgemm_shape, "form": f, "ms_per_call": ms, "calls": args.steps,
+                      "fp64_class_tflops": 8.0 * nb * m * n * k / ms / 1e9,
+                      "tensor_tflops_issued": mma / ms / 1e9, "rel_err_vs_complex128": err}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "nc", "saturated", "fermi_hubbard"])
+    ap.add_argument("--workload", default="headline",
+                    choices=["headline", "nc", "saturated", "fermi_hubbard", "spin1", "zgemm"])
+    ap.add_argument("--zgemm-shape", default="2x2560x640x2560", help="--workload zgemm: NBxMxNxK")
+    ap.add_argument("--zgemm-form", type=int, default=107, help="--workload zgemm: 107, 3 or 1")
+    ap.add_argument("--spin1-steps", type=int, default=2, help="--workload spin1: Trotter steps per leg")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--svd", default="fp64", choices=sorted(SVD_MODES))
     ap.add_argument("--save-obs", default=None, help="write final <n_i>, bond energies, Lambdas (npz)")
@@ -839,6 +1017,10 @@ def main():
                     help="extra legs of the kept-rank form at these discarded-weight bounds (FP64 and "
                          "double-float), with speedup and observable errors against the plain run")
     ap.add_argument("--cpu-updates", type=int, default=2)
+    ap.add_argument("--sat-L", type=int, default=L, help="--workload saturated: chain length")
+    ap.add_argument("--sat-chi", type=int, default=CHI, help="--workload saturated: chi")
+    ap.add_argument("--sat-decay", type=float, default=16.0, help="--workload saturated: lambda_k ~ exp(-k/decay)")
+    ap.add_argument("--random-start", action="store_true", help="--workload saturated: no preparing sweep")
     ap.add_argument("--theta-form", type=int, default=0,
                     help="Theta formation: 0 CUDA cores, 3 = 3xTF32, 100+S = S bf16 digit planes (tensor cores)")
     ap.add_argument("--outdir", default=os.path.join(ROOT, "bench_out"),
@@ -853,6 +1035,10 @@ def main():
         run_saturated(args)
     elif args.workload == "fermi_hubbard":
         run_fermi(args)
+    elif args.workload == "spin1":
+        run_spin1(args)
+    elif args.workload == "zgemm":
+        run_zgemm(args)
     else:
         run_ours(args)
 

@@ -317,6 +317,31 @@ int tebd_get_stats(tebd_handle *h, tebd_stats *stats);
 int tebd_reset_stats(tebd_handle *h);
 /* Measured FP64 FMA throughput of the device (TFLOP/s), by a short DFMA loop. */
 int tebd_measure_fp64_peak(int device, double *tflops);
+
+/* Autotuner of the SVD routes' launch shapes (no reference counterpart; the
+ * reference has no GPU launches).  Times candidate shapes on the batch of bonds
+ * `links` (at most one batch: the first nslots bonds, none sharing a site) with
+ * their gates, as tebd_apply_bonds would update them: the default choice, each
+ * cluster size 1..8 of the bidiagonalisation, each bisection team of 1, 2, 4, 8
+ * lanes with the best cluster, and, when the randomized route runs, each
+ * cluster of 1, 2, 4, 8 CTAs per bond and each panel of 4, 8, 16 rows of its
+ * Cholesky.  The fastest (by more than 1 %) is kept in
+ * a table per device under (route, largest compacted dimension rounded up to
+ * 64, bonds rounded up to a power of two), which every later batch on the device
+ * uses.  Shapes change no result beyond rounding.  The chain is left as it was
+ * (the touched Gammas, Lambdas and labels are restored after every trial) and
+ * the statistics are not counted.  base_ms / best_ms (either may be NULL): the
+ * batch's time with the default and with the chosen shape. */
+int tebd_autotune(tebd_handle *h, int nbonds, const int *links, const double *const *gates, double *base_ms,
+                  double *best_ms);
+/* The device's table: up to max_entries rows of 8 ints (route: 0 FP64
+ * bidiagonal, 1 double-float bidiagonal, 2 randomized-route Cholesky; dimension
+ * bucket; bonds bucket; bidiagonalisation cluster size; bisection team size;
+ * Cholesky cluster size; Cholesky panel height -- 0 = the default; batch time
+ * in microseconds); *count = rows in the table. */
+int tebd_get_tuning(int device, int *entries, int max_entries, int *count);
+/* Empty the device's table (the defaults apply again). */
+int tebd_clear_tuning(int device);
 /* The handle's CUDA stream (a cudaStream_t), for callers that time or order
  * their own work against the library's. */
 void *tebd_get_stream(tebd_handle *h);

@@ -209,6 +209,22 @@ INTERFACE
     INTEGER(C_INT), VALUE :: device
     REAL(C_DOUBLE) :: tflops
   END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_autotune(h, nbonds, links, gates, base_ms, best_ms) BIND(C, NAME='tebd_autotune')
+    IMPORT :: C_INT, C_PTR
+    TYPE(C_PTR), VALUE :: h
+    INTEGER(C_INT), VALUE :: nbonds
+    TYPE(C_PTR), VALUE :: links, gates, base_ms, best_ms
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_get_tuning(device, entries, max_entries, count) BIND(C, NAME='tebd_get_tuning')
+    IMPORT :: C_INT
+    INTEGER(C_INT), VALUE :: device, max_entries
+    INTEGER(C_INT) :: entries(8, *)
+    INTEGER(C_INT) :: count
+  END FUNCTION
+  INTEGER(C_INT) FUNCTION tebd_clear_tuning(device) BIND(C, NAME='tebd_clear_tuning')
+    IMPORT :: C_INT
+    INTEGER(C_INT), VALUE :: device
+  END FUNCTION
   TYPE(C_PTR) FUNCTION tebd_get_stream(h) BIND(C, NAME='tebd_get_stream')
     IMPORT :: C_PTR
     TYPE(C_PTR), VALUE :: h

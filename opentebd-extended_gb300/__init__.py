@@ -8,4 +8,5 @@ from .tebd import (  # noqa: F401
     Chain, Mlp, TebdError, TrotterStep, TwoSiteOp, TwoSiteOpNC, load_library,
     OneSiteExpVal, TotalEnergy, LocalEnergy, InnerProduct, ChainEntropy,
     MODE_DENSE, MODE_NC, SVD_FP64, SVD_JACOBI, SVD_BIDIAG, SVD_QRJ, SVD_DF, SVD_RSVD, EXPORTED_SYMBOLS, measure_fp64_peak,
+    get_tuning, clear_tuning,
 )

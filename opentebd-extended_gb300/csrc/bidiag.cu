@@ -1687,7 +1687,9 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
     const int cmax = std::max(1, std::min(8, (nmax + 127) / 128));
     int nbd = 0;  // bonds on this route (the others' clusters exit at once)
     for (int s = 0; s < nb; ++s) nbd += b.path_h[s] != kPathQRJ;
+    const TuneParams tp = tune_lookup(h, dfp ? 1 : 0, nmax, nbd);
     int C = 1;
+    bool tuned_ok = false;
     double best = 1e300;
     for (int c = 1; c <= cmax; ++c) {
       cfg.gridDim = dim3(c, nb, 1);
@@ -1697,11 +1699,18 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
         cudaGetLastError();
         continue;
       }
+      tuned_ok |= c == tp.cluster;
       const double cost = (double)((nbd + ncl - 1) / ncl) / c;
       if (cost < best * (1.0 - 1e-9)) {
         best = cost;
         C = c;
       }
+    }
+    if (tp.cluster > 0) {  // the autotuner's size, when the launch can use it
+      if (tuned_ok)
+        C = tp.cluster;
+      else
+        tune_reject(h);
     }
     cfg.gridDim = dim3(C, nb, 1);
     attr[0].val.clusterDim.x = C;
@@ -1729,8 +1738,10 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const double values = (double)nb * kk, slots_resident = 2048.0 * std::max(sms, 1);
-    const int team = values * 8 <= slots_resident ? 8 : values * 4 <= slots_resident ? 4
-                     : values * 2 <= slots_resident ? 2 : 1;
+    int team = values * 8 <= slots_resident ? 8 : values * 4 <= slots_resident ? 4
+               : values * 2 <= slots_resident ? 2 : 1;
+    const TuneParams tp = tune_lookup(h, b.dfp ? 1 : 0, nmax, nb);
+    if (tp.team == 1 || tp.team == 2 || tp.team == 4 || tp.team == 8) team = tp.team;
     auto kern = team == 8 ? k_bd_sigma<8> : team == 4 ? k_bd_sigma<4> : team == 2 ? k_bd_sigma<2> : k_bd_sigma<1>;
     if ((rc = check_cuda(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                          "bisection shared memory")))

@@ -536,8 +536,8 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
         for (int s = 0; s < nb; ++s) {
           const int mn = std::min(cps[s].m, cps[s].n);
           rank[s] = std::min(h->chi, mn);
-          // the sketch is at most 1024 wide (its Cholesky stages one row of R in shared memory)
-          h->path_h[s] = (allow[s] && rsvd_candidate(h, cps[s]) && mn >= sketch + 16 && sketch <= 1024)
+          // the sketch is at most kRsvdMaxSketch wide (its Cholesky stages panels of R in shared memory)
+          h->path_h[s] = (allow[s] && rsvd_candidate(h, cps[s]) && mn >= sketch + 16 && sketch <= kRsvdMaxSketch)
                              ? kPathRsvd
                              : kPathQRJ;
           nrs += h->path_h[s] == kPathRsvd;
@@ -601,6 +601,13 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
   if (f_pin[5]) return set_error(h, TEBD_ERR_NC_BLOCKS, "charge label outside the block range");
   return TEBD_OK;
 }
+
+namespace tebd {
+// one batch of at most nslots non-overlapping bonds (the autotuner's trials)
+int run_bond_batch(tebd_handle *h, int nb, const int *links, const double *const *gates, double *truncerr) {
+  return run_batch(h, nb, links, gates, truncerr);
+}
+}  // namespace tebd
 
 static int apply_bonds_impl(tebd_handle *h, int nbonds, const int *links,
                             const double *const *gates, double *truncerr) {

@@ -35,6 +35,8 @@
 
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
 #include "df.cuh"
 #include "tc_gemm.cuh"
 
@@ -130,7 +132,6 @@ __global__ void k_rs_pad(const Slot *slots, const RsDims *dims, double2 *ws, siz
 // same 16 bytes as a double2 -- and Ri is converted back to FP64 at the end.
 // Row j of R is staged in shared memory at step j; the trailing update runs one
 // warp per column with the lanes down the column (contiguous in memory).
-constexpr int kCholMaxS = 1024;
 
 __device__ __forceinline__ float4 df_scale(float4 v, float sh, float sl) {  // v * (sh + sl)
   float4 r;
@@ -158,21 +159,33 @@ __device__ __forceinline__ void df_split(double x, float &h, float &l) {
 // update per panel; the inverse runs block rows from the bottom, each a product
 // with the rows already inverted (one pass) and a triangular solve inside the
 // block.  Dynamic shared memory: PB x s float4.
+//
+// A cluster of C CTAs (grid x = C, y = bond) shares one bond.  Every CTA factors
+// each panel itself (the same rows and the same code give the same R rows), then
+// updates the trailing columns l = rank (mod C); one cluster barrier per panel
+// orders those updates before the next panel's rows are read, and rank 0 writes
+// the factored rows back to G one panel later (once every CTA has read them).
+// The inverse's columns are independent: each CTA solves its own, c = rank
+// (mod C).  Reads of G that another CTA may have written go to L2 (ld.global.cg).
 __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, size_t per, size_t og, size_t ori,
                                                  int s, double floor, int PB) {
-  const int p = blockIdx.x;
-  if (dims[p].s == 0) return;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks(), rank = (int)cluster.block_rank();
+  const int p = blockIdx.y;
+  if (dims[p].s == 0) return;  // uniform over the cluster: all its CTAs serve bond p
   extern __shared__ float4 P[];  // PB x s: panel rows, P[t * s + c]
   double2 *Gd = reinterpret_cast<double2 *>(ws + p * per + og);
   float4 *G = reinterpret_cast<float4 *>(Gd);
   float4 *Ri = reinterpret_cast<float4 *>(ws + p * per + ori);
   const int tid = threadIdx.x, nt = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  auto own = [&](int x) { return x + ((rank - x) % C + C) % C; };  // first column >= x of this CTA
   __shared__ double gmax;
   __shared__ float ph[16], pl[16];  // reciprocal pivots of the panel, double-float
   __shared__ double red[512];
   double mx = 0.0;
-  for (int j = tid; j < s; j += nt) mx = fmax(mx, Gd[j + (size_t)s * j].x);
+  for (int j = tid; j < s; j += nt) mx = fmax(mx, __ldcg(&Gd[j + (size_t)s * j]).x);
   red[tid] = mx;
   __syncthreads();
   for (int w = nt / 2; w > 0; w >>= 1) {
@@ -180,17 +193,27 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
     __syncthreads();
   }
   if (tid == 0) gmax = red[0];
-  __syncthreads();
-  for (size_t e = tid; e < (size_t)s * s; e += nt) G[e] = dfs(Gd[e]);  // in place
-  __syncthreads();
+  cluster.sync();  // every CTA has read the FP64 diagonal before it is converted
+  for (int c = own(0); c < s; c += C)
+    for (int r = tid; r < s; r += nt) G[r + (size_t)s * c] = dfs(__ldcg(&Gd[r + (size_t)s * c]));  // in place
+  cluster.sync();
   const double thresh = gmax * floor;
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto write_back = [&](int j0, int jb) {  // rank 0: the factored rows j0.. of the panel in P
+    for (int e = tid; e < jb * (s - j0); e += nt) {
+      const int t = e % jb, c = j0 + e / jb;
+      G[(j0 + t) + (size_t)s * c] = c >= j0 + t ? P[t * s + c] : zero;
+    }
+  };
+  int prev = -1;
   for (int j0 = 0; j0 < s; j0 += PB) {
     const int jb = min(PB, s - j0);
+    if (rank == 0 && prev >= 0) write_back(prev, min(PB, s - prev));
+    __syncthreads();
     // 1. panel rows j0..j0+jb-1, columns j0..s-1
     for (int e = tid; e < jb * (s - j0); e += nt) {
       const int t = e % jb, c = j0 + e / jb;
-      P[t * s + c] = G[(j0 + t) + (size_t)s * c];
+      P[t * s + c] = __ldcg(&G[(j0 + t) + (size_t)s * c]);
     }
     __syncthreads();
     // 2. factor the panel in shared memory
@@ -220,16 +243,11 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
       }
       __syncthreads();
     }
-    // 3. the panel's rows of R back to G
-    for (int e = tid; e < jb * (s - j0); e += nt) {
-      const int t = e % jb, c = j0 + e / jb;
-      G[(j0 + t) + (size_t)s * c] = c >= j0 + t ? P[t * s + c] : zero;
-    }
-    // 4. trailing triangle: G_kl -= sum_t conj(R_tk) R_tl, j0+jb <= k <= l
-    for (int l = j0 + jb + warp; l < s; l += nw) {
+    // 3. trailing triangle, this CTA's columns: G_kl -= sum_t conj(R_tk) R_tl, j0+jb <= k <= l
+    for (int l = own(j0 + jb) + C * warp; l < s; l += C * nw) {
       float4 *col = G + (size_t)s * l;
       for (int k = j0 + jb + lane; k <= l; k += 32) {
-        float4 g = col[k];
+        float4 g = col[k];  // written only by this CTA
         for (int t = 0; t < jb; ++t) {
           const float4 a = P[t * s + k];
           df_cmac_ca(g.x, g.y, g.z, g.w, make_float4(-a.x, -a.y, -a.z, -a.w), P[t * s + l]);
@@ -237,23 +255,27 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
         col[k] = g;
       }
     }
-    __syncthreads();
+    prev = j0;
+    cluster.sync();
   }
-  // Ri = R^-1 (upper), block rows B = [b0, b0+jb) from the bottom:
+  if (rank == 0) write_back(prev, min(PB, s - prev));
+  cluster.sync();
+  // Ri = R^-1 (upper), block rows B = [b0, b0+jb) from the bottom, this CTA's columns:
   //   T(B, c) = sum_{l >= b0+jb} R(B, l) Ri(l, c)      (one pass over the rows done)
   //   Ri(B, c) = R(B, B)^-1 (delta(B, c) - T(B, c))    (triangular solve in the block)
-  for (size_t e = tid; e < (size_t)s * s; e += nt) Ri[e] = zero;
+  for (int c = own(0); c < s; c += C)
+    for (int r = tid; r < s; r += nt) Ri[r + (size_t)s * c] = zero;
   __syncthreads();
   const int nblk = (s + PB - 1) / PB;
   for (int bi = nblk - 1; bi >= 0; --bi) {
     const int b0 = bi * PB, jb = min(PB, s - b0);
     for (int e = tid; e < jb * (s - b0); e += nt) {  // R(B, b0..s-1)
       const int t = e % jb, c = b0 + e / jb;
-      P[t * s + c] = G[(b0 + t) + (size_t)s * c];
+      P[t * s + c] = __ldcg(&G[(b0 + t) + (size_t)s * c]);
     }
     __syncthreads();
     // T into Ri(B, c), one warp per column c, lanes over l
-    for (int c = b0 + jb + warp; c < s; c += nw) {
+    for (int c = own(b0 + jb) + C * warp; c < s; c += C * nw) {
       const float4 *x = Ri + (size_t)s * c;
       for (int t = 0; t < jb; ++t) {
         float rh = 0.f, rl = 0.f, jh = 0.f, jl = 0.f;
@@ -269,7 +291,7 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
     }
     __syncthreads();
     // triangular solve in the block, one thread per column c >= b0
-    for (int c = b0 + tid; c < s; c += nt) {
+    for (int c = own(b0) + C * tid; c < s; c += C * nt) {
       float4 xs[16];
       for (int t = jb - 1; t >= 0; --t) {
         float4 acc = (b0 + t == c) ? make_float4(1.f, 0.f, 0.f, 0.f) : zero;
@@ -292,7 +314,8 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
     __syncthreads();
   }
   double2 *Rd = reinterpret_cast<double2 *>(Ri);
-  for (size_t e = tid; e < (size_t)s * s; e += nt) Rd[e] = dfd(Ri[e]);  // back to FP64, in place
+  for (int c = own(0); c < s; c += C)
+    for (int r = tid; r < s; r += nt) Rd[r + (size_t)s * c] = dfd(Ri[r + (size_t)s * c]);  // back to FP64, in place
 }
 
 // the slot's X (m x r, ld m) = the first m rows of U Sigma (ld m_max); k = r
@@ -568,19 +591,61 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
     return e;
   };
   auto rs_chol = [&](int nbk, char *w, size_t pr, size_t og, size_t ori, int ss, double fl) -> int {
-    const int PB = ss <= 512 ? 16 : 8;
+    int PB = ss <= 512 ? 16 : 8;
+    const TuneParams tp = tune_lookup(h, 2, ss, nact);
+    if (tp.panel > 0) {  // the autotuner's panel height, when its staging fits
+      if ((tp.panel == 4 || tp.panel == 8 || tp.panel == 16) && sizeof(float4) * (size_t)tp.panel * ss <= 200 * 1024)
+        PB = tp.panel;
+      else
+        tune_reject(h);
+    }
     const size_t smem = sizeof(float4) * (size_t)PB * ss;
     int e2 = check_cuda(h, cudaFuncSetAttribute(k_rs_chol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                         "Cholesky shared memory");
     if (e2) return e2;
-    k_rs_chol<<<nbk, 512, smem, st>>>(R->dims_d, w, pr, og, ori, ss, fl, PB);
+    // cluster size: the SMs shared out among the bonds on the route (at most 8),
+    // or the autotuner's size when the launch can co-schedule it
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(512, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    auto fits = [&](int cs) {
+      cfg.gridDim = dim3(cs, nbk, 1);
+      attr[0].val.clusterDim.x = cs;
+      int ncl = 0;
+      const bool ok = cudaOccupancyMaxActiveClusters(&ncl, (const void *)k_rs_chol, &cfg) == cudaSuccess && ncl >= 1;
+      if (!ok) cudaGetLastError();
+      return ok;
+    };
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int CS = std::max(1, std::min(8, sms / std::max(1, nact)));
+    while (CS > 1 && !fits(CS)) --CS;
+    if (tp.chol_cluster > 0) {
+      if (tp.chol_cluster <= 8 && fits(tp.chol_cluster))
+        CS = tp.chol_cluster;
+      else
+        tune_reject(h);
+    }
+    cfg.gridDim = dim3(CS, nbk, 1);
+    attr[0].val.clusterDim.x = CS;
+    e2 = check_cuda(h, cudaLaunchKernelEx(&cfg, k_rs_chol, (const RsDims *)R->dims_d, w, pr, og, ori, ss, fl, PB),
+                    "Cholesky launch");
     TEBD_LAUNCHED(h);
-    return check_cuda(h, cudaPeekAtLastError(), "Cholesky launch");
+    return e2;
   };
   // CholQR of the rows x s block at `buf` (ld rows), through `tmp`: one pass for
   // the range finder's intermediate bases (only their span matters), two (CholQR2,
   // the second with 7 planes) for the final basis P; the result is left in `buf`.
-  // The sketch's width s is at most kCholMaxS (the Cholesky stages one row of R).
+  // The sketch's width s is at most kRsvdMaxSketch (the Cholesky stages panels of
+  // 8 rows of R, 8 x 1536 x 16 B = 192 KB of shared memory at the largest).
   auto cholqr2 = [&](size_t buf, size_t tmp, int rows, bool twice) -> int {
     int e;
     if ((e = prod(buf, rows, 1, nullptr, pstr, buf, rows, nullptr, pstr, s, s, rows, c.g, sk))) return e;

@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <array>
 #include <vector>
 
 #include "tebd_capi.h"
@@ -125,6 +126,14 @@ constexpr int kBidiagMinDim = 64;  // default route switch: min(m, n) of the com
 constexpr int kMlpIn = 67, kMlpHidden = 128, kMlpOut = 8;
 extern const double kMlpRanks[kMlpOut];
 
+// Launch shapes chosen by the autotuner (tune.cu); 0 = the library's default.
+struct TuneParams {
+  int cluster;       // CTAs per cluster of the bidiagonalisation
+  int team;          // lanes per value of the bisection
+  int panel;         // rows of R per panel of the randomized route's Cholesky
+  int chol_cluster;  // CTAs per bond of that Cholesky
+};
+
 }  // namespace tebd
 
 struct tebd_handle {
@@ -198,6 +207,13 @@ struct tebd_handle {
   int tc_ev_used;
   tebd_mlp *rs_model;      // learned model choosing the sketch per batch (mlp.cu), or null
   double rs_target;        // the model's bound on (sigma_{r+p} / sigma_r)^(2q+2)
+  // autotuner trial in progress (tune.cu): the forced shape, the keys met, and
+  // whether a launch could not use the forced shape
+  struct {
+    int active = 0, rejected = 0;
+    tebd::TuneParams force{0, 0, 0, 0};
+    std::vector<std::array<int, 3>> seen;
+  } tune;
 };
 
 namespace tebd {
@@ -229,10 +245,17 @@ struct BidiagBatch {
   int cap;    // 1: vectors only for the first cp->k values of each problem (set between phases)
 };
 int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b);
+// Autotuner table (tune.cu): the shape for route (0 FP64 bidiagonal, 1
+// double-float bidiagonal, 2 randomized-route Cholesky), largest dimension n
+// and bonds nb; zeros where no entry exists.  tune_reject: the launch could not
+// use the shape it was given.
+TuneParams tune_lookup(tebd_handle *h, int route, int n, int nb);
+void tune_reject(tebd_handle *h);
 void bidiag_block_ws(int M, int N, int kk, size_t *aux_elems, size_t *bdws_doubles);
 size_t bidiag_ws_doubles(int n, int chi);
 size_t bidiag_aux_elems(int n);
 constexpr int kBidiagMaxDim = 4096;  // larger compacted Theta take the QR + Jacobi route
+constexpr int kRsvdMaxSketch = 1536;  // widest sketch of the randomized route (chi + oversampling)
 int jacobi_collect(tebd_handle *h);
 int measure_fp64_peak(int device, double *tflops);
 int run_nc_batch(tebd_handle *h, int nb, const int *links_host, double *truncerr_host);

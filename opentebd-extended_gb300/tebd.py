@@ -73,6 +73,7 @@ EXPORTED_SYMBOLS = (
     "tebd_zgemm_tc", "tebd_set_theta_form", "tebd_set_rsvd",
     "tebd_mlp_create", "tebd_mlp_destroy", "tebd_mlp_param_count", "tebd_mlp_last_error", "tebd_mlp_get_params",
     "tebd_mlp_set_params", "tebd_mlp_forward", "tebd_mlp_loss_grad", "tebd_mlp_train", "tebd_set_rsvd_model",
+    "tebd_autotune", "tebd_get_tuning", "tebd_clear_tuning",
 )
 
 
@@ -173,6 +174,9 @@ def load_library(path: str = LIB_PATH):
     L.tebd_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     L.tebd_reset_stats.argtypes = [vp]
     L.tebd_measure_fp64_peak.argtypes = [ctypes.c_int, dp]
+    L.tebd_autotune.argtypes = [vp, ctypes.c_int, ip, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), dp, dp]
+    L.tebd_get_tuning.argtypes = [ctypes.c_int, ip, ctypes.c_int, ip]
+    L.tebd_clear_tuning.argtypes = [ctypes.c_int]
     L.tebd_get_stream.argtypes = [vp]
     L.tebd_get_stream.restype = ctypes.c_void_p
     L.tebd_two_site_op_noalloc.argtypes = [ctypes.c_int] * 4 + [vp, vp, vp, dp, vp]
@@ -403,6 +407,16 @@ class Chain:
         self._check(self._lib.tebd_apply_bonds(self.h, len(gs), _ip(lk), arr, _dp(te)))
         return te
 
+    def autotune(self, links, gates):
+        """Tune the SVD routes' launch shapes on this batch (tebd_autotune); the
+        chain is left as it was.  Returns (default ms, tuned ms) of the batch."""
+        gs = [_as_gate(g, self.d) for g in gates]
+        arr = (ctypes.POINTER(ctypes.c_double) * len(gs))(*[_dp(g) for g in gs])
+        lk = np.ascontiguousarray(links, dtype=np.int32)
+        base, best = np.zeros(1), np.zeros(1)
+        self._check(self._lib.tebd_autotune(self.h, len(gs), _ip(lk), arr, _dp(base), _dp(best)))
+        return float(base[0]), float(best[0])
+
     def trotter_step(self, Udt, order=2):
         """TrotterStep(Udt, ...) with open boundaries; Udt[g-1] is the reference's Udt(g)."""
         gs = [_as_gate(g, self.d) for g in Udt]
@@ -565,6 +579,35 @@ def measure_fp64_peak(device=0):
     if rc != TEBD_OK:
         raise TebdError(rc, "tebd_measure_fp64_peak failed")
     return float(v[0])
+
+
+TUNE_ROUTES = {0: "fp64 bidiagonal", 1: "double-float bidiagonal", 2: "randomized-route Cholesky"}
+
+
+def get_tuning(device=0):
+    """The device's autotuner table as dicts (tebd_get_tuning); 0 = the default shape."""
+    lib = load_library()
+    cnt = np.zeros(1, dtype=np.int32)
+    rc = lib.tebd_get_tuning(device, None, 0, _ip(cnt))
+    if rc != TEBD_OK:
+        raise TebdError(rc, "tebd_get_tuning failed")
+    n = int(cnt[0])
+    buf = np.zeros(8 * max(n, 1), dtype=np.int32)
+    rc = lib.tebd_get_tuning(device, _ip(buf), n, _ip(cnt))
+    if rc != TEBD_OK:
+        raise TebdError(rc, "tebd_get_tuning failed")
+    keys = ("route", "n_bucket", "bonds_bucket", "cluster", "team", "chol_cluster", "panel", "batch_us")
+    rows = [dict(zip(keys, (int(v) for v in buf[8 * i:8 * i + 8]))) for i in range(n)]
+    for r in rows:
+        r["route"] = TUNE_ROUTES.get(r["route"], r["route"])
+    return rows
+
+
+def clear_tuning(device=0):
+    """Empty the device's autotuner table (tebd_clear_tuning)."""
+    rc = load_library().tebd_clear_tuning(device)
+    if rc != TEBD_OK:
+        raise TebdError(rc, "tebd_clear_tuning failed")
 
 
 # -- reference-named entry points ---------------------------------------------
