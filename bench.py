@@ -848,9 +848,11 @@ def run_saturated(args):
 # rank: discarded weight <= 1e-10 per update (tebd_set_rank_bound).  The same
 # steps run in plain FP64 and in the learned-rank form (randomized route sized
 # by the trained model, Theta on the tensor cores, the full SVD as fallback and
-# judge); per-step times and the final observables are compared.  Ranks reach
-# 1024 (3072 x 3072 Thetas) in the second step; a saturated plain-FP64 step takes
-# minutes, so --spin1-steps (default 2) bounds the run.
+# judge); per-step times and the final observables are compared.  Under the
+# 1e-10 bound the first steps keep ~190 values per bond (Thetas up to 576 x 576),
+# so the randomized route, which takes saturated bonds only, waits for the
+# entanglement to grow; --spin1-steps (default 3) bounds the run (a saturated
+# plain-FP64 step of 3072 x 3072 Thetas would take minutes).
 # ---------------------------------------------------------------------------
 S1_L, S1_D, S1_CHI0, S1_CHI, S1_DT, S1_BOUND = 128, 3, 64, 1024, 0.01, 1e-10
 
@@ -1007,7 +1009,7 @@ def main():
                     choices=["headline", "nc", "saturated", "fermi_hubbard", "spin1", "zgemm"])
     ap.add_argument("--zgemm-shape", default="2x2560x640x2560", help="--workload zgemm: NBxMxNxK")
     ap.add_argument("--zgemm-form", type=int, default=107, help="--workload zgemm: 107, 3 or 1")
-    ap.add_argument("--spin1-steps", type=int, default=2, help="--workload spin1: Trotter steps per leg")
+    ap.add_argument("--spin1-steps", type=int, default=3, help="--workload spin1: Trotter steps per leg")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--svd", default="fp64", choices=sorted(SVD_MODES))
     ap.add_argument("--save-obs", default=None, help="write final <n_i>, bond energies, Lambdas (npz)")

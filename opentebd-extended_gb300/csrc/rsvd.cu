@@ -243,16 +243,27 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
       }
       __syncthreads();
     }
-    // 3. trailing triangle, this CTA's columns: G_kl -= sum_t conj(R_tk) R_tl, j0+jb <= k <= l
+    // 3. trailing triangle, this CTA's columns: G_kl -= sum_t conj(R_tk) R_tl, j0+jb <= k <= l;
+    //    four rows per lane in flight (the loads are independent)
     for (int l = own(j0 + jb) + C * warp; l < s; l += C * nw) {
-      float4 *col = G + (size_t)s * l;
-      for (int k = j0 + jb + lane; k <= l; k += 32) {
-        float4 g = col[k];  // written only by this CTA
+      float4 *col = G + (size_t)s * l;  // written only by this CTA
+      for (int k0 = j0 + jb + lane; k0 <= l; k0 += 128) {
+        float4 g[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (k0 + 32 * u <= l) g[u] = col[k0 + 32 * u];
         for (int t = 0; t < jb; ++t) {
-          const float4 a = P[t * s + k];
-          df_cmac_ca(g.x, g.y, g.z, g.w, make_float4(-a.x, -a.y, -a.z, -a.w), P[t * s + l]);
+          const float4 b = P[t * s + l];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (k0 + 32 * u <= l) {
+              const float4 a = P[t * s + k0 + 32 * u];
+              df_cmac_ca(g[u].x, g[u].y, g[u].z, g[u].w, make_float4(-a.x, -a.y, -a.z, -a.w), b);
+            }
         }
-        col[k] = g;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (k0 + 32 * u <= l) col[k0 + 32 * u] = g[u];
       }
     }
     prev = j0;
@@ -274,20 +285,35 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
       P[t * s + c] = __ldcg(&G[(b0 + t) + (size_t)s * c]);
     }
     __syncthreads();
-    // T into Ri(B, c), one warp per column c, lanes over l
+    // T into Ri(B, c), one warp per column c, lanes over l: each Ri(l, c) is
+    // loaded once for all jb rows of the block (two loads in flight per lane)
     for (int c = own(b0 + jb) + C * warp; c < s; c += C * nw) {
       const float4 *x = Ri + (size_t)s * c;
-      for (int t = 0; t < jb; ++t) {
-        float rh = 0.f, rl = 0.f, jh = 0.f, jl = 0.f;
-        for (int l = b0 + jb + lane; l <= c; l += 32) df_cmac(rh, rl, jh, jl, P[t * s + l], x[l]);
-        for (int o = 16; o > 0; o >>= 1) {
-          const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
-          const float c2 = __shfl_xor_sync(0xffffffffu, jh, o), d2 = __shfl_xor_sync(0xffffffffu, jl, o);
-          df_mac(rh, rl, a, b, 1.f, 0.f);
-          df_mac(jh, jl, c2, d2, 1.f, 0.f);
-        }
-        if (lane == 0) Ri[(b0 + t) + (size_t)s * c] = make_float4(rh, rl, jh, jl);
+      float acc[16][4];
+#pragma unroll
+      for (int t = 0; t < 16; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+      for (int l0 = b0 + jb + lane; l0 <= c; l0 += 64) {
+        const bool two = l0 + 32 <= c;
+        const float4 x0 = x[l0], x1 = two ? x[l0 + 32] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < 16; ++t)
+          if (t < jb) {
+            df_cmac(acc[t][0], acc[t][1], acc[t][2], acc[t][3], P[t * s + l0], x0);
+            if (two) df_cmac(acc[t][0], acc[t][1], acc[t][2], acc[t][3], P[t * s + l0 + 32], x1);
+          }
       }
+#pragma unroll
+      for (int t = 0; t < 16; ++t)
+        if (t < jb) {
+          float rh = acc[t][0], rl = acc[t][1], jh = acc[t][2], jl = acc[t][3];
+          for (int o = 16; o > 0; o >>= 1) {
+            const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
+            const float c2 = __shfl_xor_sync(0xffffffffu, jh, o), d2 = __shfl_xor_sync(0xffffffffu, jl, o);
+            df_mac(rh, rl, a, b, 1.f, 0.f);
+            df_mac(jh, jl, c2, d2, 1.f, 0.f);
+          }
+          if (lane == 0) Ri[(b0 + t) + (size_t)s * c] = make_float4(rh, rl, jh, jl);
+        }
     }
     __syncthreads();
     // triangular solve in the block, one thread per column c >= b0

@@ -295,28 +295,56 @@ finish:
 // ---------------------------------------------------------------------------
 // digit extraction
 // ---------------------------------------------------------------------------
+// bf16 bit pattern of an integer |D| <= 128 (exact: at most 8 significant bits)
+__device__ __forceinline__ unsigned short oz_bf16_int(int D) {
+  if (D == 0) return 0;
+  const unsigned a = (unsigned)(D < 0 ? -D : D);
+  const int p = 31 - __clz(a);  // 2^p <= a < 2^(p+1), p <= 7
+  return (unsigned short)((D < 0 ? 0x8000u : 0u) | ((unsigned)(127 + p) << 7) | ((a << (7 - p)) & 0x7fu));
+}
+
+// Digits by integer arithmetic only (the FP64 pipe is the GPU's narrowest; these
+// kernels then run at memory speed).  x = +-m 2^E exactly (m the 53-bit
+// significand), q = rint(m 2^(E + 7S - e)) by a shift with rounding (ties away
+// from zero), |q| < 2^(7S) because |x| < 2^e; then balanced 7-bit digits by
+// integer shifts, rounding to nearest at every step: D_0 in [-128, 128], D_s in
+// [-64, 64] after it, and x - 2^e sum_s D_s 2^(-7(s+1)) = 2^(e - 7S)(x 2^(7S-e) - q),
+// at most 2^(e-7S-1).  Non-finite x and all-zero rows give zero digits.
 __device__ __forceinline__ void oz_digits(double x, int e, int S, unsigned short *d) {
-  if (e <= kExpZero) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (e <= kExpZero || ex == 0x7ff) {
     for (int s = 0; s < S; ++s) d[s] = 0;
     return;
   }
-  // q = rint(x 2^(7S - e)), |q| <= 2^(7S) (|x| < 2^e): one scaling by a power of two
-  // and one conversion; then balanced 7-bit digits by integer shifts, rounding to
-  // nearest at every step: D_0 in [-128, 128], D_s in [-64, 64] after it, and
-  // x - 2^e sum_s D_s 2^(-7(s+1)) = 2^(e - 7S) (x 2^(7S-e) - q), at most 2^(e-7S-1)
-  long long q = __double2ll_rn(ldexp(x, 7 * S - e));
+  long long m = (long long)(b & 0xfffffffffffffULL);
+  int E = -1074;
+  if (ex) {
+    m |= 1LL << 52;
+    E = ex - 1075;
+  }
+  const int sh = E + 7 * S - e;
+  long long q = sh >= 0 ? (m << sh) : (-sh <= 62 ? ((m + (1LL << (-sh - 1))) >> (-sh)) : 0LL);
+  if (b >> 63) q = -q;
   for (int s = 0; s < S; ++s) {
-    const int sh = 7 * (S - 1 - s);
-    const long long D = sh ? ((q + (1LL << (sh - 1))) >> sh) : q;
-    q -= D << sh;
-    d[s] = __bfloat16_as_ushort(__float2bfloat16_rn((float)D));  // |D| <= 128: exact
+    const int t = 7 * (S - 1 - s);
+    const long long D = t ? ((q + (1LL << (t - 1))) >> t) : q;
+    q -= D << t;
+    d[s] = oz_bf16_int((int)D);
   }
 }
 
-__device__ __forceinline__ int oz_exp(double mag) {
-  int e = 0;
-  frexp(mag, &e);  // mag = f 2^e, f in [1/2, 1)
-  return e;
+// |x| as its bit pattern, which orders finite magnitudes; non-finite -> 0
+__device__ __forceinline__ unsigned long long oz_absbits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+  return (b >> 52) == 0x7ff ? 0ULL : b;
+}
+
+// e with mag = f 2^e, f in [1/2, 1), from the bit pattern of a positive finite mag
+__device__ __forceinline__ int oz_exp_bits(unsigned long long b) {
+  const int ex = (int)(b >> 52);
+  if (ex) return ex - 1022;
+  return (64 - __clzll((long long)b)) - 1074;  // subnormal: mag = b 2^-1074
 }
 
 // Load a 32 x 32 complex tile of the source as tile[row r][column c] with the
@@ -373,10 +401,10 @@ __global__ void __launch_bounds__(256) k_oz_pack(const double2 *src, long long p
   if (!digits) {
     for (int yy = ty; yy < 32; yy += 8) {
       const double2 v = tile[yy][tx];
-      double mx = fmax(fabs(v.x), fabs(v.y));
-      for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      unsigned long long mx = max(oz_absbits(v.x), oz_absbits(v.y));
+      for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       const int r = r0 + yy;
-      if (tx == 0 && r < nrow && mx > 0.0) atomicMax(&exps[(size_t)p * nrow + r], oz_exp(mx));
+      if (tx == 0 && r < nrow && mx) atomicMax(&exps[(size_t)p * nrow + r], oz_exp_bits(mx));
     }
     return;
   }
@@ -422,14 +450,14 @@ __global__ void __launch_bounds__(256) k_oz_pack_rows(const double2 *src, long l
   if (r >= nrow) return;
   const bool live = r < r_ext;
   const double2 *row = src + (size_t)p * pstride + (size_t)ld * r;
-  double mx = 0.0;
+  unsigned long long mx = 0;
   if (live)
     for (int k = lane; k < c_ext; k += 32) {
       const double2 v = row[k];
-      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+      mx = max(mx, max(oz_absbits(v.x), oz_absbits(v.y)));
     }
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  const int e = mx > 0.0 ? oz_exp(mx) : (int)0x80808080;
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int e = mx ? oz_exp_bits(mx) : (int)0x80808080;
   if (lane == 0) exps[(size_t)p * nrow + r] = e;
   const size_t plane = (size_t)nprob * rows_pad * k_pad;
   for (int k = lane; 2 * k < k_pad; k += 32) {
