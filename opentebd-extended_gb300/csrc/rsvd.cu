@@ -34,6 +34,7 @@
 #include <stddef.h>
 
 #include <algorithm>
+#include <functional>
 
 #include <cooperative_groups.h>
 
@@ -49,7 +50,7 @@ size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 // per-slot carve of the randomized-SVD workspace (bytes), for n_full x n_full
 // Theta, sketch capacity sc and chi kept triplets at most
 struct RsCarve {
-  size_t xp, a, b, z, c, g, ri, w, rr, aux, tau, taup, bdws, per;
+  size_t xp, a, b, z, c, g, ri, w, rr, aux, tau, taup, bdws, th, per;
 };
 RsCarve rs_carve(int n, int sc, int chi) {
   RsCarve c;
@@ -74,6 +75,7 @@ RsCarve rs_carve(int n, int sc, int chi) {
   c.tau = take(sizeof(double2) * sc);
   c.taup = take(sizeof(double2) * sc);
   c.bdws = take(sizeof(double) * bd_d);
+  c.th = take(sizeof(double));  // the Cholesky's pivot threshold
   c.per = o;
   return c;
 }
@@ -119,19 +121,21 @@ __global__ void k_rs_pad(const Slot *slots, const RsDims *dims, double2 *ws, siz
   }
 }
 
-// CholQR step on a Gram: G (s x s, ld s, Hermitian, both triangles) = R^H R with
-// R upper triangular (right-looking Cholesky in place on the upper triangle),
-// then Ri = R^-1 (upper).  A pivot at or below `floor` times the largest diagonal
-// (the Gram's own rounding level: its products carry 7 S bits) marks a direction
-// the sketch does not span to that accuracy: its row of R and column of R^-1 are
-// zero, so A R^-1 has a zero column there.  One CTA per bond.  The O(s^3) work
-// runs in double-float on the FP32 pipe (pairs of floats, 48-bit significands:
-// the FP64 pipe gives one SM ~7 GFLOP/s, too little for s^3 / 2 complex
-// multiply-adds per call); only the s pivots and their reciprocals are FP64.
-// G and Ri hold float4 (re_hi, re_lo, im_hi, im_lo) while the kernel runs -- the
-// same 16 bytes as a double2 -- and Ri is converted back to FP64 at the end.
-// Row j of R is staged in shared memory at step j; the trailing update runs one
-// warp per column with the lanes down the column (contiguous in memory).
+// CholQR step on a Gram: G (s x s, Hermitian, both triangles) = R^H R with R
+// upper triangular (right-looking Cholesky in place on the upper triangle), then
+// Ri = R^-1 (upper).  A pivot at or below the bond's threshold (k_rs_thresh:
+// `floor` times the largest diagonal entry of the whole Gram, its own rounding
+// level: the products carry 7 S bits) marks a direction the sketch does not span
+// to that accuracy: its row of R and column of R^-1 are zero, so A R^-1 has a zero
+// column there.  The kernel works on one diagonal block (s x s inside a matrix
+// of leading dimension ld, at byte offsets og / ori of the bond's workspace): the
+// whole Gram, or a leaf of the recursive blocking in run_rsvd, whose off-diagonal
+// blocks are digit-plane products on the tensor cores.  The O(s^3) work runs in
+// double-float on the FP32 pipe (pairs of floats, 48-bit significands: the FP64
+// pipe gives one SM ~7 GFLOP/s, too little for s^3 / 2 complex multiply-adds per
+// call); only the s pivots and their reciprocals are FP64.  G and Ri hold float4
+// (re_hi, re_lo, im_hi, im_lo) while the kernel runs -- the same 16 bytes as a
+// double2 -- and Ri is converted back to FP64 at the end (R stays double-float).
 
 __device__ __forceinline__ float4 df_scale(float4 v, float sh, float sl) {  // v * (sh + sl)
   float4 r;
@@ -154,6 +158,24 @@ __device__ __forceinline__ void df_split(double x, float &h, float &l) {
   l = (float)(x - (double)h);
 }
 
+// per bond: the Cholesky's pivot threshold, floor x the largest diagonal entry of
+// the Gram (s x s, ld s, FP64) at byte offset og, to byte offset oth
+__global__ void k_rs_thresh(const RsDims *dims, char *ws, size_t per, size_t og, int s, double floor, size_t oth) {
+  const int p = blockIdx.x;
+  if (dims[p].s == 0) return;
+  const double2 *G = reinterpret_cast<const double2 *>(ws + p * per + og);
+  __shared__ double red[256];
+  double mx = 0.0;
+  for (int j = threadIdx.x; j < s; j += blockDim.x) mx = fmax(mx, G[j + (size_t)s * j].x);
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *reinterpret_cast<double *>(ws + p * per + oth) = red[0] * floor;
+}
+
 // Blocked form (panels of PB rows of R, PB = 16 up to s = 512, else 8): the panel
 // rows are factored in shared memory and the trailing triangle takes one rank-PB
 // update per panel; the inverse runs block rows from the bottom, each a product
@@ -168,7 +190,7 @@ __device__ __forceinline__ void df_split(double x, float &h, float &l) {
 // The inverse's columns are independent: each CTA solves its own, c = rank
 // (mod C).  Reads of G that another CTA may have written go to L2 (ld.global.cg).
 __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, size_t per, size_t og, size_t ori,
-                                                 int s, double floor, int PB) {
+                                                 int s, int ld, size_t oth, int PB) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks(), rank = (int)cluster.block_rank();
@@ -181,28 +203,16 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
   const int tid = threadIdx.x, nt = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   auto own = [&](int x) { return x + ((rank - x) % C + C) % C; };  // first column >= x of this CTA
-  __shared__ double gmax;
   __shared__ float ph[16], pl[16];  // reciprocal pivots of the panel, double-float
-  __shared__ double red[512];
-  double mx = 0.0;
-  for (int j = tid; j < s; j += nt) mx = fmax(mx, __ldcg(&Gd[j + (size_t)s * j]).x);
-  red[tid] = mx;
-  __syncthreads();
-  for (int w = nt / 2; w > 0; w >>= 1) {
-    if (tid < w) red[tid] = fmax(red[tid], red[tid + w]);
-    __syncthreads();
-  }
-  if (tid == 0) gmax = red[0];
-  cluster.sync();  // every CTA has read the FP64 diagonal before it is converted
+  const double thresh = *reinterpret_cast<const double *>(ws + p * per + oth);
   for (int c = own(0); c < s; c += C)
-    for (int r = tid; r < s; r += nt) G[r + (size_t)s * c] = dfs(__ldcg(&Gd[r + (size_t)s * c]));  // in place
+    for (int r = tid; r < s; r += nt) G[r + (size_t)ld * c] = dfs(__ldcg(&Gd[r + (size_t)ld * c]));  // in place
   cluster.sync();
-  const double thresh = gmax * floor;
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
   auto write_back = [&](int j0, int jb) {  // rank 0: the factored rows j0.. of the panel in P
     for (int e = tid; e < jb * (s - j0); e += nt) {
       const int t = e % jb, c = j0 + e / jb;
-      G[(j0 + t) + (size_t)s * c] = c >= j0 + t ? P[t * s + c] : zero;
+      G[(j0 + t) + (size_t)ld * c] = c >= j0 + t ? P[t * s + c] : zero;
     }
   };
   int prev = -1;
@@ -213,7 +223,7 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
     // 1. panel rows j0..j0+jb-1, columns j0..s-1
     for (int e = tid; e < jb * (s - j0); e += nt) {
       const int t = e % jb, c = j0 + e / jb;
-      P[t * s + c] = __ldcg(&G[(j0 + t) + (size_t)s * c]);
+      P[t * s + c] = __ldcg(&G[(j0 + t) + (size_t)ld * c]);
     }
     __syncthreads();
     // 2. factor the panel in shared memory
@@ -246,7 +256,7 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
     // 3. trailing triangle, this CTA's columns: G_kl -= sum_t conj(R_tk) R_tl, j0+jb <= k <= l;
     //    four rows per lane in flight (the loads are independent)
     for (int l = own(j0 + jb) + C * warp; l < s; l += C * nw) {
-      float4 *col = G + (size_t)s * l;  // written only by this CTA
+      float4 *col = G + (size_t)ld * l;  // written only by this CTA
       for (int k0 = j0 + jb + lane; k0 <= l; k0 += 128) {
         float4 g[4];
 #pragma unroll
@@ -275,20 +285,20 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
   //   T(B, c) = sum_{l >= b0+jb} R(B, l) Ri(l, c)      (one pass over the rows done)
   //   Ri(B, c) = R(B, B)^-1 (delta(B, c) - T(B, c))    (triangular solve in the block)
   for (int c = own(0); c < s; c += C)
-    for (int r = tid; r < s; r += nt) Ri[r + (size_t)s * c] = zero;
+    for (int r = tid; r < s; r += nt) Ri[r + (size_t)ld * c] = zero;
   __syncthreads();
   const int nblk = (s + PB - 1) / PB;
   for (int bi = nblk - 1; bi >= 0; --bi) {
     const int b0 = bi * PB, jb = min(PB, s - b0);
     for (int e = tid; e < jb * (s - b0); e += nt) {  // R(B, b0..s-1)
       const int t = e % jb, c = b0 + e / jb;
-      P[t * s + c] = __ldcg(&G[(b0 + t) + (size_t)s * c]);
+      P[t * s + c] = __ldcg(&G[(b0 + t) + (size_t)ld * c]);
     }
     __syncthreads();
     // T into Ri(B, c), one warp per column c, lanes over l: each Ri(l, c) is
     // loaded once for all jb rows of the block (two loads in flight per lane)
     for (int c = own(b0 + jb) + C * warp; c < s; c += C * nw) {
-      const float4 *x = Ri + (size_t)s * c;
+      const float4 *x = Ri + (size_t)ld * c;
       float acc[16][4];
 #pragma unroll
       for (int t = 0; t < 16; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
@@ -312,7 +322,7 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
             df_mac(rh, rl, a, b, 1.f, 0.f);
             df_mac(jh, jl, c2, d2, 1.f, 0.f);
           }
-          if (lane == 0) Ri[(b0 + t) + (size_t)s * c] = make_float4(rh, rl, jh, jl);
+          if (lane == 0) Ri[(b0 + t) + (size_t)ld * c] = make_float4(rh, rl, jh, jl);
         }
     }
     __syncthreads();
@@ -322,7 +332,7 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
       for (int t = jb - 1; t >= 0; --t) {
         float4 acc = (b0 + t == c) ? make_float4(1.f, 0.f, 0.f, 0.f) : zero;
         if (c >= b0 + jb) {
-          const float4 q = Ri[(b0 + t) + (size_t)s * c];
+          const float4 q = Ri[(b0 + t) + (size_t)ld * c];
           acc = make_float4(-q.x, -q.y, -q.z, -q.w);
         }
         for (int u = t + 1; u < jb; ++u) {
@@ -335,13 +345,13 @@ __global__ void __launch_bounds__(512) k_rs_chol(const RsDims *dims, char *ws, s
         df_split(d > 0.0 ? 1.0 / d : 0.0, h, l);
         xs[t] = (b0 + t <= c) ? df_scale(acc, h, l) : zero;
       }
-      for (int t = 0; t < jb; ++t) Ri[(b0 + t) + (size_t)s * c] = xs[t];
+      for (int t = 0; t < jb; ++t) Ri[(b0 + t) + (size_t)ld * c] = xs[t];
     }
     __syncthreads();
   }
   double2 *Rd = reinterpret_cast<double2 *>(Ri);
   for (int c = own(0); c < s; c += C)
-    for (int r = tid; r < s; r += nt) Rd[r + (size_t)s * c] = dfd(Ri[r + (size_t)s * c]);  // back to FP64, in place
+    for (int r = tid; r < s; r += nt) Rd[r + (size_t)ld * c] = dfd(Ri[r + (size_t)ld * c]);  // back to FP64, in place
 }
 
 // the slot's X (m x r, ld m) = the first m rows of U Sigma (ld m_max); k = r
@@ -616,7 +626,10 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
     h->stats.rsvd_flops += 8.0 * rows * (double)cols * k * nact;
     return e;
   };
-  auto rs_chol = [&](int nbk, char *w, size_t pr, size_t og, size_t ori, int ss, double fl) -> int {
+  // one diagonal block of n x n (leading dimension ld) of every bond's Gram at
+  // byte offset og, its inverse factor to ori: k_rs_chol on a cluster per bond
+  auto leaf = [&](size_t og, size_t ori, int ss, int ld) -> int {
+    const int nbk = nb;
     int PB = ss <= 512 ? 16 : 8;
     const TuneParams tp = tune_lookup(h, 2, ss, nact);
     if (tp.panel > 0) {  // the autotuner's panel height, when its staging fits
@@ -662,10 +675,74 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
     }
     cfg.gridDim = dim3(CS, nbk, 1);
     attr[0].val.clusterDim.x = CS;
-    e2 = check_cuda(h, cudaLaunchKernelEx(&cfg, k_rs_chol, (const RsDims *)R->dims_d, w, pr, og, ori, ss, fl, PB),
+    e2 = check_cuda(h, cudaLaunchKernelEx(&cfg, k_rs_chol, (const RsDims *)R->dims_d, ws, per, og, ori, ss, ld,
+                                          c.th, PB),
                     "Cholesky launch");
     TEBD_LAUNCHED(h);
     return e2;
+  };
+  // a product on blocks of the workspace: out (rows x cols, leading dimension
+  // ldo, byte offset oo) = alpha op(A) B (+ out when acc), op(A) = A or A^H
+  auto bprod = [&](size_t ao, int lda, int at, size_t bo, int ldb, int rows, int cols, int k, size_t oo, int ldo,
+                   double alpha, int acc, int slices) -> int {
+    ZProd z = {};
+    z.a = reinterpret_cast<const double2 *>(ws + ao);
+    z.a_stride = pstr;
+    z.lda = lda;
+    z.a_trans = at;
+    z.a_conj = at;
+    z.b = reinterpret_cast<const double2 *>(ws + bo);
+    z.b_stride = pstr;
+    z.ldb = ldb;
+    z.nprob = nb;
+    z.m = rows;
+    z.n = cols;
+    z.k = k;
+    z.form = 100 + slices;
+    z.out = reinterpret_cast<double2 *>(ws + oo);
+    z.out_stride = pstr;
+    z.rs = 1;
+    z.cs = ldo;
+    z.n_d = &R->dims_d[0].s;  // 0 off the route: those tiles exit at once
+    z.dim_stride = dstride;
+    z.alpha = alpha;
+    z.accumulate = acc;
+    int e = tc_reserve(h, zprod_ws_bytes(z));
+    if (e) return e;
+    tc_events(h, zprod_mma_flops(z, nact), &z.ev0, &z.ev1);
+    e = check_cuda(h, zprod_run(z, h->tc_ws, h->tc_err, st), "Cholesky block product");
+    h->launches += 5;
+    h->stats.rsvd_flops += 8.0 * rows * (double)cols * k * nact;
+    return e;
+  };
+  // Cholesky + inverse of the s x s Gram at c.g into c.ri, recursively by halves
+  // above kCholLeaf: with G = [G11 G12; G12^H G22] (n1 + n2),
+  //   R11 = chol(G11), R12 = R11^-H G12 (in place of G12), G22 -= R12^H R12,
+  //   R22 = chol(G22), Ri12 = -Ri11 (R12 Ri22) (R12 Ri22 through c.w),
+  // the off-diagonal work as digit-plane products on the tensor cores, the
+  // diagonal leaves in k_rs_chol.  Every pivot is judged against the whole
+  // Gram's threshold.
+  constexpr int kCholLeaf = 384;
+  std::function<int(size_t, size_t, int, int)> crec = [&](size_t gb, size_t rb, int n, int sl) -> int {
+    if (n <= kCholLeaf) return leaf(gb, rb, n, s);
+    const int n1 = (n / 2 + 31) / 32 * 32, n2 = n - n1;
+    const size_t col = sizeof(double2) * (size_t)s;  // bytes per column (ld s)
+    const size_t g12 = gb + col * n1, g22 = gb + col * n1 + sizeof(double2) * n1;
+    const size_t r12 = rb + col * n1, r22 = rb + col * n1 + sizeof(double2) * n1;
+    int e;
+    if ((e = crec(gb, rb, n1, sl)) || (e = bprod(rb, s, 1, g12, s, n1, n2, n1, g12, s, 1.0, 0, sl)) ||
+        (e = bprod(g12, s, 1, g12, s, n2, n2, n1, g22, s, -1.0, 1, sl)) || (e = crec(g22, r22, n2, sl)) ||
+        (e = bprod(g12, s, 0, r22, s, n1, n2, n2, c.w, n1, 1.0, 0, sl)) ||
+        (e = bprod(rb, s, 0, c.w, n1, n1, n2, n1, r12, s, -1.0, 0, sl)))
+      return e;
+    return TEBD_OK;
+  };
+  auto rs_chol = [&](int ss, double fl, int sl) -> int {
+    k_rs_thresh<<<nb, 256, 0, st>>>(R->dims_d, ws, per, c.g, ss, fl, c.th);
+    TEBD_LAUNCHED(h);
+    int e = check_cuda(h, cudaMemset2DAsync(ws + c.ri, per, 0, sizeof(double2) * (size_t)ss * ss, nb, st),
+                       "Cholesky inverse reset");
+    return e ? e : crec(c.g, c.ri, ss, sl);
   };
   // CholQR of the rows x s block at `buf` (ld rows), through `tmp`: one pass for
   // the range finder's intermediate bases (only their span matters), two (CholQR2,
@@ -675,14 +752,14 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
   auto cholqr2 = [&](size_t buf, size_t tmp, int rows, bool twice) -> int {
     int e;
     if ((e = prod(buf, rows, 1, nullptr, pstr, buf, rows, nullptr, pstr, s, s, rows, c.g, sk))) return e;
-    if ((e = rs_chol(nb, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * sk + 9)))) return e;
+    if ((e = rs_chol(s, ldexp(1.0, -7 * sk + 9), sk))) return e;
     if ((e = prod(buf, rows, 0, nullptr, pstr, c.ri, s, nullptr, pstr, rows, s, s, tmp, sk))) return e;
     if (!twice)  // one pass: back into buf
       return check_cuda(h, cudaMemcpy2DAsync(ws + buf, per, ws + tmp, per, sizeof(double2) * (size_t)rows * s, nb,
                                              cudaMemcpyDeviceToDevice, st),
                         "CholQR copy");
     if ((e = prod(tmp, rows, 1, nullptr, pstr, tmp, rows, nullptr, pstr, s, s, rows, c.g, fin))) return e;
-    if ((e = rs_chol(nb, ws, per, c.g, c.ri, s, ldexp(1.0, -7 * fin + 9)))) return e;
+    if ((e = rs_chol(s, ldexp(1.0, -7 * fin + 9), fin))) return e;
     return prod(tmp, rows, 0, nullptr, pstr, c.ri, s, nullptr, pstr, rows, s, s, buf, fin);
   };
   // 1. padded copy

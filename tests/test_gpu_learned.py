@@ -138,3 +138,64 @@ def test_learned_model_gains_over_fixed_sketch(pkg):
     assert model["rsvd_flops"] < cons["rsvd_flops"], (model["rsvd_flops"], cons["rsvd_flops"])
     assert model["rsvd_fallbacks"] <= cheap["rsvd_fallbacks"], (model, cheap)
     m.close()
+
+
+def test_spin1_learned_form_matches_fp64(pkg):
+    """The learned-rank configuration's shape at reduced size: spin-1 chain with
+    random single-ion anisotropy (d = 3), a random MPS at chi = 8 growing to
+    chi = 24 (saturated from the second sweep, so that the randomized route is
+    taken), discarded weight <= 1e-10 per update; the learned form (randomized
+    route sized by the committed model, Theta on the tensor cores) and the same
+    route with a fixed sketch against plain FP64 with the same kept-rank rule:
+    local observables within 1e-8."""
+    import os
+
+    H = pkg.hamiltonians
+    L, d, chi0, chi = 16, 3, 8, 24
+    rng = np.random.default_rng(4)
+    g = [np.asfortranarray(rng.standard_normal((chi0, d, chi0)) + 1j * rng.standard_normal((chi0, d, chi0)))
+         for _ in range(L)]
+    lm = [np.full(chi0, 1.0 / np.sqrt(chi0)) for _ in range(L + 1)]
+    lm[0] = np.eye(chi0)[0]
+    lm[L] = np.eye(chi0)[0]
+    with pkg.Chain(L, d, chi0) as c:
+        c.set_state(g, lm)
+        c.canonical_form_all()
+        g, lm = c.get_state()
+    gam = []
+    for x in g:
+        y = np.zeros((chi, d, chi), complex, order="F")
+        y[:chi0, :, :chi0] = x
+        gam.append(y)
+    lam = []
+    for x in lm:
+        y = np.zeros(chi)
+        y[:chi0] = x
+        lam.append(y)
+    Di = np.random.default_rng(4).uniform(-0.5, 0.5, L)
+    Hb = H.spin1_xxz_anisotropy(L, 1.0, 1.0, Di)
+    U = H.construct_propagators(Hb, 0.01, 2)
+    sz = H.spin_ops(1.0)[2]
+    params = np.load(os.path.join(os.path.dirname(pkg.__file__), "data", "rsvd_model.npz"))["params"]
+    m = pkg.Mlp(seed=0)
+    m.set_params(params)
+    res = {}
+    for name in ("fp64", "fixed", "learned"):
+        with pkg.Chain(L, d, chi, svd_mode=pkg.SVD_FP64 if name == "fp64" else pkg.SVD_RSVD) as c:
+            c.set_rank_bound(1e-10)
+            if name != "fp64":
+                c.set_theta_form(107)
+            if name == "fixed":
+                c.set_rsvd(oversample=24, power_iters=2)
+            if name == "learned":
+                c.set_rsvd_model(m, 1e-8)
+            c.set_state(gam, lam)
+            for _ in range(6):
+                c.trotter_step(U, 2)
+            res[name] = (c.one_site_expval(sz), c.local_energy(Hb), c.chain_entropy(), c.stats())
+    m.close()
+    f = res["fp64"]
+    assert res["fixed"][3]["rsvd_updates"] > 0  # the route is taken on this chain
+    for name in ("fixed", "learned"):
+        for a, b in zip(f[:3], res[name][:3]):
+            assert np.max(np.abs(a - b)) < 1e-8, name
