@@ -989,7 +989,7 @@ def run_zgemm(args):
     ref = torch.einsum("bkm,bnk->bnm", A, B)
     err = ((C - ref).abs().max() / ref.abs().max()).item()
     f = args.zgemm_form
-    mp, np_ = -(-m // 128) * 128, -(-2 * n // (64 if f > 100 else 128)) * (64 if f > 100 else 128)
+    mp, np_ = -(-m // 128) * 128, -(-2 * n // 128) * 128
     kp = -(-2 * k // 32) * 32
     pairs = (f - 100) * (f - 99) // 2 if f > 100 else 3 if f == 3 else 1
     mma = pairs * 2.0 * mp * np_ * kp * nb

@@ -51,6 +51,10 @@ static size_t pin_links_off(const tebd_handle *h) {
 using namespace tebd;
 
 static thread_local std::string g_noh_err;
+namespace tebd {
+// the message tebd_last_error(NULL) returns (calls that take no handle)
+void set_noh_error(const std::string &msg) { g_noh_err = msg; }
+}  // namespace tebd
 
 #define CK(expr, what)                                   \
   do {                                                   \

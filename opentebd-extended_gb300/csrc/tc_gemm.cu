@@ -22,6 +22,8 @@
 
 #include <mutex>
 
+#include <string>
+
 #include "tc_gemm.cuh"
 #include "tc_ptx.cuh"
 
@@ -504,12 +506,17 @@ extern "C" int tebd_zgemm_tc(int nprob, int m, int n, int k, const double *A, lo
   void *ws = nullptr;
   int *err = nullptr;
   int rc = TEBD_OK, herr = 0;
-  if (cudaMalloc(&ws, zprod_ws_bytes(z)) != cudaSuccess || cudaMalloc(&err, sizeof(int)) != cudaSuccess)
+  cudaError_t e = cudaSuccess;
+  if (cudaMalloc(&ws, zprod_ws_bytes(z)) != cudaSuccess || cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
     rc = TEBD_ERR_OOM;
-  else if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess || zprod_run(z, ws, err, st) != cudaSuccess ||
-           cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-           cudaStreamSynchronize(st) != cudaSuccess || herr)
+    set_noh_error("tebd_zgemm_tc: out of device memory");
+  } else if ((e = cudaMemsetAsync(err, 0, sizeof(int), st)) != cudaSuccess || (e = zprod_run(z, ws, err, st)) != cudaSuccess ||
+             (e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+             (e = cudaStreamSynchronize(st)) != cudaSuccess || herr) {
     rc = TEBD_ERR_CUDA;
+    set_noh_error(e != cudaSuccess ? std::string("tebd_zgemm_tc: ") + cudaGetErrorString(e)
+                                   : std::string("tebd_zgemm_tc: a pipeline wait of the product kernel expired"));
+  }
   (void)cudaGetLastError();
   cudaFree(ws);
   cudaFree(err);

@@ -88,7 +88,7 @@ inline int tc_planes(int form) { return form == kTc3xTF32 ? 2 : 1; }
 // combined in FP64.  Accuracy: about 2^(-7S) relative to (row max x column max)
 // per term -- S = 7 is FP64 class (~1e-15), S = 5 ~ 1e-11.
 // ---------------------------------------------------------------------------
-constexpr int kOzBN = 64;      // real output columns per CTA
+constexpr int kOzBN = 128;     // real output columns per CTA
 constexpr int kOzBK = 32;      // bf16 per 64-byte row (K block)
 constexpr int kOzMaxS = 7;
 

@@ -2,27 +2,31 @@
 // error-free splitting into bf16 integer digits (scheme and accuracy in
 // tc_gemm.cuh).
 //
-// One CTA of 6 warps computes a 128 x 64 tile of the real product of one
-// problem:
-//   warp 4, lane 0   TMA producer: per 32-wide K block the S digit tiles of A
-//                    (128 rows x 64 B) and of B (64 rows x 64 B), 64-byte
-//                    swizzle, into one of `stages` shared-memory stages;
-//   warp 5, lane 0   MMA issuer: per K block two K-steps of 16, and per step
-//                    one tcgen05.mma (M 128, N 64, K 16, kind::f16, bf16 in,
-//                    FP32 accumulation) for every digit pair (s, t) with
-//                    s + t < S, into the TMEM accumulator of group g = s + t
-//                    (columns 64 g .. 64 g + 63);
-//   warps 0-3        epilogue (warp w reads TMEM lanes 32w..32w+31): after every chunk of 16 K blocks (512 real
-//                    terms: the group sums are exact integers below 2^24) they
-//                    read the S accumulators of their 32 rows, add
-//                    2^(-7(g+2)) x group into 64 FP64 registers, and release
-//                    TMEM to the issuer; after the last chunk the row and
-//                    column exponents are applied and the complex FP64 result
-//                    is written.
-// The issuer waits for the epilogue between chunks, so the two roles live in
-// different warps (a warp's lanes reconverge before tcgen05.ld).
-// Every wait is bounded as in tc_gemm.cu; on expiry *err is set and nothing is
-// written.
+// One CTA of 10 warps computes a 128 x 128 tile of the real product of one
+// problem.  The S digit groups g = s + t do not fit the 512 TMEM columns at
+// once for N = 128 (7 x 128), so K is streamed in passes: pass q accumulates the
+// groups 4q .. 4q + 3 (four accumulators of 128 columns), reading the digit
+// slices 0 .. min(S, 4q + 4) - 1 of A and B:
+//   warp 8, lane 0   TMA producer: per 32-wide K block and pass the pass's digit
+//                    tiles of A and of B (128 rows x 64 B each, 64-byte
+//                    swizzle) into one of `stages` shared-memory stages;
+//   warp 9, lane 0   MMA issuer: per K block two K-steps of 16, and per step
+//                    one tcgen05.mma (M 128, N 128, K 16, kind::f16, bf16 in,
+//                    FP32 accumulation) for every digit pair (s, t) of the
+//                    pass's groups, into the TMEM accumulator of its group;
+//   warps 0-7        epilogue (warp w reads TMEM lanes 32 (w mod 4) .. + 31,
+//                    columns 64 (w div 4) .. + 63 of each group): after every
+//                    chunk of 16 K blocks (512 real terms: the group sums are
+//                    exact integers below 2^24) they read the pass's group
+//                    accumulators and add them, exactly, into 64 int64
+//                    registers, then release TMEM to the issuer; after the last
+//                    chunk of the last pass the row and column exponents are
+//                    applied and the complex FP64 result is written.
+// N = 128 keeps the tensor pipe at its full op rate (an N = 64 MMA runs it at
+// half) and halves the operand reads per multiply-add.  The issuer waits for
+// the epilogue between chunks, so the two roles live in different warps (a
+// warp's lanes reconverge before tcgen05.ld).  Every wait is bounded as in
+// tc_gemm.cu; on expiry *err is set and nothing is written.
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 #include <stdint.h>
@@ -36,12 +40,15 @@ namespace tebd {
 namespace {
 using namespace tcx;
 
-constexpr int kOzThreads = 192;
+constexpr int kOzEpiWarps = 8;
+constexpr int kOzThreads = 32 * (kOzEpiWarps + 2);
 constexpr int kOzMaxStages = 4;
-constexpr int kOzChunk = 16;  // K blocks per exact chunk (512 real terms)
+constexpr int kOzChunk = 16;   // K blocks per exact chunk (512 real terms)
+constexpr int kOzGroups = 4;   // digit groups per pass (4 x 128 TMEM columns)
 constexpr uint32_t kOzTileA = kTcBM * kOzBK * 2;  // 8 KB per digit tile of A
-constexpr uint32_t kOzTileB = kOzBN * kOzBK * 2;  // 4 KB per digit tile of B
+constexpr uint32_t kOzTileB = kOzBN * kOzBK * 2;  // 8 KB per digit tile of B
 constexpr uint32_t kOzTmemCols = 512;
+constexpr int kOzSmemMax = 232448;  // opt-in shared memory per block
 
 // Instruction descriptor of kind::f16: D F32 (bits 4-5 = 1), A and B BF16
 // (bits 7-9, 10-12 = 1), K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
@@ -49,12 +56,18 @@ constexpr uint32_t kIdescBF16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)
                                 ((uint32_t)(kTcBM >> 4) << 24);
 constexpr int kExpZero = -2000;  // exponents below this mark an all-zero row
 
-__host__ __device__ constexpr int oz_stages(int S) {
-  return (220 * 1024) / (S * (int)(kOzTileA + kOzTileB)) > kOzMaxStages
-             ? kOzMaxStages
-             : (220 * 1024) / (S * (int)(kOzTileA + kOzTileB));
+__host__ __device__ constexpr int oz_passes(int S) { return (S + kOzGroups - 1) / kOzGroups; }
+// digit slices pass q reads: 0 .. oz_pass_slices - 1
+__host__ __device__ constexpr int oz_pass_slices(int S, int q) {
+  return S < kOzGroups * (q + 1) ? S : kOzGroups * (q + 1);
 }
-size_t oz_smem(int S) { return 1024 + (size_t)oz_stages(S) * S * (kOzTileA + kOzTileB) + 512; }
+__host__ __device__ constexpr int oz_stage_slices(int S) { return oz_pass_slices(S, oz_passes(S) - 1); }
+__host__ __device__ constexpr int oz_stages(int S) {
+  return (kOzSmemMax - 2048) / (oz_stage_slices(S) * (int)(kOzTileA + kOzTileB)) > kOzMaxStages
+             ? kOzMaxStages
+             : (kOzSmemMax - 2048) / (oz_stage_slices(S) * (int)(kOzTileA + kOzTileB));
+}
+size_t oz_smem(int S) { return 1024 + (size_t)oz_stages(S) * oz_stage_slices(S) * (kOzTileA + kOzTileB) + 512; }
 
 __device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
@@ -87,37 +100,39 @@ __device__ __forceinline__ void tmem_wait(uint32_t (&r)[N]) {
   for (int i = 0; i < N; ++i) asm volatile("" : "+r"(r[i]));
 }
 
-// All MMAs of one K block (two K-steps of 16) for every digit pair of a stage:
-// da, db are the descriptors of slice 0 of A and B in the stage; slice q starts
-// q tiles further, a K-step 32 bytes further (descriptor units of 16 bytes).
-// The first MMA into a group in a chunk (K-step 0 of its first K block, pair
-// (0, g)) overwrites the accumulator.
-template <int S>
+// All MMAs of one K block (two K-steps of 16) for the digit pairs (sa, sb) of the
+// groups GLO <= sa + sb < min(GHI, S): da, db are the descriptors of slice 0 of
+// A and B in the stage; slice q starts q tiles further, a K-step 32 bytes further
+// (descriptor units of 16 bytes); group g accumulates at TMEM column
+// (g - GLO) x 128.  The first MMA into a group in a chunk (K-step 0 of its first
+// K block, pair (0, g)) overwrites the accumulator.
+template <int S, int GLO, int GHI>
 __device__ __forceinline__ void oz_issue(uint32_t tmem, uint64_t da, uint64_t db, bool first) {
 #pragma unroll
   for (int kk = 0; kk < kOzBK / 16; ++kk)
 #pragma unroll
     for (int sa = 0; sa < S; ++sa)
 #pragma unroll
-      for (int sb = 0; sa + sb < S; ++sb)
-        mma_bf16(tmem + (uint32_t)((sa + sb) * kOzBN), da + (uint64_t)((sa * kOzTileA + kk * 32) >> 4),
-                 db + (uint64_t)((sb * kOzTileB + kk * 32) >> 4), (first && kk == 0 && sa == 0) ? 0u : 1u);
+      for (int sb = 0; sb < S; ++sb)
+        if (sa + sb >= GLO && sa + sb < GHI && sa + sb < S)
+          mma_bf16(tmem + (uint32_t)((sa + sb - GLO) * kOzBN), da + (uint64_t)((sa * kOzTileA + kk * 32) >> 4),
+                   db + (uint64_t)((sb * kOzTileB + kk * 32) >> 4), (first && kk == 0 && sa == 0) ? 0u : 1u);
 }
 
 template <int S>
 __global__ void __launch_bounds__(kOzThreads, 1)
     k_tc_oz(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzBatch b,
             int *err) {
-  constexpr int stages = oz_stages(S);
+  constexpr int stages = oz_stages(S), NSL = oz_stage_slices(S), NP = oz_passes(S);
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem =
       reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  unsigned char *sA = smem;                                  // [stage][slice] kOzTileA
-  unsigned char *sB = sA + (size_t)stages * S * kOzTileA;    // [stage][slice] kOzTileB
-  uint64_t *full = reinterpret_cast<uint64_t *>(sB + (size_t)stages * S * kOzTileB);
+  unsigned char *sA = smem;                                    // [stage][slice] kOzTileA
+  unsigned char *sB = sA + (size_t)stages * NSL * kOzTileA;    // [stage][slice] kOzTileB
+  uint64_t *full = reinterpret_cast<uint64_t *>(sB + (size_t)stages * NSL * kOzTileB);
   uint64_t *empty = full + kOzMaxStages;
   uint64_t *cfull = empty + kOzMaxStages;  // a chunk's MMAs are complete
-  uint64_t *tfree = cfull + 1;             // the epilogue has read the chunk (4 arrivals)
+  uint64_t *tfree = cfull + 1;             // the epilogue has read the chunk (8 arrivals)
   uint64_t *done = tfree + 1;              // every MMA issued has completed
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
   volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
@@ -131,6 +146,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   if (m0 >= mp || n0 >= 2 * np) return;  // tile outside this problem: uniform over the CTA
   const int nk = b.k_pad / kOzBK;
   const int nchunks = (nk + kOzChunk - 1) / kOzChunk;
+  const int total = NP * nk;  // K blocks over all passes
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < stages; ++s) {
@@ -138,7 +154,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(cfull, 1);
-    mbar_init(tfree, 4);
+    mbar_init(tfree, kOzEpiWarps);
     mbar_init(done, 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -154,52 +170,53 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   tc_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 4) {
+  if (warp == kOzEpiWarps) {
     // ---- TMA producer ----
     if (lane != 0) goto finish;
-    const uint32_t bytes = S * (kOzTileA + kOzTileB);
     int issued = 0;
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % stages;
-      if (kb >= stages && !mbar_wait(&empty[s], ((kb / stages) & 1) ^ 1, abort)) {
+    for (int it = 0; it < total; ++it) {
+      const int s = it % stages, q = it / nk, kb = it % nk;
+      if (it >= stages && !mbar_wait(&empty[s], ((it / stages) & 1) ^ 1, abort)) {
         *abort = 1;
         atomicExch(err, 1);
         break;
       }
-      mbar_expect_tx(&full[s], bytes);
-#pragma unroll
-      for (int q = 0; q < S; ++q)
-        tma_load_3d(sA + (size_t)(s * S + q) * kOzTileA, &tmA, &full[s], kb * kOzBK, m0, q * b.nprob + p);
-#pragma unroll
-      for (int q = 0; q < S; ++q)
-        tma_load_3d(sB + (size_t)(s * S + q) * kOzTileB, &tmB, &full[s], kb * kOzBK, n0, q * b.nprob + p);
-      issued = kb + 1;
+      const int nsl = oz_pass_slices(S, q);
+      mbar_expect_tx(&full[s], (uint32_t)nsl * (kOzTileA + kOzTileB));
+      for (int sl = 0; sl < nsl; ++sl)
+        tma_load_3d(sA + (size_t)(s * NSL + sl) * kOzTileA, &tmA, &full[s], kb * kOzBK, m0, sl * b.nprob + p);
+      for (int sl = 0; sl < nsl; ++sl)
+        tma_load_3d(sB + (size_t)(s * NSL + sl) * kOzTileB, &tmB, &full[s], kb * kOzBK, n0, sl * b.nprob + p);
+      issued = it + 1;
     }
     if (*abort)
-      for (int kb = issued - stages < 0 ? 0 : issued - stages; kb < issued; ++kb)
-        mbar_wait(&full[kb % stages], (kb / stages) & 1, nullptr);
+      for (int it = issued - stages < 0 ? 0 : issued - stages; it < issued; ++it)
+        mbar_wait(&full[it % stages], (it / stages) & 1, nullptr);
     goto finish;
   }
-  if (warp == 5) {
+  if (warp == kOzEpiWarps + 1) {
     // ---- MMA issuer ----
     if (lane != 0) goto finish;
     const uint64_t da0 = sw64_desc(su32(sA)), db0 = sw64_desc(su32(sB));
-    for (int kb = 0; kb < nk; ++kb) {
-      const int c = kb / kOzChunk, kc = kb % kOzChunk;
-      const int s = kb % stages;
-      if (kc == 0 && c > 0 && !mbar_wait(tfree, (c - 1) & 1, abort)) {
+    for (int it = 0; it < total; ++it) {
+      const int q = it / nk, kb = it % nk, s = it % stages;
+      const int kc = kb % kOzChunk, gc = q * nchunks + kb / kOzChunk;
+      if (kc == 0 && gc > 0 && !mbar_wait(tfree, (gc - 1) & 1, abort)) {
         *abort = 1;
         atomicExch(err, 1);
         break;
       }
-      if (!mbar_wait(&full[s], (kb / stages) & 1, abort)) {
+      if (!mbar_wait(&full[s], (it / stages) & 1, abort)) {
         *abort = 1;
         atomicExch(err, 1);
         break;
       }
       tc_after();
-      oz_issue<S>(tmem, da0 + (uint64_t)((s * S * kOzTileA) >> 4), db0 + (uint64_t)((s * S * kOzTileB) >> 4),
-                  kc == 0);
+      const uint64_t da = da0 + (uint64_t)((s * NSL * kOzTileA) >> 4), db = db0 + (uint64_t)((s * NSL * kOzTileB) >> 4);
+      if (q == 0)
+        oz_issue<S, 0, kOzGroups>(tmem, da, db, kc == 0);
+      else
+        oz_issue<S, kOzGroups, 2 * kOzGroups>(tmem, da, db, kc == 0);
       mma_commit(&empty[s]);
       if (kc == kOzChunk - 1 || kb == nk - 1) mma_commit(cfull);
     }
@@ -208,41 +225,44 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   }
 
   {
-  // ---- epilogue (warps 0-3): exact chunk sums into 64-bit integers ----
+  // ---- epilogue (warps 0-7): exact chunk sums into 64-bit integers ----
   // acc = sum_g G_g 2^(7 (S-1-g) - R) over the chunks, in units of
   // 2^(R - 7 (S+1)): R keeps the sum inside 63 bits (|G_0| < 2^23 per chunk);
   // groups shifted right by it are rounded, 2^-60 below the total at most.
   int lg = 0;
   while ((1 << lg) < nchunks) ++lg;
   const int R = max(0, 25 + lg + 7 * (S - 1) - 63);
-  long long acc[kOzBN];
+  const int quad = warp & 3, half = warp >> 2;
+  long long acc[64];
 #pragma unroll
-  for (int i = 0; i < kOzBN; ++i) acc[i] = 0;
+  for (int i = 0; i < 64; ++i) acc[i] = 0;
   bool ok = true;
-  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-  for (int c = 0; c < nchunks; ++c) {
-    if (!mbar_wait(cfull, c & 1, abort)) {
+  const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * 64);
+  for (int gc = 0; gc < NP * nchunks; ++gc) {
+    if (!mbar_wait(cfull, gc & 1, abort)) {
       ok = false;
       break;
     }
     tc_after();
+    const int q = gc / nchunks;
+    const int ghi = min(S, kOzGroups * (q + 1));
 #pragma unroll 1
-    for (int g = 0; g < S; ++g) {
+    for (int g = kOzGroups * q; g < ghi; ++g) {
       const int sh = 7 * (S - 1 - g) - R;
+      const uint32_t col = (uint32_t)((g - kOzGroups * q) * kOzBN);
 #pragma unroll
-      for (int h = 0; h < kOzBN; h += 32) {
-        uint32_t r[32];
-        tmem_ld16_async(lane_base + (uint32_t)(g * kOzBN + h), r);
-        tmem_ld16_async(lane_base + (uint32_t)(g * kOzBN + h + 16), r + 16);
+      for (int h = 0; h < 64; h += 16) {  // 16 columns at a time: 10 warps leave 168 registers a thread
+        uint32_t r[16];
+        tmem_ld16_async(lane_base + col + (uint32_t)h, r);
         tmem_wait(r);
         if (sh >= 0) {
 #pragma unroll
-          for (int i = 0; i < 32; ++i) acc[h + i] += (long long)__float2int_rn(__uint_as_float(r[i])) << sh;
+          for (int i = 0; i < 16; ++i) acc[h + i] += (long long)__float2int_rn(__uint_as_float(r[i])) << sh;
         } else {
-          const long long half = 1LL << (-sh - 1);
+          const long long rnd = 1LL << (-sh - 1);
 #pragma unroll
-          for (int i = 0; i < 32; ++i)
-            acc[h + i] += ((long long)__float2int_rn(__uint_as_float(r[i])) + half) >> (-sh);
+          for (int i = 0; i < 16; ++i)
+            acc[h + i] += ((long long)__float2int_rn(__uint_as_float(r[i])) + rnd) >> (-sh);
         }
       }
     }
@@ -254,7 +274,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   tc_after();
   if (!all_done) atomicExch(err, 1);
   if (ok && all_done && !*abort) {
-    const int row = m0 + warp * 32 + lane;
+    const int row = m0 + quad * 32 + lane;
     if (row < mp) {
       double2 *out = b.optr ? *reinterpret_cast<double2 *const *>(b.optr + (size_t)p * b.optr_stride)
                             : b.out + (size_t)p * b.out_stride;
@@ -262,8 +282,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       const long long cs = b.cs ? b.cs : mp;  // cs == 0: column stride = this problem's row count
       const int eu = R - 7 * (S + 1);          // exponent of the accumulator's unit
 #pragma unroll
-      for (int t = 0; t < kOzBN / 2; ++t) {
-        const int j = n0 / 2 + t;
+      for (int t = 0; t < 32; ++t) {
+        const int j = n0 / 2 + half * 32 + t;
         if (j < np) {
           const int eb = b.b_exp[(size_t)p * (b.n_pad / 2) + j];
           double2 r = make_double2(0.0, 0.0);

@@ -219,6 +219,7 @@ struct tebd_handle {
 namespace tebd {
 
 int set_error(tebd_handle *h, int code, const std::string &msg);
+void set_noh_error(const std::string &msg);  // for tebd_last_error(NULL)
 int check_cuda(tebd_handle *h, cudaError_t e, const char *what);
 
 // kernels launched from capi.cu (defined in the .cu files)
