@@ -1706,6 +1706,13 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
         C = c;
       }
     }
+    if (tp.cluster > cmax && tp.cluster <= 8) {  // beyond the default's range: every CTA
+      cfg.gridDim = dim3(tp.cluster, nb, 1);      // still gets its share of the rows (or none)
+      attr[0].val.clusterDim.x = tp.cluster;
+      int ncl = 0;
+      tuned_ok = cudaOccupancyMaxActiveClusters(&ncl, (const void *)kern, &cfg) == cudaSuccess && ncl >= 1;
+      if (!tuned_ok) cudaGetLastError();
+    }
     if (tp.cluster > 0) {  // the autotuner's size, when the launch can use it
       if (tuned_ok)
         C = tp.cluster;

@@ -268,6 +268,11 @@ inline size_t gate_smem_bytes(int d) {
 // reads are coalesced), the block synchronises, and every output element
 // (pair, row) is a d^2-term dot product with one gate row.  Pairs of different
 // blocks are disjoint, so the update is in place.
+// kDF (the precision and learned-rank forms): the gate's d^2 complex
+// multiply-adds per entry in double-float on the FP32 pipe (48-bit significands;
+// the FP64 pipe made this kernel FP64-bound at chi = 512), the result rounded
+// back to FP64.
+template <bool kDF>
 __global__ void __launch_bounds__(128) k_gate_apply(Slot *slots, int chi, int d) {
   extern __shared__ double2 gsm[];  // d^4 gate | kGatePairs * d^2 vectors
   const int s = blockIdx.y;
@@ -281,12 +286,22 @@ __global__ void __launch_bounds__(128) k_gate_apply(Slot *slots, int chi, int d)
   const int m = cp.m, r0 = cp.r0, r2 = cp.r2;
   const int np = min(kGatePairs, npairs - p0);
   double2 *X = slots[s].X;
-  for (int e = threadIdx.x; e < d2 * d2; e += blockDim.x) gsm[e] = G[e];
+  float4 *gdf = reinterpret_cast<float4 *>(gsm), *vdf = reinterpret_cast<float4 *>(vsm);  // kDF views
+  for (int e = threadIdx.x; e < d2 * d2; e += blockDim.x) {
+    if (kDF)
+      gdf[e] = dfs(G[e]);
+    else
+      gsm[e] = G[e];
+  }
   for (int e = threadIdx.x; e < kGatePairs * d2; e += blockDim.x) {
     const int p = e % kGatePairs, kl = e / kGatePairs;
     if (p >= np) continue;
     const int t = p0 + p, a = t % r0, b = t / r0, k = kl / d, l = kl % d;
-    vsm[e] = X[(size_t)(k * r0 + a) + (size_t)m * (l * r2 + b)];
+    const double2 x = X[(size_t)(k * r0 + a) + (size_t)m * (l * r2 + b)];
+    if (kDF)
+      vdf[e] = dfs(x);
+    else
+      vsm[e] = x;
   }
   __syncthreads();
   for (int e = threadIdx.x; e < kGatePairs * d2; e += blockDim.x) {
@@ -294,13 +309,19 @@ __global__ void __launch_bounds__(128) k_gate_apply(Slot *slots, int chi, int d)
     if (p >= np) continue;
     const int t = p0 + p, a = t % r0, b = t / r0, i = row / d, j = row % d;
     double2 acc = make_double2(0.0, 0.0);
-    for (int kl = 0; kl < d2; ++kl) {
-      const double2 g = gsm[row + d2 * kl];
-      const double2 v = vsm[kl * kGatePairs + p];
-      acc.x = fma(g.x, v.x, acc.x);
-      acc.x = fma(-g.y, v.y, acc.x);
-      acc.y = fma(g.x, v.y, acc.y);
-      acc.y = fma(g.y, v.x, acc.y);
+    if (kDF) {
+      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+      for (int kl = 0; kl < d2; ++kl) df_cmac(rh, rl, ih, il, gdf[row + d2 * kl], vdf[kl * kGatePairs + p]);
+      acc = dfd(make_float4(rh, rl, ih, il));
+    } else {
+      for (int kl = 0; kl < d2; ++kl) {
+        const double2 g = gsm[row + d2 * kl];
+        const double2 v = vsm[kl * kGatePairs + p];
+        acc.x = fma(g.x, v.x, acc.x);
+        acc.x = fma(-g.y, v.y, acc.x);
+        acc.y = fma(g.x, v.y, acc.y);
+        acc.y = fma(g.y, v.x, acc.y);
+      }
     }
     X[(size_t)(i * r0 + a) + (size_t)m * (j * r2 + b)] = acc;
   }
@@ -308,9 +329,9 @@ __global__ void __launch_bounds__(128) k_gate_apply(Slot *slots, int chi, int d)
 
 // Opt k_gate_apply into the shared memory it needs on the current device (a
 // per-function attribute; cheap, made before every launch).
-static cudaError_t set_gate_smem(int d) {
-  return cudaFuncSetAttribute(k_gate_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)gate_smem_bytes(d));
+static cudaError_t set_gate_smem(int d, bool df = false) {
+  return cudaFuncSetAttribute(df ? k_gate_apply<true> : k_gate_apply<false>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gate_smem_bytes(d));
 }
 
 // ---------------------------------------------------------------------------
@@ -545,10 +566,11 @@ int launch_dense_prepare(tebd_handle *h, int nb, bool /*real_gate: converted on 
     k_theta_form<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,
                                                                          h->slots_d, chi, d);
   TEBD_LAUNCHED(h);
-  int rc = check_cuda(h, set_gate_smem(d), "gate shared memory");
+  const bool gdf = h->opts.svd_mode == TEBD_SVD_DF || h->opts.svd_mode == TEBD_SVD_RSVD;
+  int rc = check_cuda(h, set_gate_smem(d, gdf), "gate shared memory");
   if (rc) return rc;
-  k_gate_apply<<<dim3(cdiv((size_t)chi * chi, kGatePairs), nb), 128, gate_smem_bytes(d), st>>>(
-      h->slots_d, chi, d);
+  (gdf ? k_gate_apply<true> : k_gate_apply<false>)<<<dim3(cdiv((size_t)chi * chi, kGatePairs), nb), 128,
+                                                     gate_smem_bytes(d), st>>>(h->slots_d, chi, d);
   TEBD_LAUNCHED(h);
   k_norm_partial<<<dim3(kNormParts, nb), 256, 0, st>>>(h->slots_d, h->nrm_part);
   TEBD_LAUNCHED(h);
@@ -641,7 +663,7 @@ cudaError_t raw_dense_prepare(cudaStream_t st, double2 *gam, const double *lam, 
                                                                       chi, d);
   cudaError_t e = set_gate_smem(d);
   if (e != cudaSuccess) return e;
-  k_gate_apply<<<dim3(cdiv((size_t)chi * chi, kGatePairs), 1), 128, gate_smem_bytes(d), st>>>(
+  k_gate_apply<false><<<dim3(cdiv((size_t)chi * chi, kGatePairs), 1), 128, gate_smem_bytes(d), st>>>(
       slots_d, chi, d);
   k_norm_partial<<<dim3(kNormParts, 1), 256, 0, st>>>(slots_d, nrm_part);
   k_norm_final<<<1, 32, 0, st>>>(nrm_part, nrm, jp, 1, status);
