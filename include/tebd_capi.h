@@ -311,6 +311,9 @@ typedef struct tebd_stats {
   long long tc_launches;       /* tensor-core product kernels timed                       */
   double tc_mma_flops;         /* flops those kernels issued on the tensor cores (2 per
                                   multiply-add, bf16 or TF32 operands, padding included)  */
+  long long rsvd_batches;      /* batches that ran the randomized route                    */
+  long long rsvd_oversample_sum; /* their sketch oversampling p, summed (mean = / batches) */
+  long long rsvd_power_sum;    /* their power-iteration counts q, summed                   */
 } tebd_stats;
 int tebd_set_profiling(tebd_handle *h, int on);
 int tebd_get_stats(tebd_handle *h, tebd_stats *stats);
@@ -324,8 +327,8 @@ int tebd_measure_fp64_peak(int device, double *tflops);
  * their gates, as tebd_apply_bonds would update them: the default choice, each
  * cluster size 1..8 of the bidiagonalisation, each bisection team of 1, 2, 4, 8
  * lanes with the best cluster, and, when the randomized route runs, each
- * cluster of 1, 2, 4, 8 CTAs per bond and each panel of 4, 8, 16 rows of its
- * Cholesky.  The fastest (by more than 1 %) is kept in
+ * cluster of 1, 2, 4, 8 CTAs per bond, each panel of 4, 8, 16 rows and each leaf
+ * size 128, 192, 256, 384, 768 of its recursively blocked Cholesky.  The fastest (by more than 1 %) is kept in
  * a table per device under (route, largest compacted dimension rounded up to
  * 64, bonds rounded up to a power of two), which every later batch on the device
  * uses.  Shapes change no result beyond rounding.  The chain is left as it was
@@ -334,11 +337,12 @@ int tebd_measure_fp64_peak(int device, double *tflops);
  * batch's time with the default and with the chosen shape. */
 int tebd_autotune(tebd_handle *h, int nbonds, const int *links, const double *const *gates, double *base_ms,
                   double *best_ms);
-/* The device's table: up to max_entries rows of 8 ints (route: 0 FP64
- * bidiagonal, 1 double-float bidiagonal, 2 randomized-route Cholesky; dimension
- * bucket; bonds bucket; bidiagonalisation cluster size; bisection team size;
- * Cholesky cluster size; Cholesky panel height -- 0 = the default; batch time
- * in microseconds); *count = rows in the table. */
+/* The device's table: up to max_entries rows of 9 ints (route: 0 FP64
+ * bidiagonal, 1 double-float bidiagonal, 2 randomized-route Cholesky leaf, 3 its
+ * blocking; dimension bucket; bonds bucket; bidiagonalisation cluster size;
+ * bisection team size; Cholesky cluster size; Cholesky panel height; Cholesky
+ * leaf size -- 0 = the default; batch time in microseconds); *count = rows in
+ * the table. */
 int tebd_get_tuning(int device, int *entries, int max_entries, int *count);
 /* Empty the device's table (the defaults apply again). */
 int tebd_clear_tuning(int device);

@@ -25,6 +25,7 @@ TYPE, BIND(C) :: tebd_stats
   REAL(C_DOUBLE) :: tc_ms
   INTEGER(C_LONG_LONG) :: tc_launches
   REAL(C_DOUBLE) :: tc_mma_flops
+  INTEGER(C_LONG_LONG) :: rsvd_batches, rsvd_oversample_sum, rsvd_power_sum
 END TYPE
 INTERFACE
   SUBROUTINE tebd_default_opts(o) BIND(C, NAME='tebd_default_opts')
@@ -218,7 +219,7 @@ INTERFACE
   INTEGER(C_INT) FUNCTION tebd_get_tuning(device, entries, max_entries, count) BIND(C, NAME='tebd_get_tuning')
     IMPORT :: C_INT
     INTEGER(C_INT), VALUE :: device, max_entries
-    INTEGER(C_INT) :: entries(8, *)
+    INTEGER(C_INT) :: entries(9, *)
     INTEGER(C_INT) :: count
   END FUNCTION
   INTEGER(C_INT) FUNCTION tebd_clear_tuning(device) BIND(C, NAME='tebd_clear_tuning')

@@ -547,7 +547,12 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
           nrs += h->path_h[s] == kPathRsvd;
         }
         h->stats.rsvd_skipped += std::count(allow.begin(), allow.end(), 0);
-        if (nrs && (rc = run_rsvd(h, nb, cps, h->path_h, rank, sketch, power))) return rc;
+        if (nrs) {
+          ++h->stats.rsvd_batches;
+          h->stats.rsvd_oversample_sum += over;
+          h->stats.rsvd_power_sum += power;
+          if ((rc = run_rsvd(h, nb, cps, h->path_h, rank, sketch, power))) return rc;
+        }
       }
       for (int s = 0; s < nb; ++s) {
         if (nrs && h->path_h[s] != kPathQRJ) {  // randomized route, or its fallback to the full SVD

@@ -716,15 +716,15 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
     return e;
   };
   // Cholesky + inverse of the s x s Gram at c.g into c.ri, recursively by halves
-  // above kCholLeaf: with G = [G11 G12; G12^H G22] (n1 + n2),
+  // above chol_leaf: with G = [G11 G12; G12^H G22] (n1 + n2),
   //   R11 = chol(G11), R12 = R11^-H G12 (in place of G12), G22 -= R12^H R12,
   //   R22 = chol(G22), Ri12 = -Ri11 (R12 Ri22) (R12 Ri22 through c.w),
   // the off-diagonal work as digit-plane products on the tensor cores, the
   // diagonal leaves in k_rs_chol.  Every pivot is judged against the whole
   // Gram's threshold.
-  constexpr int kCholLeaf = 384;
+  int chol_leaf = 384;  // the default; the autotuner may set it per sketch width
   std::function<int(size_t, size_t, int, int)> crec = [&](size_t gb, size_t rb, int n, int sl) -> int {
-    if (n <= kCholLeaf) return leaf(gb, rb, n, s);
+    if (n <= chol_leaf) return leaf(gb, rb, n, s);
     const int n1 = (n / 2 + 31) / 32 * 32, n2 = n - n1;
     const size_t col = sizeof(double2) * (size_t)s;  // bytes per column (ld s)
     const size_t g12 = gb + col * n1, g22 = gb + col * n1 + sizeof(double2) * n1;
@@ -738,6 +738,14 @@ int run_rsvd(tebd_handle *h, int nb, const std::vector<Compact> &cps, std::vecto
     return TEBD_OK;
   };
   auto rs_chol = [&](int ss, double fl, int sl) -> int {
+    const TuneParams tb = tune_lookup(h, 3, ss, nact);
+    chol_leaf = 384;
+    if (tb.chol_leaf > 0) {
+      if (tb.chol_leaf >= 64 && tb.chol_leaf <= kRsvdMaxSketch)
+        chol_leaf = tb.chol_leaf;
+      else
+        tune_reject(h);
+    }
     k_rs_thresh<<<nb, 256, 0, st>>>(R->dims_d, ws, per, c.g, ss, fl, c.th);
     TEBD_LAUNCHED(h);
     int e = check_cuda(h, cudaMemset2DAsync(ws + c.ri, per, 0, sizeof(double2) * (size_t)ss * ss, nb, st),

@@ -132,6 +132,7 @@ struct TuneParams {
   int team;          // lanes per value of the bisection
   int panel;         // rows of R per panel of the randomized route's Cholesky
   int chol_cluster;  // CTAs per bond of that Cholesky
+  int chol_leaf;     // largest diagonal block the recursive Cholesky factors directly
 };
 
 }  // namespace tebd
@@ -211,7 +212,7 @@ struct tebd_handle {
   // whether a launch could not use the forced shape
   struct {
     int active = 0, rejected = 0;
-    tebd::TuneParams force{0, 0, 0, 0};
+    tebd::TuneParams force{0, 0, 0, 0, 0};
     std::vector<std::array<int, 3>> seen;
   } tune;
 };
@@ -247,8 +248,8 @@ struct BidiagBatch {
 };
 int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b);
 // Autotuner table (tune.cu): the shape for route (0 FP64 bidiagonal, 1
-// double-float bidiagonal, 2 randomized-route Cholesky), largest dimension n
-// and bonds nb; zeros where no entry exists.  tune_reject: the launch could not
+// double-float bidiagonal, 2 randomized-route Cholesky leaf, 3 its blocking),
+// largest dimension n and bonds nb; zeros where no entry exists.  tune_reject: the launch could not
 // use the shape it was given.
 TuneParams tune_lookup(tebd_handle *h, int route, int n, int nb);
 void tune_reject(tebd_handle *h);

@@ -8,13 +8,14 @@
 //   * the team size of the bisection (k_bd_sigma<team>: 1, 2, 4 or 8 lanes
 //     evaluate Sturm counts at that many points per step for one value);
 //   * the panel height of the randomized route's Cholesky (k_rs_chol: 4, 8 or 16
-//     rows of R staged in shared memory per panel) and the CTAs that share one
-//     bond's Cholesky (a cluster of 1..8).
+//     rows of R staged in shared memory per panel), the CTAs that share one
+//     bond's Cholesky (a cluster of 1..8), and the size below which its
+//     recursive blocking factors a diagonal block directly (128 .. 768).
 // Without a table the library picks them from occupancy queries and thread
 // counts (bidiag.cu, rsvd.cu).  tebd_autotune times candidates on a batch of
 // real bonds -- the default choice, then every cluster size, then every team
-// size with the best cluster, then every Cholesky cluster size and panel
-// height -- restoring the touched
+// size with the best cluster, then every Cholesky cluster size, panel height
+// and leaf size -- restoring the touched
 // Gammas, Lambdas and labels after each trial, and keeps the fastest per
 // (route, largest compacted dimension rounded up to 64, bonds in the batch
 // rounded up to a power of two) in a table per device that every later batch on
@@ -59,7 +60,7 @@ TuneParams tune_lookup(tebd_handle *h, int route, int n, int nb) {
   }
   std::lock_guard<std::mutex> lock(g_mu);
   const auto it = g_table.find({h->device, key[0], key[1], key[2]});
-  if (it == g_table.end()) return TuneParams{0, 0, 0, 0};
+  if (it == g_table.end()) return TuneParams{0, 0, 0, 0, 0};
   return it->second.p;
 }
 
@@ -132,10 +133,13 @@ extern "C" int tebd_autotune(tebd_handle *h, int nbonds, const int *links, const
   if (!rc) rc = check_cuda(h, cudaEventCreate(&e0), "autotune event");
   if (!rc) rc = check_cuda(h, cudaEventCreate(&e1), "autotune event");
   // one timed trial of the batch with the shape `f` (0 entries: the default)
+  // the keys the winning shape's launches used (the ones it is stored under)
+  std::vector<std::array<int, 3>> win_keys;
   auto trial = [&](TuneParams f, float *ms) -> int {
     h->tune.active = 1;
     h->tune.force = f;
     h->tune.rejected = 0;
+    h->tune.seen.clear();
     int r = check_cuda(h, cudaEventRecord(e0, h->stream), "autotune event");
     if (!r) r = run_bond_batch(h, nb, lk.data(), gates, te.data());
     if (!r) r = check_cuda(h, cudaEventRecord(e1, h->stream), "autotune event");
@@ -147,23 +151,25 @@ extern "C" int tebd_autotune(tebd_handle *h, int nbonds, const int *links, const
     return r ? r : r2;
   };
   float base = 0.f, best = 0.f;
-  TuneParams win{0, 0, 0, 0};
+  TuneParams win{0, 0, 0, 0, 0};
   if (!rc) rc = trial(win, &base);  // warm-up of workspaces and kernels
-  h->tune.seen.clear();
   if (!rc) rc = trial(win, &base);
   best = base;
+  win_keys = h->tune.seen;
   bool any_rsvd = false;
   for (const auto &k : h->tune.seen) any_rsvd |= k[0] == 2;
   auto sweep = [&](int which, const std::vector<int> &vals) -> int {
     for (int v : vals) {
       TuneParams f = win;
-      (which == 0 ? f.cluster : which == 1 ? f.team : which == 2 ? f.chol_cluster : f.panel) = v;
+      (which == 0 ? f.cluster : which == 1 ? f.team : which == 2 ? f.chol_cluster : which == 3 ? f.panel
+                                                                                    : f.chol_leaf) = v;
       float ms = 0.f;
       const int r = trial(f, &ms);
       if (r) return r;
       if (ms > 0.f && ms < 0.99f * best) {  // 1 %: above the trials' timing noise
         best = ms;
         win = f;
+        win_keys = h->tune.seen;
       }
     }
     return TEBD_OK;
@@ -172,10 +178,10 @@ extern "C" int tebd_autotune(tebd_handle *h, int nbonds, const int *links, const
   if (!rc) rc = sweep(1, {1, 2, 4, 8});
   if (!rc && any_rsvd) rc = sweep(2, {1, 2, 4, 8});
   if (!rc && any_rsvd) rc = sweep(3, {4, 8, 16});
+  if (!rc && any_rsvd) rc = sweep(4, {128, 192, 256, 384, 768});
   if (!rc) {
     std::lock_guard<std::mutex> lock(g_mu);
-    for (const auto &k : h->tune.seen)
-      g_table[{h->device, k[0], k[1], k[2]}] = TuneEntry{win, best * 1e3f};
+    for (const auto &k : win_keys) g_table[{h->device, k[0], k[1], k[2]}] = TuneEntry{win, best * 1e3f};
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
@@ -195,7 +201,7 @@ extern "C" int tebd_get_tuning(int device, int *entries, int max_entries, int *c
   for (const auto &kv : g_table) {
     if (kv.first[0] != device) continue;
     if (w < max_entries) {
-      int *o = entries + 8 * w++;
+      int *o = entries + 9 * w++;
       o[0] = kv.first[1];
       o[1] = kv.first[2];
       o[2] = kv.first[3];
@@ -203,7 +209,8 @@ extern "C" int tebd_get_tuning(int device, int *entries, int max_entries, int *c
       o[4] = kv.second.p.team;
       o[5] = kv.second.p.chol_cluster;
       o[6] = kv.second.p.panel;
-      o[7] = (int)kv.second.us;
+      o[7] = kv.second.p.chol_leaf;
+      o[8] = (int)kv.second.us;
     }
     ++n;
   }

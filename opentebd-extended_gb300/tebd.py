@@ -129,6 +129,9 @@ class Stats(ctypes.Structure):
         ("tc_ms", ctypes.c_double),
         ("tc_launches", ctypes.c_longlong),
         ("tc_mma_flops", ctypes.c_double),
+        ("rsvd_batches", ctypes.c_longlong),
+        ("rsvd_oversample_sum", ctypes.c_longlong),
+        ("rsvd_power_sum", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -581,7 +584,8 @@ def measure_fp64_peak(device=0):
     return float(v[0])
 
 
-TUNE_ROUTES = {0: "fp64 bidiagonal", 1: "double-float bidiagonal", 2: "randomized-route Cholesky"}
+TUNE_ROUTES = {0: "fp64 bidiagonal", 1: "double-float bidiagonal", 2: "randomized-route Cholesky",
+               3: "randomized-route Cholesky blocking"}
 
 
 def get_tuning(device=0):
@@ -592,12 +596,12 @@ def get_tuning(device=0):
     if rc != TEBD_OK:
         raise TebdError(rc, "tebd_get_tuning failed")
     n = int(cnt[0])
-    buf = np.zeros(8 * max(n, 1), dtype=np.int32)
+    buf = np.zeros(9 * max(n, 1), dtype=np.int32)
     rc = lib.tebd_get_tuning(device, _ip(buf), n, _ip(cnt))
     if rc != TEBD_OK:
         raise TebdError(rc, "tebd_get_tuning failed")
-    keys = ("route", "n_bucket", "bonds_bucket", "cluster", "team", "chol_cluster", "panel", "batch_us")
-    rows = [dict(zip(keys, (int(v) for v in buf[8 * i:8 * i + 8]))) for i in range(n)]
+    keys = ("route", "n_bucket", "bonds_bucket", "cluster", "team", "chol_cluster", "panel", "chol_leaf", "batch_us")
+    rows = [dict(zip(keys, (int(v) for v in buf[9 * i:9 * i + 9]))) for i in range(n)]
     for r in rows:
         r["route"] = TUNE_ROUTES.get(r["route"], r["route"])
     return rows
