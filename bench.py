@@ -253,7 +253,7 @@ def run_reference(args):
 # the mixed form's trained model and the saturated-bond legs
 # ---------------------------------------------------------------------------
 MODEL_PATH = os.path.join(ROOT, "opentebd-extended_gb300", "data", "rsvd_model.npz")
-MODEL_TARGET = 1e-8
+MODEL_TARGET = 1e-10
 
 
 def load_model(pkg, device):
@@ -287,7 +287,7 @@ def saturated_state(Ls=L, chi=CHI, decay=16.0, d=D):
 
 
 def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=16.0, prepare=True,
-                   tune=("fp64", "mixed")):
+                   tune=("fp64", "mixed", "mixed_without_model")):
     """The odd bonds of a saturated chain, updated `steps` times (one batched sweep
     each), in plain FP64 and in the mixed form, profiled: updates/s from CUDA events
     on each chain's stream, and the roofline of each form's dominant kernel from
@@ -323,11 +323,14 @@ def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=1
                      "as at every update of a run)" if prepare else
                      "random state: full-rank Theta, large discarded weight (harder than any step of a run)")}
     finals = {}
-    for name in ("fp64", "mixed"):
+    # "mixed_without_model": the A/B leg -- the same form with the library's fixed
+    # sketch (tebd_set_rsvd defaults, p = 64, q = 2) instead of the network's choice
+    for name in ("fp64", "mixed", "mixed_without_model"):
         c = pkg.Chain(Ls, D, chi, device=device, svd_mode=SVD_MODES["fp64" if name == "fp64" else "rsvd"])
         model = None
-        if name == "mixed":
+        if name != "fp64":
             c.set_theta_form(107)
+        if name == "mixed":
             model = load_model(pkg, device)
             c.set_rsvd_model(model, MODEL_TARGET)
         c.set_state(gam, lam)
@@ -382,6 +385,13 @@ def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=1
     out["max_abs_err_vs_plain_fp64"] = {"n_i": float(np.max(np.abs(n1 - n0))),
                                         "bond_energy": float(np.max(np.abs(e1 - e0)))}
     out["within_error_bound"] = max(out["max_abs_err_vs_plain_fp64"].values()) <= 1e-8
+    (r2, n2, e2) = finals["mixed_without_model"]
+    out["ab_model"] = {
+        "what": "the mixed form with the trained network choosing the sketch (mixed) against the same form with "
+                "the fixed default sketch p = 64, q = 2 (mixed_without_model)",
+        "speedup_from_model": out["mixed_without_model"]["ms_per_step"] / out["mixed"]["ms_per_step"],
+        "max_abs_err_vs_plain_fp64_without_model": {"n_i": float(np.max(np.abs(n2 - n0))),
+                                                    "bond_energy": float(np.max(np.abs(e2 - e0)))}}
     return out
 
 
@@ -616,7 +626,7 @@ def run_ours(args):
         "saturated_random_start": (saturated_legs(pkg, local, args, fp64_peak, prepare=False, tune=())
                                    if not args.no_precision else None),
         "saturated_chi512": (saturated_legs(pkg, local, args, fp64_peak, steps=1, Ls=32, chi=512, decay=64.0,
-                                            tune=("mixed",))
+                                            tune=("mixed", "mixed_without_model"))
                              if not args.no_precision and not args.no_chi512 else None),
         "autotune_table": pkg.get_tuning(local) if not args.no_precision else None,
         **({"rank_form": {"what": "kept-rank form: per-update discarded-weight bound "

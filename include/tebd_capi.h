@@ -220,10 +220,12 @@ int tebd_set_rsvd(tebd_handle *h, int oversample, int power_iters, double tol, i
  * Parameters: one float vector W1 (128 x 67, row-major), b1, W2 (128 x 128), b2,
  * W3 (8 x 128), b3.  Loss: mean squared error over the outputs.
  * Attached to a TEBD_SVD_RSVD handle, the model's predictions set, per batch,
- * the randomized route's oversampling and power count (the cheapest pair whose
- * predicted (sigma_{r+p} / sigma_r)^(2q+2) is at most `target`) and send bonds
- * with no such pair straight to the full SVD; the judge still checks every bond
- * the sketch decomposes. */
+ * the randomized route's oversampling p and power count q -- the cheapest pair
+ * (by the route's time model: products n^2 s (2q + 4), Choleskys and Gram SVD
+ * s^3 (6 (q + 2) + 128), s = chi + p) whose predicted missed weight
+ * (sigma_chi / sigma_0)^2 (sigma_{chi+p} / sigma_chi)^(2q+2) is at most `target` --
+ * and send bonds with no such pair straight to the full SVD; the judge still
+ * checks every bond the sketch decomposes. */
 typedef struct tebd_mlp tebd_mlp;
 int tebd_mlp_create(int device, unsigned long long seed, tebd_mlp **out);
 int tebd_mlp_destroy(tebd_mlp *m);

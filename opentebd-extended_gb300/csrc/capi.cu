@@ -432,13 +432,21 @@ static bool rsvd_candidate(const tebd_handle *h, const Compact &c) {
 
 // The learned model's choice for the randomized route of one batch: per bond
 // the predicted log10 sigma_k / sigma_0 at k / chi = kMlpRanks (interpolated
-// linearly, extended past the last point along its last segment); a pair (p, q)
-// is feasible for a bond when (2q + 2) log10(sigma_{chi+p} / sigma_chi) <=
-// log10(target), and costs (chi + p)(2q + 4) -- the sketch's product columns over
-// its passes.  Each bond takes its cheapest feasible pair; bonds with none take
-// the full SVD (allow = 0); the batch runs with the largest p and q chosen.
-static int rsvd_model_choice(tebd_handle *h, int nb, const double *const *gates, int *over, int *power,
-                             std::vector<char> &allow) {
+// linearly, extended past the last point along its last segment).  A pair (p, q)
+// is feasible for a bond when the weight the sketch can miss in the kept
+// directions, (sigma_chi / sigma_0)^2 (sigma_{chi+p} / sigma_chi)^(2q + 2), is at
+// most `target` (the directions near sigma_chi converge slowest and carry the
+// least weight) and the judge's residual of the slowest kept direction,
+// (sigma_chi / sigma_0) (sigma_{chi+p} / sigma_chi)^(2q + 1), is a decade inside
+// its tolerance.  Its cost is the route's time model, in units of one product
+// column over an n x n Theta: n^2 s (2q + 4) for the products (the sketch, q
+// power iterations and the Rayleigh-Ritz and judge passes) plus s^3 (6 (q + 2) +
+// 128) for the q + 2 Choleskys and the s x s Gram SVD (s = chi + p; weights
+// measured on GB300 at chi = 512, where the Gram SVD is about as costly as all
+// the products).  Each bond takes its cheapest feasible pair; bonds with none
+// take the full SVD (allow = 0); the batch runs with the largest p and q chosen.
+static int rsvd_model_choice(tebd_handle *h, int nb, const double *const *gates, const std::vector<Compact> &cps,
+                             int *over, int *power, std::vector<char> &allow) {
   const int d2 = h->d * h->d;
   std::vector<float> gt(3 * (size_t)nb), pred((size_t)kMlpOut * nb);
   for (int s = 0; s < nb; ++s) {
@@ -465,17 +473,23 @@ static int rsvd_model_choice(tebd_handle *h, int nb, const double *const *gates,
   };
   static const int kP[] = {16, 32, 48, 64, 96, 128};
   const double lt = log10(h->rs_target);
+  // the judge's residual of the slowest kept direction is about
+  // sigma_chi (sigma_{chi+p} / sigma_chi)^(2q+1): kept a decade inside its tolerance
+  const double ltol = log10(h->rs_tol) - 1.0;
   int pmax = 0, qmax = 0;
   for (int s = 0; s < nb; ++s) {
     const float *y = pred.data() + (size_t)kMlpOut * s;
-    const double y1 = at(y, 1.0);
+    const double y1 = std::min(0.0, at(y, 1.0));
+    const double nn = (double)std::max(cps[s].m, cps[s].n);
     double best = 1e300;
     int bp = -1, bq = -1;
     for (int p : kP)
       for (int q = 0; q <= 3; ++q) {
         const double lr = at(y, (double)(h->chi + p) / h->chi) - y1;
-        if (!(lr < 0.0) || (2.0 * q + 2.0) * lr > lt) continue;
-        const double cost = (double)(h->chi + p) * (2 * q + 4);
+        if (!(lr < 0.0) || 2.0 * y1 + (2.0 * q + 2.0) * lr > lt) continue;
+        if (y1 + (2.0 * q + 1.0) * lr > ltol) continue;  // the judge would reject the slowest direction
+        const double sk = (double)(h->chi + p);
+        const double cost = nn * nn * sk * (2 * q + 4) + sk * sk * sk * (6.0 * (q + 2) + 128.0);
         if (cost < best) {
           best = cost;
           bp = p;
@@ -535,7 +549,7 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
         std::vector<char> allow(nb, 1);
         bool any = false;
         for (int s = 0; s < nb; ++s) any |= rsvd_candidate(h, cps[s]);
-        if (any && h->rs_model && (rc = rsvd_model_choice(h, nb, gates, &over, &power, allow))) return rc;
+        if (any && h->rs_model && (rc = rsvd_model_choice(h, nb, gates, cps, &over, &power, allow))) return rc;
         const int sketch = h->chi + over;
         for (int s = 0; s < nb; ++s) {
           const int mn = std::min(cps[s].m, cps[s].n);

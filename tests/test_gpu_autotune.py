@@ -55,6 +55,12 @@ def test_autotune_keeps_state_and_results(pkg, oracle, mode):
                 assert r["batch_us"] > 0
             c.apply_bonds(links, [gate] * len(links))  # tuned shapes
             gt, lt = c.get_state()
+            st = c.stats()
+            if mode == "rsvd":  # one batch on the route, with the sketch set above
+                assert st["rsvd_batches"] == 1 and st["rsvd_updates"] > 0
+                assert st["rsvd_oversample_sum"] == 32 and st["rsvd_power_sum"] == 2
+            else:
+                assert st["rsvd_batches"] == 0
         pkg.clear_tuning(0)
         assert pkg.get_tuning(0) == []
         with pkg.Chain(L, d, chi, svd_mode=svd) as c:  # default shapes, same start

@@ -121,7 +121,7 @@ def test_learned_model_gains_over_fixed_sketch(pkg):
             if sketch is not None:
                 c.set_rsvd(oversample=sketch[0], power_iters=sketch[1])
             if model is not None:
-                c.set_rsvd_model(model, 1e-6)
+                c.set_rsvd_model(model, 1e-10)
             for _ in range(3):
                 c.trotter_step(gates, 2)
             g, l = c.get_state()
@@ -188,7 +188,7 @@ def test_spin1_learned_form_matches_fp64(pkg):
             if name == "fixed":
                 c.set_rsvd(oversample=24, power_iters=2)
             if name == "learned":
-                c.set_rsvd_model(m, 1e-8)
+                c.set_rsvd_model(m, 1e-10)
             c.set_state(gam, lam)
             for _ in range(6):
                 c.trotter_step(U, 2)
