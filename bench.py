@@ -374,7 +374,8 @@ def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=1
             leg_["rsvd"] = {"updates": st["rsvd_updates"], "fallbacks": st["rsvd_fallbacks"],
                             "skipped_by_model": st["rsvd_skipped"], "worst_residual": st["rsvd_worst_residual"],
                             "mean_oversample": st["rsvd_oversample_sum"] / max(1, st["rsvd_batches"]),
-                            "mean_power_iters": st["rsvd_power_sum"] / max(1, st["rsvd_batches"])}
+                            "mean_power_iters": st["rsvd_power_sum"] / max(1, st["rsvd_batches"]),
+                            "retries": st["rsvd_retries"]}
         out[name] = leg_
         c.close()
         if model is not None:

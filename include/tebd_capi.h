@@ -225,7 +225,8 @@ int tebd_set_rsvd(tebd_handle *h, int oversample, int power_iters, double tol, i
  * s^3 (6 (q + 2) + 128), s = chi + p) whose predicted missed weight
  * (sigma_chi / sigma_0)^2 (sigma_{chi+p} / sigma_chi)^(2q+2) is at most `target` --
  * and send bonds with no such pair straight to the full SVD; the judge still
- * checks every bond the sketch decomposes. */
+ * checks every bond the sketch decomposes, and a bond it rejects is sketched once
+ * more with (p, q) = (128, 3) before it falls back to the full SVD. */
 typedef struct tebd_mlp tebd_mlp;
 int tebd_mlp_create(int device, unsigned long long seed, tebd_mlp **out);
 int tebd_mlp_destroy(tebd_mlp *m);
@@ -316,6 +317,8 @@ typedef struct tebd_stats {
   long long rsvd_batches;      /* batches that ran the randomized route                    */
   long long rsvd_oversample_sum; /* their sketch oversampling p, summed (mean = / batches) */
   long long rsvd_power_sum;    /* their power-iteration counts q, summed                   */
+  long long rsvd_retries;      /* bonds re-sketched with (p, q) = (128, 3) after the judge
+                                  rejected the model's sketch (then the full SVD if again) */
 } tebd_stats;
 int tebd_set_profiling(tebd_handle *h, int on);
 int tebd_get_stats(tebd_handle *h, tebd_stats *stats);

@@ -25,7 +25,7 @@ TYPE, BIND(C) :: tebd_stats
   REAL(C_DOUBLE) :: tc_ms
   INTEGER(C_LONG_LONG) :: tc_launches
   REAL(C_DOUBLE) :: tc_mma_flops
-  INTEGER(C_LONG_LONG) :: rsvd_batches, rsvd_oversample_sum, rsvd_power_sum
+  INTEGER(C_LONG_LONG) :: rsvd_batches, rsvd_oversample_sum, rsvd_power_sum, rsvd_retries
 END TYPE
 INTERFACE
   SUBROUTINE tebd_default_opts(o) BIND(C, NAME='tebd_default_opts')

@@ -565,7 +565,24 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
           ++h->stats.rsvd_batches;
           h->stats.rsvd_oversample_sum += over;
           h->stats.rsvd_power_sum += power;
+          std::vector<char> tried(nb, 0);
+          for (int s = 0; s < nb; ++s) tried[s] = h->path_h[s] == kPathRsvd;
           if ((rc = run_rsvd(h, nb, cps, h->path_h, rank, sketch, power))) return rc;
+          // with the model: the bonds its sketch did not pass the judge get one more
+          // sketch, the conservative (p, q) = (128, 3), before the full SVD
+          const int sk2 = h->chi + kRsvdRetryP;
+          if (h->rs_model && (over < kRsvdRetryP || power < kRsvdRetryQ) && sk2 <= kRsvdMaxSketch) {
+            int again = 0;
+            for (int s = 0; s < nb; ++s)
+              if (tried[s] && h->path_h[s] != kPathRsvd && std::min(cps[s].m, cps[s].n) >= sk2 + 16) {
+                h->path_h[s] = kPathRsvd;
+                ++again;
+              }
+            h->stats.rsvd_retries += again;
+            if (again && (rc = run_rsvd(h, nb, cps, h->path_h, rank, sk2, kRsvdRetryQ))) return rc;
+            h->stats.rsvd_updates -= again;    // counted once per bond,
+            h->stats.rsvd_fallbacks -= again;  // and a fallback only if the second sketch failed too
+          }
         }
       }
       for (int s = 0; s < nb; ++s) {

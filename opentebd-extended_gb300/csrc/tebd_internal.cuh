@@ -258,6 +258,7 @@ size_t bidiag_ws_doubles(int n, int chi);
 size_t bidiag_aux_elems(int n);
 constexpr int kBidiagMaxDim = 4096;  // larger compacted Theta take the QR + Jacobi route
 constexpr int kRsvdMaxSketch = 1536;  // widest sketch of the randomized route (chi + oversampling)
+constexpr int kRsvdRetryP = 128, kRsvdRetryQ = 3;  // the second sketch of a bond the judge sent back
 int jacobi_collect(tebd_handle *h);
 int measure_fp64_peak(int device, double *tflops);
 int run_nc_batch(tebd_handle *h, int nb, const int *links_host, double *truncerr_host);

@@ -132,6 +132,7 @@ class Stats(ctypes.Structure):
         ("rsvd_batches", ctypes.c_longlong),
         ("rsvd_oversample_sum", ctypes.c_longlong),
         ("rsvd_power_sum", ctypes.c_longlong),
+        ("rsvd_retries", ctypes.c_longlong),
     ]
 
     def as_dict(self):
