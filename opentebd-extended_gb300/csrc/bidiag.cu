@@ -1494,7 +1494,8 @@ __global__ void k_bd_store(Slot *slots, const int *path, int kk, int cap) {
 // the left reflectors from the double-float matrix the bidiagonalisation left in
 // S.X and the right ones from Pv converted in place (k_bd_pv_to_df); the vectors
 // Yu / Ru are double-float too and k_bd_store_df converts them.
-__global__ void __launch_bounds__(256) k_bd_apply_df(Slot *slots, const int *path, int kk, int cap) {
+__global__ void __launch_bounds__(256) k_bd_apply_df(Slot *slots, const int *path, int kk, int cap,
+                                                     int right_only) {
   const int s = blockIdx.y;
   const int route = path[s];
   if (!on_route(route)) return;
@@ -1503,7 +1504,7 @@ __global__ void __launch_bounds__(256) k_bd_apply_df(Slot *slots, const int *pat
   bd_dims(*S.cp, route, m, n);
   const int N = 2 * n, K = cap ? min(min(kk, n), S.cp->k) : min(kk, n);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int col = blockIdx.x * 8 + warp;
+  const int col = blockIdx.x * 8 + warp + (right_only ? K : 0);  // right only: columns K .. 2K-1
   if (col >= 2 * K) return;
   double *base = S.bdws + bd_scratch(n, kk);
   const double *Z = base + 5 * (size_t)N * K;
@@ -1555,7 +1556,7 @@ __global__ void k_bd_pv_to_df(Slot *slots, const int *path) {  // Pv in place, N
     F[e] = dfs(S.aux[e]);
 }
 
-__global__ void k_bd_store_df(Slot *slots, const int *path, int kk, int cap) {
+__global__ void k_bd_store_df(Slot *slots, const int *path, int kk, int cap, int right_only) {
   const int s = blockIdx.y;
   const int route = path[s];
   if (!on_route(route)) return;
@@ -1568,7 +1569,7 @@ __global__ void k_bd_store_df(Slot *slots, const int *path, int kk, int cap) {
   const float4 *Yu = reinterpret_cast<const float4 *>(base + 12 * (size_t)N * K);
   const float4 *U = route == kPathBidiagT ? reinterpret_cast<const float4 *>(base) : Yu;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)m * K; e += stride) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; !right_only && e < (size_t)m * K; e += stride) {
     const int i = (int)(e / m);
     const double2 y = dfd(U[e]);
     S.X[e] = make_double2(y.x * sig[i], y.y * sig[i]);
@@ -1771,7 +1772,7 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
       TEBD_LAUNCHED(h);
     }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(2 * kOrthCluster, nb, 1);
+    cfg.gridDim = dim3((b.right_only ? 1 : 2) * kOrthCluster, nb, 1);  // part 0 (right), then 1 (left)
     cfg.blockDim = dim3(kOrthThreads, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
@@ -1792,9 +1793,10 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
   }
   TEBD_LAUNCHED(h);
   if (b.dfp) {
-    k_bd_apply_df<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(slots_d, path_d, kk, cap);
+    k_bd_apply_df<<<dim3(cdiv((b.right_only ? 1 : 2) * (size_t)kk, 8), nb), 256, 0, st>>>(slots_d, path_d, kk, cap,
+                                                                                         b.right_only);
     TEBD_LAUNCHED(h);
-    k_bd_store_df<<<dim3(256, nb), 256, 0, st>>>(slots_d, path_d, kk, cap);
+    k_bd_store_df<<<dim3(256, nb), 256, 0, st>>>(slots_d, path_d, kk, cap, b.right_only);
     TEBD_LAUNCHED(h);
   } else {
     k_bd_apply<<<dim3(cdiv(2 * (size_t)kk, 8), nb), 256, 0, st>>>(slots_d, path_d, kk, cap);

@@ -547,6 +547,7 @@ static int rs_gram_svd(tebd_handle *h, RsState *R, const std::vector<int> &on, i
   b.nmax = s;
   b.kk = kk;
   b.dfp = true;  // double-float passes: the s x s Gram's eigenvectors need no more
+  b.right_only = 1;  // M = W Lambda W^H: only W is used
   b.phase = 0;
   b.cap = 0;
   return run_bidiag_batch(h, b);

@@ -245,6 +245,7 @@ struct BidiagBatch {
   bool dfp;
   int phase;  // 0: whole route; 1: through the singular values; 2: the vectors
   int cap;    // 1: vectors only for the first cp->k values of each problem (set between phases)
+  int right_only = 0;  // 1: right singular vectors only (double-float form; S.X keeps no left vectors)
 };
 int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b);
 // Autotuner table (tune.cu): the shape for route (0 FP64 bidiagonal, 1

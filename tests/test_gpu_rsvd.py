@@ -99,3 +99,36 @@ def test_rsvd_sweep_matches_plain_fp64(pkg):
         a = obs.two_site_rho(l0[k - 1], g0[k - 1], l0[k], g0[k], l0[k + 1])
         b = obs.two_site_rho(l1[k - 1], g1[k - 1], l1[k], g1[k], l1[k + 1])
         assert np.max(np.abs(a - b)) < 1e-8, k
+
+
+def test_rsvd_wide_sketch_chi1024(pkg):
+    """The learned-rank configuration's largest bonds: d = 3, chi = 1024 (Theta
+    3072 x 3072), a sketch of 1152 columns (p = 128, wider than 1024: the
+    Cholesky's recursive blocking and the widest product tiles), on a state
+    prepared by one double-float sweep; two-site density matrices (device
+    observables) and Lambdas against plain FP64 within 1e-8."""
+    H = pkg.hamiltonians
+    L, d, chi = 4, 3, 1024
+    gam, lam = _saturated(L, d, chi, 11, decay=128.0)
+    gate = H.matrix_exponential(H.bose_hubbard(L, d, 1.0, 2.0)[1], 0.005)
+    links = [1, 3]
+    with pkg.Chain(L, d, chi, svd_mode=pkg.SVD_DF) as c:
+        c.set_state(gam, lam)
+        c.apply_bonds(links, [gate] * len(links))
+        gam, lam = c.get_state()
+    res = {}
+    for mode in (pkg.SVD_FP64, pkg.SVD_RSVD):
+        with pkg.Chain(L, d, chi, svd_mode=mode) as c:
+            c.set_state(gam, lam)
+            if mode == pkg.SVD_RSVD:
+                c.set_theta_form(107)
+                c.set_rsvd(oversample=128, power_iters=2)
+            c.apply_bonds(links, [gate] * len(links))
+            res[mode] = ([c.two_site_rho(k) for k in links], c.get_state()[1], c.stats())
+    r0, l0, _ = res[pkg.SVD_FP64]
+    r1, l1, st = res[pkg.SVD_RSVD]
+    assert st["rsvd_updates"] == len(links) and st["rsvd_fallbacks"] == 0
+    for a, b in zip(r0, r1):
+        assert np.max(np.abs(a - b)) < 1e-8
+    for k in links:
+        assert np.max(np.abs(l0[k] - l1[k])) < 1e-8
