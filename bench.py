@@ -13,7 +13,9 @@ configuration) from the initial state, after W warm-up steps on a copy.
 value: updates/s with the chain resident in HBM: CUDA events on the library's
        stream around exactly the K steps (one more event per step gives the
        per-step costs: early steps are cheap, the chain saturates chi = 128 near
-       step 50 and the SVD dimension then stays near 600).
+       step 50 and the SVD dimension then stays near 600).  Before the timed
+       pass (untimed) the autotuner sets the launch shapes on the window's own
+       batches, replayed from the initial state (--no-tune-window skips it).
 e2e:   the same K steps end to end through the reference-facing C ABI: the chain
        is uploaded from pinned host buffers (tebd_set_gamma/lambda), every step
        passes its gates from host memory and returns the truncation error to the
@@ -399,6 +401,25 @@ def saturated_legs(pkg, device, args, fp64_peak, steps=3, Ls=L, chi=CHI, decay=1
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def window_autotune(pkg, chain, gam, lam, Udt, steps, every=4):
+    """Autotune (tebd_autotune) the odd and the even sweep of every `every`-th
+    Trotter step of the timed window, replayed from the initial state on the same
+    chain: the compacted Theta grows step by step, and each tuned batch fills the
+    table entries of its size; the chain is left at the replayed state and the
+    timed pass uploads the initial state again.  Returns the tuned batches'
+    default and tuned times."""
+    odd, even = list(range(1, L, 2)), list(range(2, L, 2))
+    chain.set_state(gam, lam)
+    out = []
+    for k in range(1, steps + 1):
+        if k % every == 0 or k == steps:
+            for links in (odd, even):
+                b_ms, t_ms = chain.autotune(links, [Udt[i - 1] for i in links])
+                out.append({"step": k, "bonds": len(links), "default_ms": b_ms, "tuned_ms": t_ms})
+        chain.trotter_step(Udt, ORDER)
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -432,6 +453,9 @@ def run_ours(args):
     # update's cost grows with the Schmidt rank as the state entangles)
     for _ in range(args.warmup):
         chain.trotter_step(Udt, ORDER)
+    tune_window = None
+    if not args.no_tune_window:  # untimed: tune the launch shapes on the window's own batches
+        tune_window = window_autotune(pkg, chain, gam, lam, Udt, args.steps)
 
     # host-side inputs of the end-to-end path: the initial chain in pinned memory
     # (Fortran order, as the reference holds it) and the gates
@@ -511,6 +535,8 @@ def run_ours(args):
         pc.set_state(gam, lam)
         for _ in range(args.warmup):
             pc.trotter_step(Udt, ORDER)
+        if not args.no_tune_window:  # the same untimed tuning as the plain run's
+            window_autotune(pkg, pc, gam, lam, Udt, args.steps)
         pc.set_state(gam, lam)
         pstream = torch.cuda.ExternalStream(pc.stream(), device=local)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -617,6 +643,7 @@ def run_ours(args):
                 "steps": args.steps, "path": "tebd_set_gamma/lambda + tebd_trotter_step (host gates) + "
                                               "tebd_get_gamma/lambda, host wall clock"},
         "gpu_launches": launches,
+        "window_autotune": tune_window,
         "roofline": roof,
         "roofline_hbm": hbm_roofline(roof["traffic"], roof["avg_launch_ms"],
                                      os.path.join(ROOT, "MEASURED_PEAKS.json")),
@@ -1031,6 +1058,8 @@ def main():
     ap.add_argument("--zgemm-form", type=int, default=107, help="--workload zgemm: 107, 3 or 1")
     ap.add_argument("--spin1-steps", type=int, default=3, help="--workload spin1: Trotter steps per leg")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune-window", action="store_true",
+                    help="skip autotuning the plain run's launch shapes on the window's batches before timing")
     ap.add_argument("--svd", default="fp64", choices=sorted(SVD_MODES))
     ap.add_argument("--save-obs", default=None, help="write final <n_i>, bond energies, Lambdas (npz)")
     ap.add_argument("--no-precision", action="store_true", help="skip the precision, mixed and saturated legs")
