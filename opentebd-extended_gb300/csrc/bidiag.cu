@@ -1685,7 +1685,9 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
     // goes as waves / C; clusters must fit in one GPC, so the co-resident count
     // (occupancy query) decides how many waves a size needs.  Ties keep the
     // smaller size (fewer barriers' worth of idle SMs in a partial wave).
-    const int cmax = std::max(1, std::min(8, (nmax + 127) / 128));
+    // sizes up to 8, at least 4 (the autotuner measured 4 CTAs fastest for
+    // 64..320-column batches of 32 bonds, where ceil(n / 128) had allowed 1..3)
+    const int cmax = std::min(8, std::max(4, (nmax + 127) / 128));
     int nbd = 0;  // bonds on this route (the others' clusters exit at once)
     for (int s = 0; s < nb; ++s) nbd += b.path_h[s] != kPathQRJ;
     const TuneParams tp = tune_lookup(h, dfp ? 1 : 0, nmax, nbd);
