@@ -331,7 +331,8 @@ int tebd_measure_fp64_peak(int device, double *tflops);
  * `links` (at most one batch: the first nslots bonds, none sharing a site) with
  * their gates, as tebd_apply_bonds would update them: the default choice, each
  * cluster size 1..8 of the bidiagonalisation, each bisection team of 1, 2, 4, 8
- * lanes with the best cluster, and, when the randomized route runs, each
+ * lanes with the best cluster, each cluster of 1, 2, 4, 8 CTAs per side of the
+ * singular vectors' re-orthogonalisation, and, when the randomized route runs, each
  * cluster of 1, 2, 4, 8 CTAs per bond, each panel of 4, 8, 16 rows and each leaf
  * size 128, 192, 256, 384, 768 of its recursively blocked Cholesky.  The fastest (by more than 1 %) is kept in
  * a table per device under (route, largest compacted dimension rounded up to
@@ -342,12 +343,12 @@ int tebd_measure_fp64_peak(int device, double *tflops);
  * batch's time with the default and with the chosen shape. */
 int tebd_autotune(tebd_handle *h, int nbonds, const int *links, const double *const *gates, double *base_ms,
                   double *best_ms);
-/* The device's table: up to max_entries rows of 9 ints (route: 0 FP64
+/* The device's table: up to max_entries rows of 10 ints (route: 0 FP64
  * bidiagonal, 1 double-float bidiagonal, 2 randomized-route Cholesky leaf, 3 its
  * blocking; dimension bucket; bonds bucket; bidiagonalisation cluster size;
  * bisection team size; Cholesky cluster size; Cholesky panel height; Cholesky
- * leaf size -- 0 = the default; batch time in microseconds); *count = rows in
- * the table. */
+ * leaf size; re-orthogonalisation cluster size -- 0 = the default; batch time in
+ * microseconds); *count = rows in the table. */
 int tebd_get_tuning(int device, int *entries, int max_entries, int *count);
 /* Empty the device's table (the defaults apply again). */
 int tebd_clear_tuning(int device);

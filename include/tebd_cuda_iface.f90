@@ -219,7 +219,7 @@ INTERFACE
   INTEGER(C_INT) FUNCTION tebd_get_tuning(device, entries, max_entries, count) BIND(C, NAME='tebd_get_tuning')
     IMPORT :: C_INT
     INTEGER(C_INT), VALUE :: device, max_entries
-    INTEGER(C_INT) :: entries(9, *)
+    INTEGER(C_INT) :: entries(10, *)
     INTEGER(C_INT) :: count
   END FUNCTION
   INTEGER(C_INT) FUNCTION tebd_clear_tuning(device) BIND(C, NAME='tebd_clear_tuning')

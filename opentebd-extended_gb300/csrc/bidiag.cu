@@ -1774,17 +1774,31 @@ int run_bidiag_batch(tebd_handle *h, const BidiagBatch &b) {
       TEBD_LAUNCHED(h);
     }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((b.right_only ? 1 : 2) * kOrthCluster, nb, 1);  // part 0 (right), then 1 (left)
     cfg.blockDim = dim3(kOrthThreads, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kOrthCluster;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    int oc = kOrthCluster;  // or the autotuner's size, when the launch can co-schedule it
+    const TuneParams tpo = tune_lookup(h, b.dfp ? 1 : 0, nmax, nb);
+    if (tpo.orth_cluster > 0) {
+      cfg.gridDim = dim3((b.right_only ? 1 : 2) * tpo.orth_cluster, nb, 1);
+      attr[0].val.clusterDim.x = tpo.orth_cluster;
+      int ncl = 0;
+      if (tpo.orth_cluster <= 8 &&
+          cudaOccupancyMaxActiveClusters(&ncl, (const void *)okern, &cfg) == cudaSuccess && ncl >= 1) {
+        oc = tpo.orth_cluster;
+      } else {
+        cudaGetLastError();
+        tune_reject(h);
+      }
+    }
+    cfg.gridDim = dim3((b.right_only ? 1 : 2) * oc, nb, 1);  // part 0 (right), then 1 (left)
+    attr[0].val.clusterDim.x = oc;
     if ((rc = check_cuda(h, cudaLaunchKernelEx(&cfg, okern, slots_d, path_d, kk, cap),
                          "orthogonalisation launch")))
       return rc;

@@ -133,6 +133,7 @@ struct TuneParams {
   int panel;         // rows of R per panel of the randomized route's Cholesky
   int chol_cluster;  // CTAs per bond of that Cholesky
   int chol_leaf;     // largest diagonal block the recursive Cholesky factors directly
+  int orth_cluster;  // CTAs per (bond, side) of the singular vectors' re-orthogonalisation
 };
 
 }  // namespace tebd
@@ -212,7 +213,7 @@ struct tebd_handle {
   // whether a launch could not use the forced shape
   struct {
     int active = 0, rejected = 0;
-    tebd::TuneParams force{0, 0, 0, 0, 0};
+    tebd::TuneParams force{0, 0, 0, 0, 0, 0};
     std::vector<std::array<int, 3>> seen;
   } tune;
 };

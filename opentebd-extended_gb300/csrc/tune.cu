@@ -6,7 +6,9 @@
 //     cluster of 1..8 CTAs per bond; more CTAs share each column's passes but
 //     fewer bonds run at once);
 //   * the team size of the bisection (k_bd_sigma<team>: 1, 2, 4 or 8 lanes
-//     evaluate Sturm counts at that many points per step for one value);
+//     evaluate Sturm counts at that many points per step for one value) and the
+//     CTAs that share one side of a bond's vector re-orthogonalisation
+//     (k_bd_orth, a cluster of 1, 2, 4 or 8);
 //   * the panel height of the randomized route's Cholesky (k_rs_chol: 4, 8 or 16
 //     rows of R staged in shared memory per panel), the CTAs that share one
 //     bond's Cholesky (a cluster of 1..8), and the size below which its
@@ -60,7 +62,7 @@ TuneParams tune_lookup(tebd_handle *h, int route, int n, int nb) {
   }
   std::lock_guard<std::mutex> lock(g_mu);
   const auto it = g_table.find({h->device, key[0], key[1], key[2]});
-  if (it == g_table.end()) return TuneParams{0, 0, 0, 0, 0};
+  if (it == g_table.end()) return TuneParams{0, 0, 0, 0, 0, 0};
   return it->second.p;
 }
 
@@ -151,7 +153,7 @@ extern "C" int tebd_autotune(tebd_handle *h, int nbonds, const int *links, const
     return r ? r : r2;
   };
   float base = 0.f, best = 0.f;
-  TuneParams win{0, 0, 0, 0, 0};
+  TuneParams win{0, 0, 0, 0, 0, 0};
   if (!rc) rc = trial(win, &base);  // warm-up of workspaces and kernels
   if (!rc) rc = trial(win, &base);
   best = base;
@@ -161,8 +163,12 @@ extern "C" int tebd_autotune(tebd_handle *h, int nbonds, const int *links, const
   auto sweep = [&](int which, const std::vector<int> &vals) -> int {
     for (int v : vals) {
       TuneParams f = win;
-      (which == 0 ? f.cluster : which == 1 ? f.team : which == 2 ? f.chol_cluster : which == 3 ? f.panel
-                                                                                    : f.chol_leaf) = v;
+      (which == 0   ? f.cluster
+       : which == 1 ? f.team
+       : which == 2 ? f.chol_cluster
+       : which == 3 ? f.panel
+       : which == 4 ? f.chol_leaf
+                    : f.orth_cluster) = v;
       float ms = 0.f;
       const int r = trial(f, &ms);
       if (r) return r;
@@ -176,6 +182,7 @@ extern "C" int tebd_autotune(tebd_handle *h, int nbonds, const int *links, const
   };
   if (!rc) rc = sweep(0, {1, 2, 3, 4, 5, 6, 7, 8});
   if (!rc) rc = sweep(1, {1, 2, 4, 8});
+  if (!rc) rc = sweep(5, {1, 2, 4, 8});
   if (!rc && any_rsvd) rc = sweep(2, {1, 2, 4, 8});
   if (!rc && any_rsvd) rc = sweep(3, {4, 8, 16});
   if (!rc && any_rsvd) rc = sweep(4, {128, 192, 256, 384, 768});
@@ -201,7 +208,7 @@ extern "C" int tebd_get_tuning(int device, int *entries, int max_entries, int *c
   for (const auto &kv : g_table) {
     if (kv.first[0] != device) continue;
     if (w < max_entries) {
-      int *o = entries + 9 * w++;
+      int *o = entries + 10 * w++;
       o[0] = kv.first[1];
       o[1] = kv.first[2];
       o[2] = kv.first[3];
@@ -210,7 +217,8 @@ extern "C" int tebd_get_tuning(int device, int *entries, int max_entries, int *c
       o[5] = kv.second.p.chol_cluster;
       o[6] = kv.second.p.panel;
       o[7] = kv.second.p.chol_leaf;
-      o[8] = (int)kv.second.us;
+      o[8] = kv.second.p.orth_cluster;
+      o[9] = (int)kv.second.us;
     }
     ++n;
   }

@@ -597,12 +597,13 @@ def get_tuning(device=0):
     if rc != TEBD_OK:
         raise TebdError(rc, "tebd_get_tuning failed")
     n = int(cnt[0])
-    buf = np.zeros(9 * max(n, 1), dtype=np.int32)
+    buf = np.zeros(10 * max(n, 1), dtype=np.int32)
     rc = lib.tebd_get_tuning(device, _ip(buf), n, _ip(cnt))
     if rc != TEBD_OK:
         raise TebdError(rc, "tebd_get_tuning failed")
-    keys = ("route", "n_bucket", "bonds_bucket", "cluster", "team", "chol_cluster", "panel", "chol_leaf", "batch_us")
-    rows = [dict(zip(keys, (int(v) for v in buf[9 * i:9 * i + 9]))) for i in range(n)]
+    keys = ("route", "n_bucket", "bonds_bucket", "cluster", "team", "chol_cluster", "panel", "chol_leaf",
+            "orth_cluster", "batch_us")
+    rows = [dict(zip(keys, (int(v) for v in buf[10 * i:10 * i + 10]))) for i in range(n)]
     for r in rows:
         r["route"] = TUNE_ROUTES.get(r["route"], r["route"])
     return rows

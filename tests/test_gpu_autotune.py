@@ -52,6 +52,7 @@ def test_autotune_keeps_state_and_results(pkg, oracle, mode):
                 assert r["cluster"] in (0, 1, 2, 3, 4, 5, 6, 7, 8) and r["team"] in (0, 1, 2, 4, 8)
                 assert r["panel"] in (0, 4, 8, 16) and r["chol_cluster"] in (0, 1, 2, 4, 8)
                 assert r["chol_leaf"] in (0, 128, 192, 256, 384, 768)
+                assert r["orth_cluster"] in (0, 1, 2, 4, 8)
                 assert r["batch_us"] > 0
             c.apply_bonds(links, [gate] * len(links))  # tuned shapes
             gt, lt = c.get_state()
