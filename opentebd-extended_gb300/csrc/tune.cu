@@ -16,8 +16,9 @@
 // Without a table the library picks them from occupancy queries and thread
 // counts (bidiag.cu, rsvd.cu).  tebd_autotune times candidates on a batch of
 // real bonds -- the default choice, then every cluster size, then every team
-// size with the best cluster, then every Cholesky cluster size, panel height
-// and leaf size -- restoring the touched
+// size with the best cluster, then every re-orthogonalisation cluster size, then
+// (randomized route only) every Cholesky cluster size, panel height and leaf
+// size -- restoring the touched
 // Gammas, Lambdas and labels after each trial, and keeps the fastest per
 // (route, largest compacted dimension rounded up to 64, bonds in the batch
 // rounded up to a power of two) in a table per device that every later batch on
