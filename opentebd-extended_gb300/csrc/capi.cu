@@ -627,6 +627,9 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
      "read truncerr");
   CK(cudaMemcpyAsync(f_pin + 4, h->status_d, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->stream),
      "read status");
+  f_pin[8] = 0;
+  if (h->tc_err)  // a tensor-core product of the batch whose pipeline wait expired
+    CK(cudaMemcpyAsync(f_pin + 8, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read tensor-core flag");
   if (h->profiling) cudaEventRecord(h->ev[3], h->stream);
   CK(cudaStreamSynchronize(h->stream), "bond batch");
   for (int s = 0; s < nb; ++s) truncerr[s] = t_pin[s];
@@ -637,6 +640,10 @@ static int run_batch(tebd_handle *h, int nb, const int *links, const double *con
   }
   h->stats.updates += nb;
   if ((rc = jacobi_collect(h))) return rc;
+  if (f_pin[8]) {
+    cudaMemsetAsync(h->tc_err, 0, sizeof(int), h->stream);
+    return set_error(h, TEBD_ERR_CUDA, "a tensor-core pipeline wait timed out");
+  }
   if (f_pin[4] & 1) return set_error(h, TEBD_ERR_NONFINITE, "non-finite value in Theta or sigma");
   if (f_pin[5]) return set_error(h, TEBD_ERR_NC_BLOCKS, "charge label outside the block range");
   return TEBD_OK;

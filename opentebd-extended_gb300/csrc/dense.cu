@@ -557,7 +557,7 @@ int launch_dense_prepare(tebd_handle *h, int nb, bool /*real_gate: converted on 
   k_compact<<<nb, 96, 0, st>>>(h->lam, h->links_d, h->slots_d, jp, chi, d);
   TEBD_LAUNCHED(h);
   int tc = -1;  // tensor-core Theta (theta_tc.cu); -1: formed on the CUDA cores below
-  if (h->theta_form != 0 && (tc = launch_theta_tc(h, nb)) > 0) return tc;
+  if (h->theta_form != 0 && h->mode == TEBD_MODE_DENSE && (tc = launch_theta_tc(h, nb)) > 0) return tc;
   if (tc == 0) {
   } else if (h->opts.svd_mode == TEBD_SVD_DF || h->opts.svd_mode == TEBD_SVD_RSVD)
     k_theta_form_df<<<dim3(cdiv(n, TT_M), cdiv(n, TT_N), nb), 256, 0, st>>>(h->gam, h->lam, h->links_d,

@@ -36,12 +36,17 @@
 // 10000 is written for unused indices, and `10.0**(-10)` (single precision)
 // decides kept singular values and the Lambda divisions.
 #include <math.h>
+#include <stddef.h>
 #include <string.h>
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <vector>
 
 #include "df.cuh"
+#include "oz_digits.cuh"
+#include "tc_gemm.cuh"
 #include "tebd_internal.cuh"
 
 namespace tebd {
@@ -72,6 +77,20 @@ struct NcLocal {
   int n[8];
 };
 
+// Tensor-core Theta: block k of a bond as stored in X (m >= n: the block itself,
+// else its conjugate transpose), and the class size K of its betas
+struct NcSize {
+  int m, n, K, trans, boffx;
+};
+// one product of a grouped launch: X = the block's storage, (m, n) as stored,
+// q = minNL + k the block's (and its betas' class) left number
+struct NcProd {
+  double2 *X;
+  int m, n, K, s, k, trans, q, pad;
+};
+static_assert(sizeof(NcProd) == 40 && offsetof(NcProd, m) == 8 && offsetof(NcProd, n) == 12,
+              "NcProd: per-problem sizes at a stride of 10 ints");
+
 struct NcWorkspace {
   int bmax;
   std::vector<NcSlot> slots;
@@ -88,6 +107,7 @@ struct NcWorkspace {
   std::vector<int> bpath_h;
   std::vector<int> blk2bs_h;  // (bond, block) -> bidiagonal block index, -1 for Jacobi
   int *blk2bs_d = nullptr;
+  NcSize *sizes_d = nullptr;  // nslots * bmax block sizes (tensor-core Theta)
 };
 
 
@@ -424,6 +444,220 @@ __global__ void __launch_bounds__(256) k_nc_theta(const double2 *__restrict__ ga
   if (threadIdx.x == 0) S.part[blockIdx.x] = red[0];
 }
 
+// ---------------------------------------------------------------------------
+// Theta on the tensor cores (theta form 103..107 on an NC handle).
+//
+// The class sums of FormThetaNC are, block by block, one dense product: for
+// block k (left number q = minNL + k, rows (alpha, i) with LabelLeft(link) +
+// n_i = q, columns (gamma, j) with LabelRight(link+2) + n_j = totNum - q)
+//   P_k(r, c) = sum_beta A(alpha_r, i_r, beta) B(beta, j_c, gamma_c),
+// beta over the class q betas with LabelRight(link+1) = totNum - q (the betas
+// whose labels FormThetaNC's filter accepts for every entry of the block),
+// A = l0 G1 l1, B = G2 l2.  Every allowed entry with a nonzero sum lies in a
+// block (the block range is clipped to where rows and columns can meet), and
+// every block entry is allowed, so the products written straight into the
+// blocks' storage in X (conjugate-transposed blocks as P^H = B^H A^H) hold the
+// whole pre-gate Theta.  k_nc_mix then applies ThetaOperationNC in place and
+// sums RenormThetaNC's partials.  The products of all (bond, block) pairs run as
+// grouped digit-plane products (tc_ozaki.cu), one launch per size bucket.
+// ---------------------------------------------------------------------------
+__global__ void k_nc_sizes(const NcSlot *nc, int totNum, int bmax, NcSize *out) {
+  const int s = blockIdx.x;
+  const NcSlot S = nc[s];
+  const int nb = S.hdr[H_ERR] ? 0 : S.hdr[H_NB];
+  const int mnl = S.hdr[H_MINNL];
+  for (int k = threadIdx.x; k < bmax; k += blockDim.x) {
+    NcSize z = {0, 0, 0, 0, 0};
+    if (k < nb) {
+      const int m = S.rows[k], n = S.cols[k], q = mnl + k;
+      z.m = max(m, n);
+      z.n = min(m, n);
+      z.trans = m < n;
+      z.K = (q >= 0 && q <= totNum) ? S.cls_off[q + 1] - S.cls_off[q] : 0;
+      z.boffx = S.boffx[k];
+    }
+    out[(size_t)s * bmax + k] = z;
+  }
+}
+
+// Digit planes of the grouped products' operands, one warp per line.  A line of
+// the stored product's left factor (kB = false: its rows) or right factor (kB =
+// true: its columns) is a row (alpha, i) of Theta or a column (gamma, j): rows
+// when not transposed on the left and transposed on the right.  Its values over
+// the class's betas (K, the class list order) are A(alpha, i, beta) and
+// B(beta, j, gamma), conjugated for transposed blocks, zero for the betas that
+// the label filter drops.
+template <bool kB>
+__global__ void __launch_bounds__(256) k_nc_oz_pack(const double2 *__restrict__ gam, const double *__restrict__ lam,
+                                                    const int *__restrict__ lab_r, const int *links,
+                                                    const NcSlot *nc, const NcProd *tab, int chi, int d,
+                                                    int totNum, int nprob, int rows_pad, int k_pad, int S,
+                                                    unsigned short *dig, int *exps) {
+  const int p = blockIdx.y;
+  const int lines = kB ? rows_pad / 2 : rows_pad;
+  const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (r >= lines) return;
+  const NcProd P = tab[p];
+  const NcSlot &Sl = nc[P.s];
+  const int link = links[P.s];
+  const bool live = r < (kB ? P.n : P.m);
+  const bool theta_row = kB == (P.trans != 0);
+  int x = 0, y = 0;  // (alpha, i) or (gamma, j)
+  if (live) {
+    if (theta_row) {
+      const int e = Sl.roff[P.k] + r;
+      x = Sl.l_alpha[e];
+      y = Sl.l_i[e];
+    } else {
+      const int e = Sl.coff[P.k] + r;
+      x = Sl.r_gamma[e];
+      y = Sl.r_j[e];
+    }
+  }
+  const size_t csz = (size_t)chi * d * chi;
+  const double2 *G1 = gam + (size_t)(link - 1) * csz;
+  const double2 *G2 = gam + (size_t)link * csz;
+  const double *l0 = lam + (size_t)(link - 1) * chi;
+  const double *l1 = lam + (size_t)link * chi;
+  const double *l2 = lam + (size_t)(link + 1) * chi;
+  const int *lr1 = lab_r + (size_t)link * chi;  // LabelRight(link+1)
+  const int *beta = Sl.cls_beta + (P.K > 0 ? Sl.cls_off[P.q] : 0);
+  const int want = totNum - P.q;
+  const bool cj = P.trans != 0;
+  oz_pack_line<kB>(
+      [&](int l) {
+        const int b = beta[l];
+        const int rb = lr1[b];
+        double2 v = make_double2(0.0, 0.0);
+        if (rb < 1000 && rb == want) {
+          if (theta_row) {
+            const double w = l0[x] * l1[b];
+            const double2 g = G1[x + (size_t)chi * y + (size_t)chi * d * b];
+            v = make_double2(w * g.x, w * g.y);
+          } else {
+            const double w = l2[x];
+            const double2 g = G2[b + (size_t)chi * y + (size_t)chi * d * x];
+            v = make_double2(w * g.x, w * g.y);
+          }
+          if (cj) v.y = -v.y;
+        }
+        return v;
+      },
+      live, P.K, p, r, nprob, rows_pad, k_pad, S, dig, exps);
+}
+
+// ThetaOperationNC + RenormThetaNC partials on the pre-gate Theta held in the
+// blocks (the tensor-core form): one thread per (alpha, gamma) reads its <= d
+// allowed entries (or its intDegFree pairs), mixes them with the gate and writes
+// them back to the same places; the entries of different (alpha, gamma) are
+// disjoint.  Same chunking and loop order as k_nc_theta.
+template <bool kIdf>
+__global__ void __launch_bounds__(256) k_nc_mix(const int *__restrict__ lab_l, const int *__restrict__ lab_r,
+                                                const int *links, Slot *slots, NcSlot *nc, int chi, int d,
+                                                int totNum, int maxFilling, NcLocal nl) {
+  const int s = blockIdx.y;
+  const NcSlot S = nc[s];
+  __shared__ double red[256];
+  const int nb = S.hdr[H_NB];
+  const int link = links[s];
+  const int *ll0 = lab_l + (size_t)(link - 1) * chi;
+  const int *lr2 = lab_r + (size_t)(link + 1) * chi;
+  const double2 *op = slots[s].gate;
+  double2 *X = slots[s].X;
+  const int d2 = d * d;
+  const int mnl = S.hdr[H_MINNL];
+  // storage of the allowed entry (alpha, i; j, gamma) in its block, or null
+  auto at = [&](int a, int i, int j, int g, bool *cj) -> double2 * {
+    const int rp = S.rowpos[a * d + i], cp = S.colpos[g * d + j];
+    if (nb == 0 || rp < 0 || cp < 0) return nullptr;
+    const int blk = ll0[a] + nl.n[i] - mnl;
+    const int m = S.rows[blk], n = S.cols[blk];
+    *cj = m < n;
+    return X + S.boffx[blk] + (m >= n ? rp + (size_t)m * cp : cp + (size_t)n * rp);
+  };
+  auto get = [&](int a, int i, int j, int g) -> double2 {
+    bool cj = false;
+    const double2 *e = at(a, i, j, g, &cj);
+    if (!e) return make_double2(0.0, 0.0);
+    const double2 v = *e;
+    return cj ? make_double2(v.x, -v.y) : v;
+  };
+  auto put = [&](int a, int i, int j, int g, double2 v) {
+    bool cj = false;
+    double2 *e = at(a, i, j, g, &cj);
+    if (e) *e = cj ? make_double2(v.x, -v.y) : v;
+  };
+  const size_t total = (size_t)chi * chi;
+  const size_t chunk = (total + kNormParts - 1) / kNormParts;
+  const size_t beg = blockIdx.x * chunk, end = min(beg + chunk, total);
+  double acc = 0.0;
+  for (size_t t = beg + threadIdx.x; t < end; t += blockDim.x) {
+    const int a = (int)(t % chi), g = (int)(t / chi);
+    const int lftN = ll0[a], rgtN = lr2[g];
+    if (max(lftN, rgtN) >= 1000) continue;
+    const int ntot = totNum - lftN - rgtN;
+    if constexpr (kIdf) {
+      double2 th[kMaxPairs];
+      int pi[kMaxPairs], pl[kMaxPairs];
+      int np = 0;
+      for (int i = 0; i < d; ++i) {
+        const int r = ntot - nl.n[i];
+        if (r < 0 || r > maxFilling) continue;
+        for (int l = 0; l < d && np < kMaxPairs; ++l) {
+          if (nl.n[l] != r) continue;
+          const int q = lftN + nl.n[i];
+          th[np] = (nl.n[i] <= maxFilling && q >= 0 && q <= totNum) ? get(a, i, l, g) : make_double2(0.0, 0.0);
+          pi[np] = i;
+          pl[np] = l;
+          ++np;
+        }
+      }
+      for (int o = 0; o < np; ++o) {
+        const int k = pi[o], jj = pl[o];
+        double2 v = make_double2(0.0, 0.0);
+        for (int p = 0; p < np; ++p) {
+          const double2 gv = op[(size_t)(k * d + jj) + (size_t)d2 * (pi[p] * d + pl[p])];
+          v.x += gv.x * th[p].x - gv.y * th[p].y;
+          v.y += gv.x * th[p].y + gv.y * th[p].x;
+        }
+        acc += v.x * v.x + v.y * v.y;
+        put(a, k, jj, g, v);
+      }
+    } else {
+      double2 th[kMaxDnc];
+      for (int i = 0; i < d; ++i) {
+        th[i] = make_double2(0.0, 0.0);
+        const int li = ntot - i;
+        if (li < 0 || li > maxFilling) continue;
+        const int q = lftN + i;
+        if (q < 0 || q > totNum) continue;
+        th[i] = get(a, i, li, g);
+      }
+      for (int k = 0; k < d; ++k) {
+        const int jj = ntot - k;
+        if (jj < 0 || jj > maxFilling) continue;
+        double2 o = make_double2(0.0, 0.0);
+        for (int i = 0; i < d; ++i) {
+          const int li = ntot - i;
+          if (li < 0 || li > maxFilling) continue;
+          const double2 gv = op[(size_t)(k * d + jj) + (size_t)d2 * (i * d + li)];
+          o.x += gv.x * th[i].x - gv.y * th[i].y;
+          o.y += gv.x * th[i].y + gv.y * th[i].x;
+        }
+        acc += o.x * o.x + o.y * o.y;
+        put(a, k, jj, g, o);
+      }
+    }
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) S.part[blockIdx.x] = red[0];
+}
+
 // V = identity for every block problem; norm from the fixed-order partials
 // unnormalized = 1 for SwappingNC, which skips RenormThetaNC: the block singular
 // values are taken as they are (norm 1 in the flattening).
@@ -742,8 +976,8 @@ int nc_alloc(tebd_handle *h) {
   if (!w) return TEBD_ERR_OOM;
   w->bmax = bmax;
   char *base = nullptr;
-  const size_t bytes = per * ns + al(sizeof(NcSlot) * ns) + al(sizeof(JacobiProblem<double>) * ns * bmax) +
-                       sizeof(JacobiProblem<double>) * ns * bmax;
+  const size_t bytes = per * ns + al(sizeof(NcSlot) * ns) + 2 * al(sizeof(JacobiProblem<double>) * ns * bmax) +
+                       sizeof(NcSize) * ns * bmax;
   int rc = check_cuda(h, cudaMalloc((void **)&base, bytes), "alloc NC workspace");
   if (rc) {
     delete w;
@@ -786,6 +1020,8 @@ int nc_alloc(tebd_handle *h) {
   w->probs_d = (JacobiProblem<double> *)p;
   p += al(sizeof(JacobiProblem<double>) * ns * bmax);
   w->small_d = (JacobiProblem<double> *)p;
+  p += al(sizeof(JacobiProblem<double>) * ns * bmax);
+  w->sizes_d = (NcSize *)p;
   h->nc_ws = base;
   rc = check_cuda(h, cudaMemcpy(w->slots_d, w->slots.data(), sizeof(NcSlot) * ns,
                                 cudaMemcpyHostToDevice), "upload NC slot table");
@@ -928,6 +1164,144 @@ int nc_route_blocks(tebd_handle *h, NcWorkspace *w, int nb, int *nbd, int *small
   return TEBD_OK;
 }
 
+// The batch's Theta on the tensor cores (k_nc_sizes .. k_nc_mix above).  The
+// bonds' headers are read into hdr first, since the products are sized from
+// them; a bond whose labels fall outside its block range fails the batch here
+// (TEBD_ERR_NC_BLOCKS), before anything is written.  Products are grouped in
+// size buckets (stored rows up to 128 x 2^a, columns up to 64 x 2^b, class sizes
+// up to 16 x 2^c), one grouped launch per bucket, padded to the bucket's largest
+// problem; a launch skips the tiles outside each problem's own rows and columns.
+int nc_theta_tc(tebd_handle *h, NcWorkspace *w, int nb, int N, int mf, const NcLocal &nl, std::vector<int> &hdr) {
+  cudaStream_t st = h->stream;
+  const int bmax = w->bmax, chi = h->chi, d = h->d, S = h->theta_form - 100;
+  k_nc_sizes<<<nb, 128, 0, st>>>(w->slots_d, N, bmax, w->sizes_d);
+  TEBD_LAUNCHED(h);
+  std::vector<NcSize> sz((size_t)nb * bmax);
+  hdr.assign((size_t)nb * H_COUNT, 0);
+  int rc = check_cuda(h, cudaMemcpyAsync(sz.data(), w->sizes_d, sizeof(NcSize) * sz.size(), cudaMemcpyDeviceToHost,
+                                         st),
+                      "read NC block sizes");
+  for (int s = 0; s < nb && !rc; ++s)
+    rc = check_cuda(h, cudaMemcpyAsync(hdr.data() + (size_t)s * H_COUNT, w->slots[s].hdr, sizeof(int) * H_COUNT,
+                                       cudaMemcpyDeviceToHost, st),
+                    "read NC header");
+  if (!rc) rc = check_cuda(h, cudaStreamSynchronize(st), "NC block sizes");
+  if (rc) return rc;
+  for (int s = 0; s < nb; ++s)
+    if (hdr[(size_t)s * H_COUNT + H_ERR])
+      return set_error(h, TEBD_ERR_NC_BLOCKS, "charge label outside the block range");
+  auto level = [](int x, int unit) {
+    int l = 0;
+    while ((unit << l) < x) ++l;
+    return l;
+  };
+  std::map<std::array<int, 3>, std::vector<NcProd>> buckets;
+  for (int s = 0; s < nb; ++s)
+    for (int k = 0; k < bmax; ++k) {
+      const NcSize &z = sz[(size_t)s * bmax + k];
+      if (z.m <= 0 || z.n <= 0) continue;
+      NcProd P;
+      P.X = h->slots[s].X + z.boffx;
+      P.m = z.m;
+      P.n = z.n;
+      P.K = z.K;
+      P.s = s;
+      P.k = k;
+      P.trans = z.trans;
+      P.q = hdr[(size_t)s * H_COUNT + H_MINNL] + k;
+      P.pad = 0;
+      buckets[{level(z.m, kTcBM), level(z.n, kOzBN / 2), level(std::max(z.K, 1), 16)}].push_back(P);
+    }
+  struct Launch {
+    int off, np, m, n, m_pad, n_pad, k_pad;
+    double flops;
+  };
+  constexpr int kMaxProblems = 65535;  // the product's grid z and the packers' grid y
+  const double pairs = S * (S + 1) / 2.0;
+  std::vector<Launch> launches;
+  std::vector<NcProd> tab;
+  size_t da = 0, db = 0, ea = 0, eb = 0;
+  for (const auto &kv : buckets) {
+    const std::vector<NcProd> &v = kv.second;
+    for (size_t c0 = 0; c0 < v.size(); c0 += kMaxProblems) {
+      Launch L = {(int)tab.size(), (int)std::min(v.size() - c0, (size_t)kMaxProblems), 0, 0, 0, 0, 0, 0.0};
+      int K = 1;
+      for (int i = 0; i < L.np; ++i) {
+        L.m = std::max(L.m, v[c0 + i].m);
+        L.n = std::max(L.n, v[c0 + i].n);
+        K = std::max(K, v[c0 + i].K);
+      }
+      L.m_pad = tc_pad(L.m, kTcBM);
+      L.n_pad = tc_pad(2 * L.n, kOzBN);
+      L.k_pad = tc_pad(2 * K, kOzBK);
+      for (int i = 0; i < L.np; ++i)  // the tiles the launch runs
+        L.flops += pairs * 2.0 * tc_pad(v[c0 + i].m, kTcBM) * (double)tc_pad(2 * v[c0 + i].n, kOzBN) * L.k_pad;
+      da = std::max(da, (size_t)S * L.np * L.m_pad * L.k_pad);
+      db = std::max(db, (size_t)S * L.np * L.n_pad * L.k_pad);
+      ea = std::max(ea, (size_t)L.np * L.m_pad);
+      eb = std::max(eb, (size_t)L.np * (L.n_pad / 2));
+      tab.insert(tab.end(), v.begin() + c0, v.begin() + c0 + L.np);
+      launches.push_back(L);
+    }
+  }
+  if (!launches.empty()) {
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t tb = al(sizeof(NcProd) * tab.size()), ab = al(sizeof(unsigned short) * da),
+                 bb = al(sizeof(unsigned short) * db), eab = al(sizeof(int) * ea);
+    if ((rc = tc_reserve(h, tb + ab + bb + eab + al(sizeof(int) * eb)))) return rc;
+    char *p = static_cast<char *>(h->tc_ws);
+    NcProd *tab_d = reinterpret_cast<NcProd *>(p);
+    auto *dA = reinterpret_cast<unsigned short *>(p + tb);
+    auto *dB = reinterpret_cast<unsigned short *>(p + tb + ab);
+    int *eA = reinterpret_cast<int *>(p + tb + ab + bb);
+    int *eB = reinterpret_cast<int *>(p + tb + ab + bb + eab);
+    if ((rc = check_cuda(h, cudaMemcpyAsync(tab_d, tab.data(), sizeof(NcProd) * tab.size(), cudaMemcpyHostToDevice, st),
+                         "upload NC products")))
+      return rc;
+    for (const Launch &L : launches) {
+      const NcProd *t = tab_d + L.off;
+      k_nc_oz_pack<false><<<dim3(L.m_pad / 8, L.np), 256, 0, st>>>(h->gam, h->lam, h->lab_r, h->links_d, w->slots_d,
+                                                                   t, chi, d, N, L.np, L.m_pad, L.k_pad, S, dA, eA);
+      TEBD_LAUNCHED(h);
+      k_nc_oz_pack<true><<<dim3(L.n_pad / 16, L.np), 256, 0, st>>>(h->gam, h->lam, h->lab_r, h->links_d, w->slots_d,
+                                                                   t, chi, d, N, L.np, L.n_pad, L.k_pad, S, dB, eB);
+      TEBD_LAUNCHED(h);
+      const unsigned char *tp = reinterpret_cast<const unsigned char *>(t);
+      OzBatch b = {};
+      b.a_dig = dA;
+      b.b_dig = dB;
+      b.a_exp = eA;
+      b.b_exp = eB;
+      b.nprob = L.np;
+      b.m_pad = L.m_pad;
+      b.n_pad = L.n_pad;
+      b.k_pad = L.k_pad;
+      b.slices = S;
+      b.rs = 1;
+      b.cs = 0;  // column stride = the problem's own stored rows
+      b.m_d = reinterpret_cast<const int *>(tp + offsetof(NcProd, m));
+      b.n_d = reinterpret_cast<const int *>(tp + offsetof(NcProd, n));
+      b.dim_stride = (int)(sizeof(NcProd) / sizeof(int));
+      b.m = L.m;
+      b.n = L.n;
+      b.alpha = 1.0;
+      b.optr = tp + offsetof(NcProd, X);
+      b.optr_stride = (int)sizeof(NcProd);
+      cudaEvent_t e0, e1;
+      tc_events(h, L.flops, &e0, &e1);
+      if (e0) cudaEventRecord(e0, st);
+      if ((rc = check_cuda(h, oz_gemm_launch(b, h->tc_err, st), "NC tensor-core Theta"))) return rc;
+      if (e1) cudaEventRecord(e1, st);
+      TEBD_LAUNCHED(h);
+    }
+  }
+  auto mix = h->nc_idf ? k_nc_mix<true> : k_nc_mix<false>;
+  mix<<<dim3(kNormParts, nb), 256, 0, st>>>(h->lab_l, h->lab_r, h->links_d, h->slots_d, w->slots_d, chi, d, N, mf,
+                                            nl);
+  TEBD_LAUNCHED(h);
+  return TEBD_OK;
+}
+
 }  // namespace
 
 int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*truncerr*/) {
@@ -948,36 +1322,39 @@ int run_nc_batch(tebd_handle *h, int nb, const int * /*links_host*/, double * /*
   k_nc_blocks<<<nb, 32, 0, st>>>(h->lab_l, h->lab_r, h->links_d, h->slots_d, w->slots_d, w->probs_d,
                                  chi, d, N, mf, bmax, nl);
   TEBD_LAUNCHED(h);
-  // A = l0 G1 l1 and B = G2 l2 of each bond, once per update, in the slot's V
-  // buffer (they fill 2/d of it; d >= 2 in NC mode): FP64, or double-float in the
-  // precision form
   if (d < 2) return set_error(h, TEBD_ERR_ARG, "NC mode needs d >= 2");
   const bool df = h->opts.svd_mode == TEBD_SVD_DF;
-  if (df)
-    k_nc_scale<true><<<dim3(64, nb), 256, 0, st>>>(h->gam, h->lam, h->links_d, h->slots_d, chi, d);
-  else
-    k_nc_scale<false><<<dim3(64, nb), 256, 0, st>>>(h->gam, h->lam, h->links_d, h->slots_d, chi, d);
-  TEBD_LAUNCHED(h);
-  {
+  std::vector<int> hdr;  // the bonds' headers: sizes for the launch configuration
+  int rc = TEBD_OK;
+  if (zprod_oz(h->theta_form)) {
+    if ((rc = nc_theta_tc(h, w, nb, N, mf, nl, hdr))) return rc;
+  } else {
+    // A = l0 G1 l1 and B = G2 l2 of each bond, once per update, in the slot's V
+    // buffer (they fill 2/d of it; d >= 2 in NC mode): FP64, or double-float in
+    // the precision form
+    if (df)
+      k_nc_scale<true><<<dim3(64, nb), 256, 0, st>>>(h->gam, h->lam, h->links_d, h->slots_d, chi, d);
+    else
+      k_nc_scale<false><<<dim3(64, nb), 256, 0, st>>>(h->gam, h->lam, h->links_d, h->slots_d, chi, d);
+    TEBD_LAUNCHED(h);
     auto kern = h->nc_idf ? (df ? k_nc_theta<true, true> : k_nc_theta<true, false>)
                           : (df ? k_nc_theta<false, true> : k_nc_theta<false, false>);
     kern<<<dim3(kNormParts, nb), 256, 0, st>>>(h->gam, h->lam, h->lab_l, h->lab_r, h->links_d, h->slots_d,
                                                w->slots_d, chi, d, N, mf, nl);
+    TEBD_LAUNCHED(h);
   }
-  TEBD_LAUNCHED(h);
   k_nc_prepare_svd<<<dim3(32, nb), 256, 0, st>>>(w->slots_d, w->probs_d, h->nrm, bmax, h->status_d,
                                                  h->unnormalized);
   TEBD_LAUNCHED(h);
-  // sizes for the launch configuration
-  std::vector<int> hdr((size_t)nb * H_COUNT);
-  for (int s = 0; s < nb; ++s) {
-    int rc = check_cuda(h, cudaMemcpyAsync(hdr.data() + (size_t)s * H_COUNT, w->slots[s].hdr,
-                                           sizeof(int) * H_COUNT, cudaMemcpyDeviceToHost, st),
-                        "read NC header");
-    if (rc) return rc;
+  if (hdr.empty()) {
+    hdr.resize((size_t)nb * H_COUNT);
+    for (int s = 0; s < nb; ++s)
+      if ((rc = check_cuda(h, cudaMemcpyAsync(hdr.data() + (size_t)s * H_COUNT, w->slots[s].hdr,
+                                              sizeof(int) * H_COUNT, cudaMemcpyDeviceToHost, st),
+                           "read NC header")))
+        return rc;
+    if ((rc = check_cuda(h, cudaStreamSynchronize(st), "NC blocks"))) return rc;
   }
-  int rc = check_cuda(h, cudaStreamSynchronize(st), "NC blocks");
-  if (rc) return rc;
   int maxdim = 0, maxsz = 0;
   for (int s = 0; s < nb; ++s) {
     if (hdr[(size_t)s * H_COUNT + H_ERR])

@@ -33,6 +33,7 @@
 
 #include <mutex>
 
+#include "oz_digits.cuh"
 #include "tc_gemm.cuh"
 #include "tc_ptx.cuh"
 
@@ -54,7 +55,6 @@ constexpr int kOzSmemMax = 232448;  // opt-in shared memory per block
 // (bits 7-9, 10-12 = 1), K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
 constexpr uint32_t kIdescBF16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kOzBN >> 3) << 17) |
                                 ((uint32_t)(kTcBM >> 4) << 24);
-constexpr int kExpZero = -2000;  // exponents below this mark an all-zero row
 
 __host__ __device__ constexpr int oz_passes(int S) { return (S + kOzGroups - 1) / kOzGroups; }
 // digit slices pass q reads: 0 .. oz_pass_slices - 1
@@ -312,61 +312,6 @@ finish:
   }
 }
 
-// ---------------------------------------------------------------------------
-// digit extraction
-// ---------------------------------------------------------------------------
-// bf16 bit pattern of an integer |D| <= 128 (exact: at most 8 significant bits)
-__device__ __forceinline__ unsigned short oz_bf16_int(int D) {
-  if (D == 0) return 0;
-  const unsigned a = (unsigned)(D < 0 ? -D : D);
-  const int p = 31 - __clz(a);  // 2^p <= a < 2^(p+1), p <= 7
-  return (unsigned short)((D < 0 ? 0x8000u : 0u) | ((unsigned)(127 + p) << 7) | ((a << (7 - p)) & 0x7fu));
-}
-
-// Digits by integer arithmetic only (the FP64 pipe is the GPU's narrowest; these
-// kernels then run at memory speed).  x = +-m 2^E exactly (m the 53-bit
-// significand), q = rint(m 2^(E + 7S - e)) by a shift with rounding (ties away
-// from zero), |q| < 2^(7S) because |x| < 2^e; then balanced 7-bit digits by
-// integer shifts, rounding to nearest at every step: D_0 in [-128, 128], D_s in
-// [-64, 64] after it, and x - 2^e sum_s D_s 2^(-7(s+1)) = 2^(e - 7S)(x 2^(7S-e) - q),
-// at most 2^(e-7S-1).  Non-finite x and all-zero rows give zero digits.
-__device__ __forceinline__ void oz_digits(double x, int e, int S, unsigned short *d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int ex = (int)((b >> 52) & 0x7ff);
-  if (e <= kExpZero || ex == 0x7ff) {
-    for (int s = 0; s < S; ++s) d[s] = 0;
-    return;
-  }
-  long long m = (long long)(b & 0xfffffffffffffULL);
-  int E = -1074;
-  if (ex) {
-    m |= 1LL << 52;
-    E = ex - 1075;
-  }
-  const int sh = E + 7 * S - e;
-  long long q = sh >= 0 ? (m << sh) : (-sh <= 62 ? ((m + (1LL << (-sh - 1))) >> (-sh)) : 0LL);
-  if (b >> 63) q = -q;
-  for (int s = 0; s < S; ++s) {
-    const int t = 7 * (S - 1 - s);
-    const long long D = t ? ((q + (1LL << (t - 1))) >> t) : q;
-    q -= D << t;
-    d[s] = oz_bf16_int((int)D);
-  }
-}
-
-// |x| as its bit pattern, which orders finite magnitudes; non-finite -> 0
-__device__ __forceinline__ unsigned long long oz_absbits(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
-  return (b >> 52) == 0x7ff ? 0ULL : b;
-}
-
-// e with mag = f 2^e, f in [1/2, 1), from the bit pattern of a positive finite mag
-__device__ __forceinline__ int oz_exp_bits(unsigned long long b) {
-  const int ex = (int)(b >> 52);
-  if (ex) return ex - 1022;
-  return (64 - __clzll((long long)b)) - 1074;  // subnormal: mag = b 2^-1074
-}
-
 // Load a 32 x 32 complex tile of the source as tile[row r][column c] with the
 // same conventions as the TF32 packers: A (trans: element (i, k) at src[k + ld i],
 // else src[i + ld k]); B (element (k, j) at src[j + ld k] if trans, else
@@ -456,51 +401,25 @@ __global__ void __launch_bounds__(256) k_oz_pack(const double2 *src, long long p
 
 // Digits of an operand whose K index is contiguous in memory (A read transposed,
 // element (i, k) at src[k + ld i]; B read as stored, element (k, j) at
-// src[k + ld j]): one warp per row of the packed operand, two passes over that
-// row (largest magnitude, then the digits), coalesced reads and writes, no
-// atomics.  Rows beyond the source extent and K beyond it are packed as zeros.
+// src[k + ld j]): one warp per row of the packed operand (oz_pack_line),
+// coalesced reads and writes, no atomics.  Rows beyond the source extent and K
+// beyond it are packed as zeros.
 template <bool kB>
 __global__ void __launch_bounds__(256) k_oz_pack_rows(const double2 *src, long long pstride, int ld, int r_ext,
                                                       int c_ext, int conj, int nprob, int rows_pad, int k_pad,
                                                       int S, unsigned short *dig, int *exps) {
   const int p = blockIdx.y;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nrow = kB ? rows_pad / 2 : rows_pad;
-  const int r = blockIdx.x * 8 + warp;
+  const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (r >= nrow) return;
-  const bool live = r < r_ext;
   const double2 *row = src + (size_t)p * pstride + (size_t)ld * r;
-  unsigned long long mx = 0;
-  if (live)
-    for (int k = lane; k < c_ext; k += 32) {
-      const double2 v = row[k];
-      mx = max(mx, max(oz_absbits(v.x), oz_absbits(v.y)));
-    }
-  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  const int e = mx ? oz_exp_bits(mx) : (int)0x80808080;
-  if (lane == 0) exps[(size_t)p * nrow + r] = e;
-  const size_t plane = (size_t)nprob * rows_pad * k_pad;
-  for (int k = lane; 2 * k < k_pad; k += 32) {
-    double2 v = make_double2(0.0, 0.0);
-    if (live && k < c_ext) v = row[k];
-    if (conj) v.y = -v.y;
-    unsigned short dr[kOzMaxS], di[kOzMaxS];
-    oz_digits(v.x, e, S, dr);
-    oz_digits(v.y, e, S, di);
-    if (!kB) {
-      unsigned short *o = dig + ((size_t)p * rows_pad + r) * k_pad + 2 * k;
-      for (int q = 0; q < S; ++q)
-        *reinterpret_cast<uint32_t *>(o + q * plane) = (uint32_t)dr[q] | ((uint32_t)di[q] << 16);
-    } else {
-      unsigned short *o0 = dig + ((size_t)p * rows_pad + 2 * r) * k_pad + 2 * k;
-      unsigned short *o1 = o0 + k_pad;
-      for (int q = 0; q < S; ++q) {
-        const unsigned short ni = di[q] ^ 0x8000u;
-        *reinterpret_cast<uint32_t *>(o0 + q * plane) = (uint32_t)dr[q] | ((uint32_t)ni << 16);
-        *reinterpret_cast<uint32_t *>(o1 + q * plane) = (uint32_t)di[q] | ((uint32_t)dr[q] << 16);
-      }
-    }
-  }
+  oz_pack_line<kB>(
+      [&](int k) {
+        double2 x = row[k];
+        if (conj) x.y = -x.y;
+        return x;
+      },
+      r < r_ext, c_ext, p, r, nprob, rows_pad, k_pad, S, dig, exps);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 oz_encode_fn() {

@@ -196,8 +196,8 @@ extern "C" int tebd_set_theta_form(tebd_handle *h, int form) {
   if (!h) return TEBD_ERR_ARG;
   if (!(form == 0 || form == kTc3xTF32 || (form >= 103 && form <= 100 + kOzMaxS)))
     return set_error(h, TEBD_ERR_ARG, "theta form must be 0, 3 (3xTF32) or 103..107 (bf16 digit planes)");
-  if (h->mode != TEBD_MODE_DENSE && form != 0)
-    return set_error(h, TEBD_ERR_STATE, "tensor-core Theta formation is for dense handles");
+  if (h->mode != TEBD_MODE_DENSE && form != 0 && !zprod_oz(form))
+    return set_error(h, TEBD_ERR_STATE, "NC handles take theta form 0 or 103..107 (3xTF32 is for dense handles)");
   h->theta_form = form;
   return TEBD_OK;
 }
