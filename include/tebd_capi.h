@@ -245,12 +245,15 @@ int tebd_mlp_train(tebd_mlp *m, int n, const float *x, const float *t, int epoch
 int tebd_set_rsvd_model(tebd_handle *h, tebd_mlp *m, double target);
 
 /* Theta formation (FormTheta, local_operations_module.f90:184-211) on the tensor
- * cores, dense handles (no counterpart in the reference, which forms Theta in
- * FP64 loops).  form 0: CUDA cores (FP64, or double-float with TEBD_SVD_DF), the
- * default; 3: 3xTF32 split-precision product with FP32 accumulation (~FP32
- * accuracy; the precision tier's Theta); 100 + S, S = 3..7: S bf16 digit planes
- * (error ~2^(-7S) of the largest terms; S = 7 is FP64 class).  ThetaOperation,
- * the SVD and the restoration are unchanged. */
+ * cores (no counterpart in the reference, which forms Theta in FP64 loops).
+ * form 0: CUDA cores (FP64, or double-float with TEBD_SVD_DF), the default; 3:
+ * 3xTF32 split-precision product with FP32 accumulation (~FP32 accuracy; the
+ * precision tier's Theta; dense handles only); 100 + S, S = 3..7: S bf16 digit
+ * planes (error ~2^(-7S) of the largest terms; S = 7 is FP64 class).  On
+ * TEBD_MODE_NC handles (0 or 103..107; 3 gives TEBD_ERR_STATE) FormThetaNC
+ * (:748-818) runs as one product per charge block over its beta class, and
+ * ThetaOperationNC is applied in the blocks afterwards.  ThetaOperation, the SVD
+ * and the restoration are unchanged. */
 int tebd_set_theta_form(tebd_handle *h, int form);
 
 /* Internal degrees of freedom for every NC routine of the handle: the reference

@@ -275,8 +275,9 @@ class Chain:
         self._check(self._lib.tebd_set_rank_bound(self.h, float(bound)))
 
     def set_theta_form(self, form):
-        """Theta formation: 0 CUDA cores (default), 3 = 3xTF32 on the tensor cores,
-        100 + S = S bf16 digit planes on the tensor cores (S = 7: FP64 class)."""
+        """Theta formation: 0 CUDA cores (default), 3 = 3xTF32 on the tensor cores
+        (dense chains), 100 + S = S bf16 digit planes on the tensor cores (S = 7:
+        FP64 class; on number-conserving chains one product per charge block)."""
         self._check(self._lib.tebd_set_theta_form(self.h, int(form)))
 
     def set_rsvd(self, oversample=64, power_iters=2, tol=1e-5, slices=7):
