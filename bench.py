@@ -653,12 +653,13 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "precision_form": prec,
         "mixed_form": mixed,
-        "saturated": saturated_legs(pkg, local, args, fp64_peak) if not args.no_precision else None,
+        "saturated": (saturated_legs(pkg, local, args, fp64_peak)
+                      if not args.no_precision and not args.no_saturated else None),
         "saturated_random_start": (saturated_legs(pkg, local, args, fp64_peak, prepare=False, tune=())
-                                   if not args.no_precision else None),
+                                   if not args.no_precision and not args.no_saturated else None),
         "saturated_chi512": (saturated_legs(pkg, local, args, fp64_peak, steps=1, Ls=32, chi=512, decay=64.0,
                                             tune=("mixed", "mixed_without_model"))
-                             if not args.no_precision and not args.no_chi512 else None),
+                             if not args.no_precision and not args.no_saturated and not args.no_chi512 else None),
         "autotune_table": pkg.get_tuning(local) if not args.no_precision else None,
         **({"rank_form": {"what": "kept-rank form: per-update discarded-weight bound "
                                   "(tebd_set_rank_bound), Lambda beyond the kept rank exactly zero",
@@ -1082,6 +1083,8 @@ def main():
     ap.add_argument("--save-obs", default=None, help="write final <n_i>, bond energies, Lambdas (npz)")
     ap.add_argument("--no-precision", action="store_true", help="skip the precision, mixed and saturated legs")
     ap.add_argument("--no-chi512", action="store_true", help="skip the chi=512 saturated leg")
+    ap.add_argument("--no-saturated", action="store_true",
+                    help="skip the saturated legs (e.g. for the whole 200-step run: --steps 200)")
     ap.add_argument("--rank-bound", type=float, nargs="*", default=None,
                     help="extra legs of the kept-rank form at these discarded-weight bounds (FP64 and "
                          "double-float), with speedup and observable errors against the plain run")
