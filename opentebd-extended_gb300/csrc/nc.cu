@@ -6,6 +6,8 @@
 //   minmaxNLR :1201, SizeOfBlocks :1252, IndexLeft/Right :1339/:1393   -> k_nc_blocks
 //   FormThetaNC :748, ThetaOperationNC :853/:950, RenormThetaNC :1046,
 //   FormBlockTheta :1445                                                -> k_nc_theta
+//     (theta form 103..107: FormThetaNC per charge block on the tensor cores,
+//      k_nc_sizes / k_nc_oz_pack / k_tc_oz, then the rest in k_nc_mix)
 //   SVDNC :1470 (one ZGESVD per block)                                  -> persistent Jacobi
 //                                     (blocks with both sides >= 64: bidiagonalisation)
 //   FlattenSS :1494, Ordering :1515, JudgePosition :1540,

@@ -8,7 +8,8 @@
   1024 x 1024 Thetas);
 * number-conserving Bose-Hubbard L=128, d=5, chi=512, U_i ~ U[1,3] (seed 3),
   dt=0.01, 2nd order, from the Mott state: three steps (573 updates), labels
-  compared exactly.
+  compared exactly -- in plain FP64 and in the mixed form (charge blocks of
+  Theta on the tensor cores, double-float block SVDs).
 
 The oracle runs each sweep's bonds on all host cores (oracle/pool.py).  Compared:
 the summed truncation error, every Lambda, <n_i>, every bond energy and the
@@ -104,26 +105,38 @@ def test_fermi_hubbard_chi256_forest_ruth_two_steps(pkg):
 
 
 def test_nc_bose_hubbard_chi512_three_steps(pkg):
+    """Plain FP64, and the mixed form (Theta's charge blocks on the tensor cores,
+    double-float block SVDs) from the same start, both against the oracle."""
     H = pkg.hamiltonians
     L, d, chi, N, dt, steps = 128, 5, 512, 128, 0.01, 3
     gam, lam, ll, lr = H.initial_set_nc(L, d, chi, N)
     Hb = H.bose_hubbard(L, d, 1.0, np.random.default_rng(3).uniform(1.0, 3.0, L))
     U = H.construct_propagators(Hb, dt, 2)
     num = np.diag(np.arange(d, dtype=float))
-    with pkg.Chain(L, d, chi, mode=pkg.MODE_NC, tot_num=N) as c:
+    forms = {"fp64": (pkg.SVD_FP64, 0), "mixed": (pkg.SVD_DF, 107)}
+    chains = {}
+    for name, (svd, theta) in forms.items():
+        c = pkg.Chain(L, d, chi, mode=pkg.MODE_NC, tot_num=N, svd_mode=svd)
+        c.set_theta_form(theta)
         c.set_state(gam, lam, ll, lr)
         te = sum(c.trotter_step(U, 2) for _ in range(steps))
-        g1, l1, ll1, lr1 = c.get_state()
-        e1 = c.local_energy(Hb)
+        chains[name] = (c, te, c.get_state(), c.local_energy(Hb))
+    try:
         with SweepPool() as P:
             rte = sum(P.trotter_step_nc(gam, lam, ll, lr, U, N, d - 1, 2) for _ in range(steps))
-        e0, ov = _device_obs(pkg, L, d, chi, (gam, lam, ll, lr), None, Hb, c, mode=pkg.MODE_NC, tot_num=N)
-    for link, (a, b) in enumerate(zip(ll1, ll), start=1):
-        assert np.array_equal(a, b), ("label_left", link)
-    for link, (a, b) in enumerate(zip(lr1, lr), start=1):
-        assert np.array_equal(a, b), ("label_right", link)
-    assert max(int(np.sum(x > 0)) for x in l1) > 4  # several charge blocks per bond by now
-    dev = {"truncerr": abs(te - rte), "lambda": _lam_dev(l1, lam),
-           "n_i": float(np.max(np.abs(obs.one_site_expval(g1, l1, num) - obs.one_site_expval(gam, lam, num)))),
-           "bond_energy": float(np.max(np.abs(e1 - e0))), "overlap": abs(abs(ov) - 1.0)}
-    _report(dev, {"truncerr": 1e-10, "lambda": 1e-10, "n_i": 1e-10, "bond_energy": 1e-10, "overlap": 1e-10})
+        for name, (c, te, (g1, l1, ll1, lr1), e1) in chains.items():
+            e0, ov = _device_obs(pkg, L, d, chi, (gam, lam, ll, lr), None, Hb, c, mode=pkg.MODE_NC, tot_num=N)
+            for link, (a, b) in enumerate(zip(ll1, ll), start=1):
+                assert np.array_equal(a, b), (name, "label_left", link)
+            for link, (a, b) in enumerate(zip(lr1, lr), start=1):
+                assert np.array_equal(a, b), (name, "label_right", link)
+            assert max(int(np.sum(x > 0)) for x in l1) > 4  # several charge blocks per bond by now
+            dev = {"truncerr": abs(te - rte), "lambda": _lam_dev(l1, lam),
+                   "n_i": float(np.max(np.abs(obs.one_site_expval(g1, l1, num) -
+                                              obs.one_site_expval(gam, lam, num)))),
+                   "bond_energy": float(np.max(np.abs(e1 - e0))), "overlap": abs(abs(ov) - 1.0)}
+            _report(dev, {"truncerr": 1e-10, "lambda": 1e-10, "n_i": 1e-10, "bond_energy": 1e-10,
+                          "overlap": 1e-10})
+    finally:
+        for c, *_ in chains.values():
+            c.close()
