@@ -50,7 +50,8 @@ J, U, MU, DT, ORDER = 1.0, 2.0, 0.0, 0.005, 2
 AMP, SEED = 1e-3, 1
 UPDATES_PER_STEP = (L // 2) * 2 + (L - 1) // 2  # 32 + 31 + 32 = 95
 METRIC = "two-site updates/sec (Trotter steps/sec = value/95)"
-SVD_MODES = {"fp64": 0, "df": 5, "rsvd": 6}  # plain FP64 / double-float / randomized (learned-rank) route
+SVD_MODES = {"fp64": 0, "df": 5, "rsvd": 6,  # plain FP64 / double-float / randomized (learned-rank) route
+             "jacobi": 2, "bidiag": 3, "qrj": 4}  # the FP64 routes forced for every bond (route comparisons)
 WORKLOAD = "bose_hubbard_L64_d5_chi128_fp64_trotter2"
 
 
@@ -603,37 +604,44 @@ def run_ours(args):
                          "C restatement of TwoSiteOp_c (naive loops) + LAPACK ZGESVD, 1 thread, %.1f s"
                          % (len(links), ",".join(map(str, links)), wall)}
 
-    # ---- roofline of the dominant kernel: the bidiagonalisation, FP64 pipe ----
-    nl = max(1, st["gebrd_launches"])
-    flops_launch = st["gebrd_flops"] / nl
-    achieved = st["gebrd_flops"] / (st["gebrd_ms"] / 1e3) / 1e12 if st["gebrd_ms"] > 0 else None
-    roof = {
-        "kernel": "k_gebrd", "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-        "frac": (achieved / fp64_peak) if achieved else None,
-        "traffic": None,
-        "peak_source": "measured FP64 FMA throughput of this GPU (tebd_measure_fp64_peak); "
-                       "MEASURED_PEAKS.json carries no FP64 figure",
-        "algorithmic": "16 M N^2 - 16 N^3/3 real flops per bond (complex Householder bidiagonalisation, M >= N)",
-        "flops_per_launch": flops_launch, "launches": st["gebrd_launches"],
-        "avg_launch_ms": st["gebrd_ms"] / nl, "share_of_timed": st["gebrd_ms"] / ms if ms > 0 else None,
-        "traffic_source": "not measured for this window: DRAM traffic comes only from an ncu capture, "
-                          "never from a run that is timed",
-        "bidiag_route_share_of_timed": st["bidiag_ms"] / ms if ms > 0 else None,
-        "qrj": {"kernel": "k_jacobi_persistent<double>",
-                "achieved": st["jacobi_flops"] / (st["jacobi_ms"] / 1e3) / 1e12 if st["jacobi_ms"] > 0 else None,
-                "share_of_timed": (st["jacobi_ms"] + st["qr_ms"]) / ms if ms > 0 else None},
-    }
+    # ---- roofline of the dominant kernel (FP64 pipe): the bidiagonalisation when
+    # the window's batches take the bidiagonal route, else the QR route's Jacobi --
+    def fp64_roof(kernel, t_ms, flops, launches, algorithmic):
+        nl = max(1, launches)
+        achieved = flops / (t_ms / 1e3) / 1e12 if t_ms > 0 else None
+        return {"kernel": kernel, "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": (achieved / fp64_peak) if achieved else None, "traffic": None,
+                "peak_source": "measured FP64 FMA throughput of this GPU (tebd_measure_fp64_peak); "
+                               "MEASURED_PEAKS.json carries no FP64 figure",
+                "algorithmic": algorithmic, "flops_per_launch": flops / nl, "launches": launches,
+                "avg_launch_ms": t_ms / nl, "share_of_timed": t_ms / ms if ms > 0 else None,
+                "traffic_source": "not measured for this window: DRAM traffic comes only from an ncu capture, "
+                                  "never from a run that is timed"}
+
+    gebrd_roof = fp64_roof("k_gebrd", st["gebrd_ms"], st["gebrd_flops"], st["gebrd_launches"],
+                           "16 M N^2 - 16 N^3/3 real flops per bond (complex Householder bidiagonalisation, "
+                           "M >= N)")
+    jacobi_roof = fp64_roof("k_jacobi_persistent<double>", st["jacobi_ms"], st["jacobi_flops"],
+                            st["jacobi_launches"],
+                            "counted on the device: 16 m per visited column pair (three complex dot products "
+                            "over m rows) + 20 (m + n) per rotated pair (the 2 x 2 rotation of X's and V's "
+                            "columns)")
+    roof = dict(gebrd_roof if st["gebrd_ms"] >= st["jacobi_ms"] else jacobi_roof)
+    roof["bidiag_route_share_of_timed"] = st["bidiag_ms"] / ms if ms > 0 else None
+    roof["qr_route_share_of_timed"] = (st["jacobi_ms"] + st["qr_ms"]) / ms if ms > 0 else None
+    roof["other"] = jacobi_roof if roof["kernel"] == "k_gebrd" else gebrd_roof
     clocks = clk.summary()
     out = {
         "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "c128 (f64)" if args.svd == "fp64" else "c128 (f64; bidiagonalisation passes in double-float)",
+        "dtype": "c128 (f64; bidiagonalisation passes in double-float)" if args.svd == "df" else "c128 (f64)",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "L": L, "d": D, "chi": CHI, "J": J, "U": U, "mu": MU, "dt": DT,
                    "trotter_order": ORDER, "updates_per_step": UPDATES_PER_STEP,
-                   "svd": "fp64 per bond: Householder bidiagonalisation + bisection + inverse iteration "
-                          "(both compacted dimensions >= 64), else pivoted QR + one-sided Jacobi on R^H",
+                   "svd": ("fp64 per bond: Householder bidiagonalisation + bisection + inverse iteration "
+                           "(both compacted dimensions >= 64), else pivoted QR + one-sided Jacobi on R^H"
+                           if args.svd == "fp64" else "svd_mode %s for every bond" % args.svd),
                    "timed_window": "Trotter steps 1..%d of the configured 200-step run (warm-up on a copy)" % args.steps,
                    "bidiag_updates": st["bidiag_updates"], "updates": st["updates"],
                    "mean_svd_cols": st["compact_cols"] / max(1, st["updates"]),

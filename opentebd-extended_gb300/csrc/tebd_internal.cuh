@@ -121,6 +121,7 @@ constexpr int kPathBidiag = 1;   // bidiagonalisation + bisection + inverse iter
 constexpr int kPathBidiagT = 2;  // the same on Theta^H, for a wide compacted Theta (m < n)
 constexpr int kPathRsvd = 3;     // randomized sketch + Rayleigh-Ritz (rsvd.cu), full SVD as fallback
 constexpr int kBidiagMinDim = 64;  // default route switch: min(m, n) of the compacted Theta
+constexpr int kQrjMaxDim = 384;    // a batch of unsaturated bonds up to this min(m, n) keeps the QR route
 
 // learned model (mlp.cu): sizes and the relative ranks k / chi of its outputs
 constexpr int kMlpIn = 67, kMlpHidden = 128, kMlpOut = 8;
