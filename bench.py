@@ -640,7 +640,8 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "L": L, "d": D, "chi": CHI, "J": J, "U": U, "mu": MU, "dt": DT,
                    "trotter_order": ORDER, "updates_per_step": UPDATES_PER_STEP,
                    "svd": ("fp64 per bond: Householder bidiagonalisation + bisection + inverse iteration "
-                           "(both compacted dimensions >= 64), else pivoted QR + one-sided Jacobi on R^H"
+                           "(both compacted dimensions >= 64 in a batch holding a saturated bond or one above "
+                           "384 columns), else pivoted QR + one-sided Jacobi on R^H"
                            if args.svd == "fp64" else "svd_mode %s for every bond" % args.svd),
                    "timed_window": "Trotter steps 1..%d of the configured 200-step run (warm-up on a copy)" % args.steps,
                    "bidiag_updates": st["bidiag_updates"], "updates": st["updates"],

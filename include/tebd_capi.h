@@ -70,8 +70,9 @@ extern "C" {
 /* SVD algorithm (all FP64 but the precision form) */
 #define TEBD_SVD_FP64 0           /* default: per bond, bidiagonalisation when both
                                      dimensions of the compacted Theta are >= 64 (a wide
-                                     one as Theta^H), else column-pivoted QR + one-sided
-                                     Jacobi on R^H                                       */
+                                     one as Theta^H) and its batch holds a saturated bond
+                                     (all chi of its Lambda in use) or one above 384,
+                                     else column-pivoted QR + one-sided Jacobi on R^H    */
 #define TEBD_SVD_JACOBI 2         /* one-sided Jacobi on the whole (compacted) Theta    */
 #define TEBD_SVD_BIDIAG 3         /* bidiagonalisation for every Theta (>= 2 x 2)       */
 #define TEBD_SVD_QRJ 4            /* pivoted QR + Jacobi on R^H for every bond          */
