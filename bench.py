@@ -26,6 +26,16 @@ precision_form: the same K steps again with the precision form of the SVD
        (TEBD_SVD_DF), its updates/s, the ratio to the plain FP64 value and the
        largest differences of the final <n_i>, bond energies and entropies
        (the metric's "mixed vs plain FP64 at error <= 1e-8"); --no-precision skips it.
+mixed_form: the same K steps in the mixed form (TEBD_SVD_RSVD + tensor-core Theta
+       + the trained model), with the same comparisons.
+saturated, saturated_random_start, saturated_chi512: batched sweeps over
+       saturated bonds (chi = 128 prepared / from a random state, chi = 512) in
+       plain FP64, the mixed form and the mixed form without the model (the A/B
+       of what the network gains), each with its observable errors and the
+       tensor-core products' roofline; --no-saturated / --no-chi512 skip them.
+roofline: the window's dominant FP64 kernel by CUDA-event time (the QR route's
+       Jacobi or the bidiagonalisation), achieved flops against the measured FP64
+       peak; cpu_baseline: the oracle on one core for a bounded sample.
 --impl reference: the reference's CPU algorithm (the C restatement in oracle/,
        naive FormTheta/ThetaOperation loops + LAPACK ZGESVD) on all host cores,
        one bond update per core per step.
