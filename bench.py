@@ -8,8 +8,9 @@ entry, renormalised.  One step = one Trotter step = 95 bond updates (32 odd +
 31 even + 32 odd, each sweep batched on the GPU).  Data are synthetic (the
 reference has no dataset); the configuration is the one the metric is quoted on.
 
-A bench run is the configured run itself: K Trotter steps (default 200, the whole
-configuration) from the initial state, after W warm-up steps on a copy.
+A bench run is the configured run itself: K Trotter steps from the initial state
+(default 20, steps 1..20, about a second of timed work; --steps 200 runs the whole
+configuration), after W warm-up steps (default 5) on a copy.
 value: updates/s with the chain resident in HBM: CUDA events on the library's
        stream around exactly the K steps (one more event per step gives the
        per-step costs: early steps are cheap, the chain saturates chi = 128 near
@@ -1087,8 +1088,8 @@ def run_zgemm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "nc", "saturated", "fermi_hubbard", "spin1", "zgemm"])
